@@ -1,0 +1,136 @@
+/*
+ * rajzel_gb300.h -- C ABI of the GB300 forward + adjoint Eikonal engine.
+ *
+ * Drop-in for RAJZEL's hot path: the shot loop of grad_obj()/forward() and
+ * the solvers eikonal()/eikonal_adj() (reference fd.h:60,62,68,72 and
+ * grad_obj.c:10-81).  Plain C types only; every call returns an RZ_* status
+ * (the reference aborts through err()/MPI_Abort instead, util.c:7-17).
+ *
+ * Conventions (identical to the reference's data, only the container
+ * differs):
+ *   - fields are row-major [ny][nx] float32, x fastest: cell (h,k) at
+ *     k*nx+h, i.e. the memory order of the reference's NR matrix A[k+1][h+1]
+ *     (util.c:177-203) with the row pointers dropped;
+ *   - source positions are metres, like srcpos[1][s] (x) and srcpos[2][s]
+ *     (depth) (sources.c:68-69); the grid index is iround(x/DH)
+ *     (eikonal.c:31-32);
+ *   - receiver positions are the reference's 1-based grid indices,
+ *     recpos[1][i] (x) and recpos[2][i] (depth) (receiver.c:55-56);
+ *   - rz_grid carries the process globals the path reads (NX, NY, DH, TIME,
+ *     TTNORM, EPS_ADJ; globvar.h:12-15,96).
+ *
+ * Pointers are host pointers unless RZ_DEVICE_PTRS is passed in `flags`, in
+ * which case every array argument of that call is a device pointer on the
+ * context's device and the call returns without synchronising (results are
+ * valid once the context stream reaches them).
+ *
+ * Threading: one context per host thread at a time; contexts are independent.
+ */
+#ifndef RAJZEL_GB300_H
+#define RAJZEL_GB300_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RZ_ABI_VERSION 1
+
+/* status codes */
+#define RZ_OK 0
+#define RZ_EINVAL 1          /* bad argument (the reference would read out of bounds or spin) */
+#define RZ_ENOCONV 2         /* TTNORM not met within rz_grid.max_passes outer passes */
+#define RZ_ECUDA 3           /* CUDA runtime/driver error (see rz_last_error) */
+#define RZ_ENOMEM 4          /* device allocation failed */
+#define RZ_ETIMEOUT 5        /* a bounded device-side wait gave up (kernel returned cleanly) */
+#define RZ_ESTATE 6          /* call order: grid/model/receivers not set */
+#define RZ_EUNSUPPORTED 7    /* grid shape beyond this build's kernel limits */
+
+/* arithmetic modes */
+#define RZ_MODE_REFERENCE 0  /* bit-identical to the reference's float/double arithmetic */
+#define RZ_MODE_FAST 1       /* FP32 sweeps, FP64 misfit and gradient stack */
+
+/* flags */
+#define RZ_DEVICE_PTRS 1
+
+typedef struct rz_context rz_context;
+
+/* The reference globals the hot path reads. */
+typedef struct {
+    int nx;          /* NX */
+    int ny;          /* NY */
+    float dh;        /* DH [m] */
+    float time;      /* TIME: 2*TIME initialises traveltimes, 10*TIME lambda */
+    float ttnorm;    /* TTNORM: stop when mean |change| < TTNORM; must be > 0 */
+    float eps_adj;   /* EPS_ADJ: adjoint water level */
+    int max_passes;  /* outer-pass limit (the reference loops forever); <=0 -> 10000 */
+} rz_grid;
+
+int rz_abi_version(void);
+const char *rz_strerror(int status);
+
+/* Context on CUDA device `device` (owns all device memory it allocates). */
+int rz_create(rz_context **ctx, int device);
+void rz_destroy(rz_context *ctx);
+const char *rz_last_error(const rz_context *ctx);
+
+/* cudaStream_t to issue work on (NULL = the context's own stream). */
+int rz_set_stream(rz_context *ctx, void *cuda_stream);
+/* RZ_MODE_REFERENCE (default) or RZ_MODE_FAST. */
+int rz_set_mode(rz_context *ctx, int mode);
+
+/* Grid and solver constants (replaces the globals NX..EPS_ADJ). */
+int rz_set_grid(rz_context *ctx, const rz_grid *grid);
+
+/* Slowness model S [ny][nx] (the S matrix of eikonal(), fd.h:60). */
+int rz_set_slowness(rz_context *ctx, const float *S, int flags);
+/* Velocity model; S = 1/vp per cell as calc_S.c:21 (float division). */
+int rz_set_velocity(rz_context *ctx, const float *vp, int flags);
+
+/* Receiver geometry shared by all shots: ntr receivers at 1-based grid
+   indices (recpos[1..2][1..ntr] of receiver.c).  Host pointers. */
+int rz_set_receivers(rz_context *ctx, int ntr, const int *recx, const int *recz);
+
+/* forward(): traveltimes for nshots sources (forward.c:19-24 over
+   eikonal(), eikonal.c:10-76).
+     srcx, srcz : [nshots] metres (host pointers)
+     TT         : [nshots][ny][nx] or NULL
+     Tmod       : [nshots][ntr]   or NULL (calc_FA.c:15-18)
+     passes     : [nshots] outer passes per shot or NULL (host pointer) */
+int rz_forward(rz_context *ctx, int nshots, const float *srcx, const float *srcz, float *TT, float *Tmod,
+               int *passes, int flags);
+
+/* grad_obj(): misfit and stacked gradient over nshots sources on one GPU
+   (grad_obj.c:27-73 with sum_grad_MPI/MPI_Allreduce replaced by the
+   in-device shot stack; preconditioning not applied).
+     Tobs : [nshots][ntr] observed picks; Tobs<0 mutes a pick (calc_FA_res.c:39)
+     grad : [ny][nx] stacked gradient
+     L2   : misfit 0.5*sum(Tres^2) (grad_obj.c:61)
+   A muted pick contributes a zero residual. */
+int rz_grad_obj(rz_context *ctx, int nshots, const float *srcx, const float *srcz, const float *Tobs, float *grad,
+                double *L2, int flags);
+
+/* Per-shot results of the last rz_forward/rz_grad_obj (host pointers, any
+   may be NULL): outer passes of forward/adjoint, device status bits. */
+int rz_shot_info(rz_context *ctx, int shot, int *fwd_passes, int *adj_passes, int *status);
+
+/* Fields of shot `shot` from the last rz_grad_obj: TT, lambda [ny][nx],
+   Tres [ntr] (scaled residuals as passed to eikonal_adj). */
+int rz_shot_fields(rz_context *ctx, int shot, float *TT, float *lam, float *Tres, int flags);
+
+/* Diagnostics: device time stamps (ns, %globaltimer) of shot `shot` in the
+   last batch: [0] start, [1] forward converged, [2] residuals done,
+   [3] adjoint prepared, [4] adjoint converged, [5] first forward sweep done,
+   [6] first adjoint sweep done, [7] unused.  stamps has 8 entries. */
+int rz_shot_timeline(rz_context *ctx, int shot, unsigned long long *stamps);
+
+/* eikonal(): one source -> TT [ny][nx] and Tmod [ntr] (eikonal.c:10-76). */
+int rz_eikonal(rz_context *ctx, float srcx, float srcz, float *TT, float *Tmod, int *passes, int flags);
+
+/* eikonal_adj(): adjoint field lam [ny][nx] for a given traveltime field
+   TT [ny][nx] and scaled residuals Tres [ntr] (eikonal_adj.c:10-59). */
+int rz_eikonal_adj(rz_context *ctx, const float *TT, const float *Tres, float *lam, int *passes, int flags);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

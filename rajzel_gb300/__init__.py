@@ -1,0 +1,228 @@
+"""rajzel_gb300 -- GB300-native forward + adjoint Eikonal engine for RAJZEL.
+
+Python mirror of the C ABI in ``include/rajzel_gb300.h`` (ctypes over the
+in-tree ``librajzel_gb300.so``).  Names follow the reference's C entry points:
+
+    ctx = Context(device=0)
+    ctx.set_grid(nx, ny, dh, time, ttnorm, eps_adj)     # the reference globals
+    ctx.set_velocity(vp)  or  ctx.set_slowness(S)       # calc_S.c
+    ctx.set_receivers(recx, recz)                       # 1-based grid indices
+    TT, Tmod, passes = ctx.eikonal(srcx, srcz)          # eikonal()
+    lam, passes = ctx.eikonal_adj(TT, Tres)             # eikonal_adj()
+    TT, Tmod, passes = ctx.forward(srcx[], srcz[])      # forward()
+    grad, L2 = ctx.grad_obj(srcx[], srcz[], Tobs)       # grad_obj()
+
+Fields are numpy float32 arrays shaped [ny][nx] (row-major, x fastest), the
+memory order of the reference's NR matrices.  There is no CPU fallback: the
+CUDA library must be built (``python -m rajzel_gb300.build``) and a CUDA
+device present, or the calls raise.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "librajzel_gb300.so")
+
+RZ_OK, RZ_EINVAL, RZ_ENOCONV, RZ_ECUDA, RZ_ENOMEM, RZ_ETIMEOUT, RZ_ESTATE, RZ_EUNSUPPORTED = range(8)
+RZ_MODE_REFERENCE, RZ_MODE_FAST = 0, 1
+RZ_DEVICE_PTRS = 1
+
+MAX_NY = 512  # rows per shot handled by one CTA in this build
+
+
+class RajzelError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"[{status}] {msg}")
+        self.status = status
+
+
+class _Grid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("dh", C.c_float), ("time", C.c_float),
+                ("ttnorm", C.c_float), ("eps_adj", C.c_float), ("max_passes", C.c_int)]
+
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(f"{path} is missing: build it with `python -m rajzel_gb300.build`")
+    lib = C.CDLL(path)
+    vp = C.c_void_p
+    lib.rz_abi_version.restype = C.c_int
+    lib.rz_strerror.restype = C.c_char_p
+    lib.rz_strerror.argtypes = [C.c_int]
+    lib.rz_create.argtypes = [C.POINTER(vp), C.c_int]
+    lib.rz_destroy.argtypes = [vp]
+    lib.rz_destroy.restype = None
+    lib.rz_last_error.argtypes = [vp]
+    lib.rz_last_error.restype = C.c_char_p
+    lib.rz_set_stream.argtypes = [vp, vp]
+    lib.rz_set_mode.argtypes = [vp, C.c_int]
+    lib.rz_set_grid.argtypes = [vp, C.POINTER(_Grid)]
+    lib.rz_set_slowness.argtypes = [vp, vp, C.c_int]
+    lib.rz_set_velocity.argtypes = [vp, vp, C.c_int]
+    lib.rz_set_receivers.argtypes = [vp, C.c_int, vp, vp]
+    lib.rz_forward.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, C.c_int]
+    lib.rz_grad_obj.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, C.c_int]
+    lib.rz_shot_info.argtypes = [vp, C.c_int, vp, vp, vp]
+    lib.rz_shot_fields.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int]
+    lib.rz_eikonal.argtypes = [vp, C.c_float, C.c_float, vp, vp, vp, C.c_int]
+    lib.rz_shot_timeline.argtypes = [vp, C.c_int, vp]
+    lib.rz_eikonal_adj.argtypes = [vp, vp, vp, vp, vp, C.c_int]
+    for name in ("rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
+                 "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
+                 "rz_eikonal_adj", "rz_shot_timeline"):
+        getattr(lib, name).restype = C.c_int
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+class Context:
+    """One GPU engine instance (owns device buffers and a CUDA stream)."""
+
+    def __init__(self, device: int = 0, mode: str = "reference"):
+        self.lib = load_library()
+        h = C.c_void_p()
+        st = self.lib.rz_create(C.byref(h), int(device))
+        if st != RZ_OK:
+            raise RajzelError(st, f"rz_create(device={device}) failed: {self.lib.rz_strerror(st).decode()}")
+        self.h = h
+        self.nx = self.ny = 0
+        self.ntr = 0
+        self.set_mode(mode)
+
+    # -- plumbing -----------------------------------------------------------
+    def _check(self, st, what):
+        if st != RZ_OK:
+            msg = self.lib.rz_last_error(self.h).decode(errors="replace")
+            raise RajzelError(st, f"{what}: {self.lib.rz_strerror(st).decode()}: {msg}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.rz_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream_handle: int | None):
+        self._check(self.lib.rz_set_stream(self.h, C.c_void_p(stream_handle or 0)), "rz_set_stream")
+
+    def set_mode(self, mode):
+        m = {"reference": RZ_MODE_REFERENCE, "fast": RZ_MODE_FAST}.get(mode, mode)
+        self._check(self.lib.rz_set_mode(self.h, int(m)), "rz_set_mode")
+        self.mode = m
+
+    # -- configuration (the reference's globals, model, receivers) ----------
+    def set_grid(self, nx, ny, dh, time, ttnorm=1e-6, eps_adj=1e-9, max_passes=10000):
+        g = _Grid(int(nx), int(ny), float(dh), float(time), float(ttnorm), float(eps_adj), int(max_passes))
+        self._check(self.lib.rz_set_grid(self.h, C.byref(g)), "rz_set_grid")
+        self.nx, self.ny = int(nx), int(ny)
+
+    def set_slowness(self, S):
+        S = _f32(S)
+        assert S.size == self.nx * self.ny
+        self._check(self.lib.rz_set_slowness(self.h, _ptr(S), 0), "rz_set_slowness")
+
+    def set_velocity(self, vp):
+        vp = _f32(vp)
+        assert vp.size == self.nx * self.ny
+        self._check(self.lib.rz_set_velocity(self.h, _ptr(vp), 0), "rz_set_velocity")
+
+    def set_receivers(self, recx, recz):
+        recx, recz = _i32(recx), _i32(recz)
+        self._check(self.lib.rz_set_receivers(self.h, len(recx), _ptr(recx), _ptr(recz)), "rz_set_receivers")
+        self.ntr = len(recx)
+
+    # -- the hot path -------------------------------------------------------
+    def eikonal(self, srcx, srcz):
+        TT = np.empty((self.ny, self.nx), np.float32)
+        Tmod = np.empty(max(self.ntr, 1), np.float32)
+        p = C.c_int(0)
+        self._check(self.lib.rz_eikonal(self.h, float(srcx), float(srcz), _ptr(TT), _ptr(Tmod), C.byref(p), 0),
+                    "rz_eikonal")
+        return TT, Tmod[: self.ntr], p.value
+
+    def eikonal_adj(self, TT, Tres):
+        TT = _f32(TT)
+        Tres = _f32(Tres) if self.ntr else np.zeros(1, np.float32)
+        lam = np.empty((self.ny, self.nx), np.float32)
+        p = C.c_int(0)
+        self._check(self.lib.rz_eikonal_adj(self.h, _ptr(TT), _ptr(Tres), _ptr(lam), C.byref(p), 0), "rz_eikonal_adj")
+        return lam, p.value
+
+    def forward(self, srcx, srcz, want_tt=True):
+        srcx, srcz = _f32(srcx), _f32(srcz)
+        n = len(srcx)
+        TT = np.empty((n, self.ny, self.nx), np.float32) if want_tt else None
+        Tmod = np.empty((n, max(self.ntr, 1)), np.float32)
+        passes = np.zeros(n, np.int32)
+        self._check(self.lib.rz_forward(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(TT), _ptr(Tmod), _ptr(passes), 0),
+                    "rz_forward")
+        return TT, Tmod[:, : self.ntr], passes
+
+    def grad_obj(self, srcx, srcz, Tobs):
+        srcx, srcz = _f32(srcx), _f32(srcz)
+        n = len(srcx)
+        Tobs = _f32(Tobs).reshape(n, self.ntr)
+        grad = np.empty((self.ny, self.nx), np.float32)
+        L2 = C.c_double(0.0)
+        self._check(self.lib.rz_grad_obj(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(Tobs), _ptr(grad), C.byref(L2), 0),
+                    "rz_grad_obj")
+        return grad, L2.value
+
+    def grad_obj_device(self, srcx, srcz, tobs_ptr: int, grad_ptr: int, l2_ptr: int):
+        """Asynchronous variant on device buffers (RZ_DEVICE_PTRS): Tobs
+        [n][ntr] float32, grad [ny][nx] float32, L2 one float64."""
+        srcx, srcz = _f32(srcx), _f32(srcz)
+        self._check(self.lib.rz_grad_obj(self.h, len(srcx), _ptr(srcx), _ptr(srcz), C.c_void_p(tobs_ptr),
+                                         C.c_void_p(grad_ptr), C.c_void_p(l2_ptr), RZ_DEVICE_PTRS),
+                    "rz_grad_obj(device)")
+
+    def shot_info(self, shot):
+        a, b, s = C.c_int(0), C.c_int(0), C.c_int(0)
+        self._check(self.lib.rz_shot_info(self.h, int(shot), C.byref(a), C.byref(b), C.byref(s)), "rz_shot_info")
+        return a.value, b.value, s.value
+
+    def shot_timeline(self, shot):
+        """Device time stamps (ns) of one shot of the last batch (see rz_shot_timeline)."""
+        out = np.zeros(8, np.uint64)
+        self._check(self.lib.rz_shot_timeline(self.h, int(shot), _ptr(out)), "rz_shot_timeline")
+        return out
+
+    def shot_fields(self, shot):
+        TT = np.empty((self.ny, self.nx), np.float32)
+        lam = np.empty((self.ny, self.nx), np.float32)
+        Tres = np.empty(max(self.ntr, 1), np.float32)
+        self._check(self.lib.rz_shot_fields(self.h, int(shot), _ptr(TT), _ptr(lam), _ptr(Tres), 0), "rz_shot_fields")
+        return TT, lam, Tres[: self.ntr]

@@ -1,0 +1,651 @@
+// rz_api.cu -- implementation of the C ABI declared in include/rajzel_gb300.h.
+//
+// A context owns: the grid constants (the reference's globals), the model
+// (slowness, its two skewed copies, the pow(S,3) table of the reference
+// gradient), the receiver geometry (skewed adjoint skip bits, de-duplicated
+// receiver cells), and per-shot work buffers sized for the largest batch
+// seen so far, with their TMA descriptors.  All work is issued on one CUDA
+// stream.  Host-side validation rejects every input on which the reference
+// would index out of bounds or loop forever.
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "../../include/rajzel_gb300.h"
+#include "rz_internal.h"
+
+using namespace rz;
+
+struct DevBuf {
+    void *p = nullptr;
+    size_t bytes = 0;
+};
+
+struct rz_context {
+    int device = 0;
+    cudaStream_t own = nullptr, st = nullptr;
+    int mode = RZ_MODE_REFERENCE;
+    std::string err;
+
+    // grid
+    bool grid_set = false;
+    rz_grid g{};
+    int nxp = 0, nstrips = 0, nxb = 0, qn = 0;
+    int div_fast = 0;
+    float div_dh = -1.f;
+
+    // model
+    bool model_set = false;
+    float *dS = nullptr, *dSA = nullptr, *dSB = nullptr, *dVp = nullptr;
+    double *dCube = nullptr;
+    bool cube_valid = false;
+    std::vector<float> hS;
+
+    // receivers
+    bool rec_set = false;
+    int ntr = 0, nrcell = 0;
+    int *dRecH = nullptr, *dRecK = nullptr, *dRcH = nullptr, *dRcK = nullptr, *dRcRec = nullptr;
+    uint8_t *dSkip = nullptr;
+    uint32_t *dMA = nullptr, *dMB = nullptr;
+
+    // per-shot buffers
+    int cap = 0;
+    float *dT = nullptr, *dTold = nullptr, *dL = nullptr, *dTA = nullptr, *dTB = nullptr, *dEU = nullptr,
+          *dED = nullptr;
+    float *dTobs = nullptr, *dTmod = nullptr, *dTres = nullptr;
+    double *dl2 = nullptr, *dL2 = nullptr;
+    int *dPf = nullptr, *dPa = nullptr, *dStat = nullptr, *dSrcH = nullptr, *dSrcK = nullptr;
+    unsigned long long *dTl = nullptr;
+    float *dGrad = nullptr;
+    CUtensorMap mTld{}, mTrow{}, mLrow{};
+
+    int last_n = 0;
+    bool last_adj = false;
+};
+
+// ---------------------------------------------------------------------------
+// helpers
+// ---------------------------------------------------------------------------
+static int fail(rz_context *c, int code, const char *fmt, ...) {
+    if (c) {
+        char buf[512];
+        va_list ap;
+        va_start(ap, fmt);
+        vsnprintf(buf, sizeof buf, fmt, ap);
+        va_end(ap);
+        c->err = buf;
+    }
+    return code;
+}
+
+#define CK(call)                                                                                         \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess)                                                                           \
+            return fail(c, e_ == cudaErrorMemoryAllocation ? RZ_ENOMEM : RZ_ECUDA, "%s: %s (%s:%d)", #call, \
+                        cudaGetErrorString(e_), __FILE__, __LINE__);                                     \
+    } while (0)
+
+template <typename T>
+static cudaError_t dalloc(T **p, size_t count) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    if (count == 0) count = 1;
+    return cudaMalloc((void **)p, count * sizeof(T));
+}
+
+template <typename T>
+static void dfree(T *&p) {
+    if (p) cudaFree(p);
+    p = nullptr;
+}
+
+static int iround_pos(float x, float dh) { return (int)std::floor((double)(x / dh) + 0.5); }
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_fn() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
+// 3-D map over [cap][ny][nxp] float fields, logical extent [cap][ny][nx].
+static int make_map(rz_context *c, CUtensorMap *m, float *base, int box_rows) {
+    EncodeTiledFn enc = encode_fn();
+    if (!enc) return fail(c, RZ_ECUDA, "cuTensorMapEncodeTiled entry point unavailable");
+    cuuint64_t dims[3] = {(cuuint64_t)c->g.nx, (cuuint64_t)c->g.ny, (cuuint64_t)c->cap};
+    cuuint64_t strides[2] = {(cuuint64_t)c->nxp * 4, (cuuint64_t)c->nxp * c->g.ny * 4};
+    cuuint32_t box[3] = {(cuuint32_t)kBlk, (cuuint32_t)box_rows, 1};
+    cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+                     CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                     CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return fail(c, RZ_ECUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return RZ_OK;
+}
+
+static void free_batch(rz_context *c) {
+    dfree(c->dT), dfree(c->dTold), dfree(c->dL), dfree(c->dTA), dfree(c->dTB), dfree(c->dEU), dfree(c->dED);
+    dfree(c->dTobs), dfree(c->dTmod), dfree(c->dTres), dfree(c->dl2), dfree(c->dPf), dfree(c->dPa);
+    dfree(c->dStat), dfree(c->dSrcH), dfree(c->dSrcK), dfree(c->dTl);
+    c->cap = 0;
+}
+
+static int ensure_batch(rz_context *c, int n) {
+    if (n <= c->cap) return RZ_OK;
+    free_batch(c);
+    const size_t fs = (size_t)c->g.ny * c->nxp, ss = (size_t)c->nstrips * c->qn * 32,
+                 es = (size_t)c->nstrips * edge_row(c->nxp), nt = (size_t)(c->ntr > 0 ? c->ntr : 1);
+    CK(dalloc(&c->dT, fs * n));
+    CK(dalloc(&c->dTold, fs * n));
+    CK(dalloc(&c->dL, fs * n));
+    CK(dalloc(&c->dTA, ss * n));
+    CK(dalloc(&c->dTB, ss * n));
+    CK(dalloc(&c->dEU, es * n));
+    CK(dalloc(&c->dED, es * n));
+    CK(cudaMemsetAsync(c->dEU, 0, es * n * 4, c->st));
+    CK(cudaMemsetAsync(c->dED, 0, es * n * 4, c->st));
+    CK(dalloc(&c->dTobs, nt * n));
+    CK(dalloc(&c->dTmod, nt * n));
+    CK(dalloc(&c->dTres, nt * n));
+    CK(dalloc(&c->dl2, (size_t)n));
+    CK(dalloc(&c->dPf, (size_t)n));
+    CK(dalloc(&c->dPa, (size_t)n));
+    CK(dalloc(&c->dStat, (size_t)n));
+    CK(dalloc(&c->dSrcH, (size_t)n));
+    CK(dalloc(&c->dSrcK, (size_t)n));
+    CK(dalloc(&c->dTl, (size_t)n * kTimelineSlots));
+    c->cap = n;
+    int r;
+    if ((r = make_map(c, &c->mTld, c->dT, kBoxRows))) return r;
+    if ((r = make_map(c, &c->mTrow, c->dT, 1))) return r;
+    if ((r = make_map(c, &c->mLrow, c->dL, 1))) return r;
+    return RZ_OK;
+}
+
+static int ensure_div(rz_context *c) {
+    if (c->div_dh == c->g.dh) return RZ_OK;
+    unsigned int *dbad = nullptr, hbad = 1;
+    CK(cudaMalloc(&dbad, sizeof(unsigned int)));
+    CK(cudaMemsetAsync(dbad, 0, sizeof(unsigned int), c->st));
+    const float rcp = (float)(1.0 / (double)c->g.dh);
+    CK(launch_check_div(c->g.dh, rcp, dbad, c->st));
+    CK(cudaMemcpyAsync(&hbad, dbad, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    cudaFree(dbad);
+    c->div_fast = (hbad == 0);
+    c->div_dh = c->g.dh;
+    return RZ_OK;
+}
+
+// reference-mode gradient needs pow(S,3.0) exactly as the host C library
+// returns it (ass_grad.c:23); it is faithful but not always correctly rounded
+static int ensure_cube(rz_context *c) {
+    if (c->cube_valid) return RZ_OK;
+    const size_t n = (size_t)c->g.nx * c->g.ny;
+    std::vector<double> cube(n);
+    for (size_t i = 0; i < n; ++i) cube[i] = std::pow((double)c->hS[i], 3.0);
+    CK(dalloc(&c->dCube, n));
+    CK(cudaMemcpyAsync(c->dCube, cube.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    c->cube_valid = true;
+    return RZ_OK;
+}
+
+static bool have_dev(int flags) { return (flags & RZ_DEVICE_PTRS) != 0; }
+
+static void fill_params(rz_context *c, ShotParams &P, int n) {
+    memset(&P, 0, sizeof P);
+    P.nx = c->g.nx;
+    P.ny = c->g.ny;
+    P.nxp = c->nxp;
+    P.nstrips = c->nstrips;
+    P.nxb = c->nxb;
+    P.qn = c->qn;
+    P.dh = c->g.dh;
+    P.time = c->g.time;
+    P.ttnorm = c->g.ttnorm;
+    P.eps_adj = c->g.eps_adj;
+    P.dh_rcp = (float)(1.0 / (double)c->g.dh);
+    P.div_fast = c->div_fast;
+    P.max_passes = c->g.max_passes > 0 ? c->g.max_passes : 10000;
+    P.nshots = n;
+    P.SA = c->dSA;
+    P.SB = c->dSB;
+    P.MA = c->dMA;
+    P.MB = c->dMB;
+    P.T = c->dT;
+    P.Told = c->dTold;
+    P.L = c->dL;
+    P.TA = c->dTA;
+    P.TB = c->dTB;
+    P.EU = c->dEU;
+    P.ED = c->dED;
+    P.fstride = (size_t)c->g.ny * c->nxp;
+    P.sstride = (size_t)c->nstrips * c->qn * 32;
+    P.estride = (size_t)c->nstrips * edge_row(c->nxp);
+    P.src_h = c->dSrcH;
+    P.src_k = c->dSrcK;
+    P.ntr = c->ntr;
+    P.rec_h = c->dRecH;
+    P.rec_k = c->dRecK;
+    P.nrcell = c->nrcell;
+    P.rcell_h = c->dRcH;
+    P.rcell_k = c->dRcK;
+    P.rcell_rec = c->dRcRec;
+    P.Tobs = c->dTobs;
+    P.Tmod = c->dTmod;
+    P.Tres = c->dTres;
+    P.l2 = c->dl2;
+    P.passes_fwd = c->dPf;
+    P.passes_adj = c->dPa;
+    P.status = c->dStat;
+    P.timeline = c->dTl;
+}
+
+static int status_to_code(int bits) {
+    if (bits & 3) return RZ_ETIMEOUT;
+    if (bits & 12) return RZ_ENOCONV;
+    if (bits) return RZ_EINVAL;
+    return RZ_OK;
+}
+
+// upload validated source indices for n shots
+static int set_sources(rz_context *c, int n, const float *srcx, const float *srcz) {
+    if (!srcx || !srcz) return fail(c, RZ_EINVAL, "source arrays are NULL");
+    std::vector<int> hh(n), kk(n);
+    for (int i = 0; i < n; ++i) {
+        int h = iround_pos(srcx[i], c->g.dh) - 1, k = iround_pos(srcz[i], c->g.dh) - 1;
+        if (!(std::isfinite(srcx[i]) && std::isfinite(srcz[i])) || h < 0 || h >= c->g.nx || k < 0 || k >= c->g.ny)
+            return fail(c, RZ_EINVAL, "shot %d: source (%g, %g) m maps to grid index (%d, %d) outside 1..%d x 1..%d", i,
+                        srcx[i], srcz[i], h + 1, k + 1, c->g.nx, c->g.ny);
+        hh[i] = h;
+        kk[i] = k;
+    }
+    CK(cudaMemcpyAsync(c->dSrcH, hh.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    CK(cudaMemcpyAsync(c->dSrcK, kk.data(), n * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    return RZ_OK;
+}
+
+static int ready(rz_context *c, bool need_rec) {
+    if (!c) return RZ_EINVAL;
+    if (!c->grid_set) return fail(c, RZ_ESTATE, "rz_set_grid has not been called");
+    if (!c->model_set) return fail(c, RZ_ESTATE, "no slowness/velocity model set");
+    if (need_rec && !c->rec_set) return fail(c, RZ_ESTATE, "rz_set_receivers has not been called");
+    return RZ_OK;
+}
+
+// copy a [n][ny][nxp] device field batch to a packed [n][ny][nx] destination
+static int copy_out_fields(rz_context *c, const float *src, float *dst, int n, int flags) {
+    const size_t fs = (size_t)c->g.ny * c->nxp;
+    for (int z = 0; z < n; ++z) {
+        CK(cudaMemcpy2DAsync(dst + (size_t)z * c->g.nx * c->g.ny, (size_t)c->g.nx * 4, src + z * fs,
+                             (size_t)c->nxp * 4, (size_t)c->g.nx * 4, c->g.ny,
+                             have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
+    }
+    return RZ_OK;
+}
+
+static int run_batch(rz_context *c, int n, bool adjoint, bool residual, bool start_adj) {
+    int r;
+    if ((r = ensure_div(c))) return r;
+    ShotParams P;
+    fill_params(c, P, n);
+    P.do_residual = residual ? 1 : 0;
+    P.do_adjoint = adjoint ? 1 : 0;
+    P.start_adjoint = start_adj ? 1 : 0;
+    CK(cudaMemsetAsync(c->dStat, 0, n * sizeof(int), c->st));
+    CK(cudaMemsetAsync(c->dTl, 0, (size_t)n * kTimelineSlots * sizeof(unsigned long long), c->st));
+    CK(cudaMemsetAsync(c->dPf, 0, n * sizeof(int), c->st));
+    CK(cudaMemsetAsync(c->dPa, 0, n * sizeof(int), c->st));
+    CK(launch_shot_kernel(P, c->mode, c->mTld, c->mTrow, c->mLrow, c->st));
+    c->last_n = n;
+    c->last_adj = adjoint;
+    return RZ_OK;
+}
+
+static int collect_status(rz_context *c, int n) {
+    std::vector<int> st(n);
+    CK(cudaMemcpyAsync(st.data(), c->dStat, n * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    int worst = 0;
+    for (int i = 0; i < n; ++i) worst |= st[i];
+    int code = status_to_code(worst);
+    if (code != RZ_OK) return fail(c, code, "device status bits 0x%x", worst);
+    return RZ_OK;
+}
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+extern "C" {
+
+int rz_abi_version(void) { return RZ_ABI_VERSION; }
+
+const char *rz_strerror(int s) {
+    switch (s) {
+        case RZ_OK: return "ok";
+        case RZ_EINVAL: return "invalid argument";
+        case RZ_ENOCONV: return "no convergence within max_passes";
+        case RZ_ECUDA: return "CUDA error";
+        case RZ_ENOMEM: return "out of device memory";
+        case RZ_ETIMEOUT: return "device-side wait timed out";
+        case RZ_ESTATE: return "call order: grid/model/receivers not set";
+        case RZ_EUNSUPPORTED: return "unsupported grid shape";
+        default: return "unknown status";
+    }
+}
+
+int rz_create(rz_context **out, int device) {
+    if (!out) return RZ_EINVAL;
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || device < 0 || device >= ndev) return RZ_ECUDA;
+    rz_context *c = new rz_context();
+    c->device = device;
+    if (cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&c->own, cudaStreamNonBlocking) != cudaSuccess) {
+        delete c;
+        return RZ_ECUDA;
+    }
+    c->st = c->own;
+    *out = c;
+    return RZ_OK;
+}
+
+void rz_destroy(rz_context *c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->st) cudaStreamSynchronize(c->st);
+    free_batch(c);
+    dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dVp), dfree(c->dCube), dfree(c->dGrad), dfree(c->dL2);
+    dfree(c->dRecH), dfree(c->dRecK), dfree(c->dRcH), dfree(c->dRcK), dfree(c->dRcRec), dfree(c->dSkip);
+    dfree(c->dMA), dfree(c->dMB);
+    if (c->own) cudaStreamDestroy(c->own);
+    delete c;
+}
+
+const char *rz_last_error(const rz_context *c) { return c ? c->err.c_str() : "no context"; }
+
+int rz_set_stream(rz_context *c, void *stream) {
+    if (!c) return RZ_EINVAL;
+    c->st = stream ? (cudaStream_t)stream : c->own;
+    return RZ_OK;
+}
+
+int rz_set_mode(rz_context *c, int mode) {
+    if (!c) return RZ_EINVAL;
+    if (mode != RZ_MODE_REFERENCE && mode != RZ_MODE_FAST) return fail(c, RZ_EINVAL, "unknown mode %d", mode);
+    c->mode = mode;
+    return RZ_OK;
+}
+
+int rz_set_grid(rz_context *c, const rz_grid *g) {
+    if (!c || !g) return RZ_EINVAL;
+    if (g->nx < 3 || g->ny < 3) return fail(c, RZ_EINVAL, "grid %d x %d: NX and NY must be >= 3", g->nx, g->ny);
+    if (!(g->dh > 0.f) || !std::isfinite(g->dh)) return fail(c, RZ_EINVAL, "DH must be > 0");
+    if (!(g->ttnorm > 0.f))
+        return fail(c, RZ_EINVAL, "TTNORM must be > 0 (the reference never terminates otherwise)");
+    if (!std::isfinite(g->time) || !std::isfinite(g->eps_adj)) return fail(c, RZ_EINVAL, "TIME/EPS_ADJ not finite");
+    const int nstrips = (g->ny + kStrip - 1) / kStrip;
+    if (nstrips > kMaxWarps)
+        return fail(c, RZ_EUNSUPPORTED, "NY=%d exceeds %d rows per shot in this build", g->ny, kMaxWarps * kStrip);
+    cudaSetDevice(c->device);
+    const bool same_shape = c->grid_set && c->g.nx == g->nx && c->g.ny == g->ny;
+    c->g = *g;
+    c->grid_set = true;
+    if (!same_shape) {
+        c->nxb = (g->nx + kBlk - 1) / kBlk;
+        c->nxp = c->nxb * kBlk;
+        c->nstrips = nstrips;
+        c->qn = skew_lines(c->nxb);
+        free_batch(c);
+        c->model_set = false;
+        c->rec_set = false;
+        c->cube_valid = false;
+    }
+    return RZ_OK;
+}
+
+static int set_model_common(rz_context *c) {
+    const int nx = c->g.nx, ny = c->g.ny;
+    const size_t skew = (size_t)c->nstrips * c->qn * 32;
+    if (!c->dSA) {
+        CK(dalloc(&c->dSA, skew));
+        CK(dalloc(&c->dSB, skew));
+    }
+    CK(launch_skew_field(c->dS, nx, ny, nx, c->nstrips, c->nxb, c->dSA, c->dSB, c->st));
+    c->hS.resize((size_t)nx * ny);
+    CK(cudaMemcpyAsync(c->hS.data(), c->dS, (size_t)nx * ny * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (size_t i = 0; i < c->hS.size(); ++i)
+        if (!(c->hS[i] > 0.f) || !std::isfinite(c->hS[i])) {
+            c->model_set = false;
+            return fail(c, RZ_EINVAL, "slowness at cell %zu is not a positive finite number", i);
+        }
+    c->model_set = true;
+    c->cube_valid = false;
+    return RZ_OK;
+}
+
+static int alloc_model(rz_context *c) {
+    const size_t n = (size_t)c->g.nx * c->g.ny;
+    if (!c->dS) CK(dalloc(&c->dS, n));
+    return RZ_OK;
+}
+
+int rz_set_slowness(rz_context *c, const float *S, int flags) {
+    if (!c || !S) return RZ_EINVAL;
+    if (!c->grid_set) return fail(c, RZ_ESTATE, "rz_set_grid first");
+    cudaSetDevice(c->device);
+    // allocations follow the grid; they are dropped when the shape changes
+    if (c->dS && !c->model_set) {
+        dfree(c->dS), dfree(c->dSA), dfree(c->dSB);
+    }
+    int r;
+    if ((r = alloc_model(c))) return r;
+    const size_t n = (size_t)c->g.nx * c->g.ny;
+    CK(cudaMemcpyAsync(c->dS, S, n * 4, have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
+    return set_model_common(c);
+}
+
+int rz_set_velocity(rz_context *c, const float *vp, int flags) {
+    if (!c || !vp) return RZ_EINVAL;
+    if (!c->grid_set) return fail(c, RZ_ESTATE, "rz_set_grid first");
+    cudaSetDevice(c->device);
+    if (c->dS && !c->model_set) {
+        dfree(c->dS), dfree(c->dSA), dfree(c->dSB);
+    }
+    int r;
+    if ((r = alloc_model(c))) return r;
+    const size_t n = (size_t)c->g.nx * c->g.ny;
+    const float *src = vp;
+    if (!have_dev(flags)) {
+        CK(dalloc(&c->dVp, n));
+        CK(cudaMemcpyAsync(c->dVp, vp, n * 4, cudaMemcpyHostToDevice, c->st));
+        src = c->dVp;
+    }
+    CK(launch_calc_s(src, c->dS, (long)n, c->st));
+    return set_model_common(c);
+}
+
+int rz_set_receivers(rz_context *c, int ntr, const int *recx, const int *recz) {
+    if (!c) return RZ_EINVAL;
+    if (!c->grid_set) return fail(c, RZ_ESTATE, "rz_set_grid first");
+    if (ntr < 0 || (ntr > 0 && (!recx || !recz))) return fail(c, RZ_EINVAL, "bad receiver arrays");
+    cudaSetDevice(c->device);
+    const int nx = c->g.nx, ny = c->g.ny;
+    std::vector<int> hh(ntr), kk(ntr);
+    std::vector<uint8_t> skip((size_t)nx * ny, 0);
+    std::map<long, int> last;  // interior receiver cell -> last receiver index
+    for (int i = 0; i < ntr; ++i) {
+        if (recx[i] < 1 || recx[i] > nx || recz[i] < 1 || recz[i] > ny)
+            return fail(c, RZ_EINVAL, "receiver %d at grid index (%d, %d) outside 1..%d x 1..%d", i + 1, recx[i],
+                        recz[i], nx, ny);
+        hh[i] = recx[i] - 1;
+        kk[i] = recz[i] - 1;
+        skip[(size_t)kk[i] * nx + hh[i]] = 1;
+        if (hh[i] > 0 && hh[i] < nx - 1 && kk[i] > 0 && kk[i] < ny - 1) last[(long)kk[i] * nx + hh[i]] = i;
+    }
+    std::vector<int> rh, rk, rr;
+    for (auto &kv : last) {
+        rk.push_back((int)(kv.first / nx));
+        rh.push_back((int)(kv.first % nx));
+        rr.push_back(kv.second);
+    }
+    c->ntr = ntr;
+    c->nrcell = (int)rr.size();
+    CK(dalloc(&c->dRecH, (size_t)ntr));
+    CK(dalloc(&c->dRecK, (size_t)ntr));
+    CK(dalloc(&c->dRcH, rr.size()));
+    CK(dalloc(&c->dRcK, rr.size()));
+    CK(dalloc(&c->dRcRec, rr.size()));
+    CK(dalloc(&c->dSkip, skip.size()));
+    if (ntr) {
+        CK(cudaMemcpyAsync(c->dRecH, hh.data(), ntr * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(c->dRecK, kk.data(), ntr * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    }
+    if (!rr.empty()) {
+        CK(cudaMemcpyAsync(c->dRcH, rh.data(), rr.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(c->dRcK, rk.data(), rr.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(c->dRcRec, rr.data(), rr.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    }
+    CK(cudaMemcpyAsync(c->dSkip, skip.data(), skip.size(), cudaMemcpyHostToDevice, c->st));
+    const size_t lines = (size_t)c->nstrips * c->qn;
+    CK(dalloc(&c->dMA, lines));
+    CK(dalloc(&c->dMB, lines));
+    CK(launch_skip_masks(c->dSkip, nx, ny, c->nstrips, c->nxb, c->dMA, c->dMB, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    free_batch(c);  // receiver-sized buffers follow ntr
+    c->rec_set = true;
+    return RZ_OK;
+}
+
+int rz_forward(rz_context *c, int nshots, const float *srcx, const float *srcz, float *TT, float *Tmod, int *passes,
+               int flags) {
+    int r;
+    if ((r = ready(c, false))) return r;
+    if (nshots < 1) return fail(c, RZ_EINVAL, "nshots must be >= 1");
+    cudaSetDevice(c->device);
+    if (!c->rec_set) {
+        if ((r = rz_set_receivers(c, 0, nullptr, nullptr))) return r;
+    }
+    if ((r = ensure_batch(c, nshots))) return r;
+    if ((r = set_sources(c, nshots, srcx, srcz))) return r;
+    if ((r = run_batch(c, nshots, false, false, false))) return r;
+    if (TT && (r = copy_out_fields(c, c->dT, TT, nshots, flags))) return r;
+    if (Tmod && c->ntr > 0)
+        CK(cudaMemcpyAsync(Tmod, c->dTmod, (size_t)nshots * c->ntr * 4,
+                           have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
+    if (passes) CK(cudaMemcpyAsync(passes, c->dPf, nshots * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    if (have_dev(flags) && !passes) return RZ_OK;
+    return collect_status(c, nshots);
+}
+
+int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *Tobs, float *grad,
+                double *L2, int flags) {
+    int r;
+    if ((r = ready(c, true))) return r;
+    if (nshots < 1 || !Tobs || !grad) return fail(c, RZ_EINVAL, "bad arguments");
+    cudaSetDevice(c->device);
+    if ((r = ensure_batch(c, nshots))) return r;
+    if ((r = set_sources(c, nshots, srcx, srcz))) return r;
+    if (c->mode == RZ_MODE_REFERENCE && (r = ensure_cube(c))) return r;
+    const size_t nt = (size_t)nshots * c->ntr;
+    if (nt) CK(cudaMemcpyAsync(c->dTobs, Tobs, nt * 4, have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
+    if ((r = run_batch(c, nshots, true, true, false))) return r;
+    float *gdst = grad;
+    if (!have_dev(flags)) {
+        if (!c->dGrad) CK(dalloc(&c->dGrad, (size_t)c->g.nx * c->g.ny));
+        gdst = c->dGrad;
+    }
+    CK(launch_stack(c->dL, (size_t)c->g.ny * c->nxp, nshots, c->dCube, c->dS, c->g.nx, c->g.ny, c->nxp, c->mode, gdst,
+                    c->g.nx, nullptr, c->st));
+    CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, c->st));
+    if (!c->dL2) CK(dalloc(&c->dL2, 1));
+    CK(launch_sum_l2(c->dl2, nshots, c->dL2, c->st));
+    if (have_dev(flags)) {
+        if (L2) CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+        return RZ_OK;
+    }
+    CK(cudaMemcpyAsync(grad, gdst, (size_t)c->g.nx * c->g.ny * 4, cudaMemcpyDeviceToHost, c->st));
+    if (L2) CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    return collect_status(c, nshots);
+}
+
+int rz_shot_info(rz_context *c, int shot, int *fwd_passes, int *adj_passes, int *status) {
+    if (!c) return RZ_EINVAL;
+    if (shot < 0 || shot >= c->last_n) return fail(c, RZ_EINVAL, "shot %d not in the last batch", shot);
+    cudaSetDevice(c->device);
+    int v[3] = {0, 0, 0};
+    CK(cudaMemcpyAsync(&v[0], c->dPf + shot, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(&v[1], c->dPa + shot, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaMemcpyAsync(&v[2], c->dStat + shot, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    if (fwd_passes) *fwd_passes = v[0];
+    if (adj_passes) *adj_passes = v[1];
+    if (status) *status = v[2];
+    return RZ_OK;
+}
+
+int rz_shot_fields(rz_context *c, int shot, float *TT, float *lam, float *Tres, int flags) {
+    if (!c) return RZ_EINVAL;
+    if (shot < 0 || shot >= c->last_n) return fail(c, RZ_EINVAL, "shot %d not in the last batch", shot);
+    cudaSetDevice(c->device);
+    const size_t fs = (size_t)c->g.ny * c->nxp;
+    int r;
+    if (TT && (r = copy_out_fields(c, c->dT + shot * fs, TT, 1, flags))) return r;
+    if (lam && (r = copy_out_fields(c, c->dL + shot * fs, lam, 1, flags))) return r;
+    if (Tres && c->ntr)
+        CK(cudaMemcpyAsync(Tres, c->dTres + (size_t)shot * c->ntr, c->ntr * 4,
+                           have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return RZ_OK;
+}
+
+int rz_shot_timeline(rz_context *c, int shot, unsigned long long *stamps) {
+    if (!c || !stamps) return RZ_EINVAL;
+    if (shot < 0 || shot >= c->last_n) return fail(c, RZ_EINVAL, "shot %d not in the last batch", shot);
+    cudaSetDevice(c->device);
+    CK(cudaMemcpyAsync(stamps, c->dTl + (size_t)shot * kTimelineSlots, kTimelineSlots * sizeof(unsigned long long),
+                       cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return RZ_OK;
+}
+
+int rz_eikonal(rz_context *c, float srcx, float srcz, float *TT, float *Tmod, int *passes, int flags) {
+    return rz_forward(c, 1, &srcx, &srcz, TT, Tmod, passes, flags);
+}
+
+int rz_eikonal_adj(rz_context *c, const float *TT, const float *Tres, float *lam, int *passes, int flags) {
+    int r;
+    if ((r = ready(c, true))) return r;
+    if (!TT || !lam || (c->ntr > 0 && !Tres)) return fail(c, RZ_EINVAL, "bad arguments");
+    cudaSetDevice(c->device);
+    if ((r = ensure_batch(c, 1))) return r;
+    const cudaMemcpyKind kin = have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    CK(cudaMemcpy2DAsync(c->dT, (size_t)c->nxp * 4, TT, (size_t)c->g.nx * 4, (size_t)c->g.nx * 4, c->g.ny, kin, c->st));
+    if (c->ntr) CK(cudaMemcpyAsync(c->dTres, Tres, c->ntr * 4, kin, c->st));
+    if ((r = run_batch(c, 1, true, false, true))) return r;
+    if ((r = copy_out_fields(c, c->dL, lam, 1, flags))) return r;
+    if (passes) CK(cudaMemcpyAsync(passes, c->dPa, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    return collect_status(c, 1);
+}
+
+}  // extern "C"

@@ -1,0 +1,340 @@
+// rz_device.cuh -- device-side building blocks for the RAJZEL GB300 kernels:
+// inline-PTX wrappers for TMA (cp.async.bulk.tensor), mbarriers, proxy fences
+// and release/acquire flags, plus the point updates of the forward
+// (Godunov-upwind, sweep.c:89-97) and adjoint (Leung-Qian, sweep_adj.c:33-68)
+// sweeps in two arithmetic modes:
+//   * reference mode: bit-identical to the reference's float/double mix;
+//   * fast mode: plain FP32.
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define RZ_DEV __device__ __forceinline__
+
+namespace rz {
+
+// ---------------------------------------------------------------------------
+// error bits written to the per-shot status word
+// ---------------------------------------------------------------------------
+enum : int {
+    ERR_TMA_TIMEOUT = 1 << 0,    // an mbarrier wait for a TMA load gave up
+    ERR_FLAG_TIMEOUT = 1 << 1,   // a warp-to-warp progress wait gave up
+    ERR_NOCONV_FWD = 1 << 2,     // forward did not meet TTNORM within max passes
+    ERR_NOCONV_ADJ = 1 << 3,     // adjoint did not meet TTNORM within max passes
+    ERR_BAD_SOURCE = 1 << 4,     // source index outside the grid
+};
+
+// Bounded waits.  Legitimate waits in these kernels last microseconds; a
+// wait that exceeds its poll budget records an error bit, raises the CTA's
+// abort word, and every later wait in that CTA returns at once, so a faulty
+// launch still ends within about one budget per CTA.
+constexpr uint32_t kSpinLimit = 1u << 21;
+
+// ---------------------------------------------------------------------------
+// shared-memory address helpers
+// ---------------------------------------------------------------------------
+RZ_DEV uint32_t smem_u32(const void *p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// ---------------------------------------------------------------------------
+// mbarrier
+// ---------------------------------------------------------------------------
+RZ_DEV void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+RZ_DEV void mbar_inval(uint64_t *bar) {
+    asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+RZ_DEV void mbar_arrive_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+RZ_DEV void mbar_arrive(uint64_t *bar) {
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+RZ_DEV bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// the same operations on 32-bit shared-window addresses (kept in registers)
+RZ_DEV void mbar_arrive_a(uint32_t bar) {
+    asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
+}
+RZ_DEV bool mbar_try_wait_a(uint32_t bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.acquire.cta.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait; returns false on timeout or abort (abort word in shared memory).
+RZ_DEV bool mbar_wait_a(uint32_t bar, uint32_t parity, uint32_t abort_word) {
+    if (mbar_try_wait_a(bar, parity)) return true;
+    for (uint32_t i = 0; i < kSpinLimit; ++i) {
+        if (mbar_try_wait_a(bar, parity)) return true;
+        int ab;
+        asm volatile("ld.volatile.shared.b32 %0, [%1];" : "=r"(ab) : "r"(abort_word) : "memory");
+        if (ab) return false;
+    }
+    asm volatile("st.volatile.shared.b32 [%0], %1;" ::"r"(abort_word), "r"(1) : "memory");
+    return false;
+}
+
+// Bounded wait on an mbarrier phase.  Returns false on timeout or abort.
+RZ_DEV bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_word) {
+    for (uint32_t i = 0; i < kSpinLimit; ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if (*abort_word) return false;
+    }
+    *abort_word = 1;
+    return false;
+}
+
+// ---------------------------------------------------------------------------
+// fences
+// ---------------------------------------------------------------------------
+// make this thread's generic-proxy shared-memory writes visible to the async
+// proxy (before a TMA store reads them)
+RZ_DEV void fence_proxy_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+// order generic-proxy global accesses with later/earlier async-proxy (TMA)
+// accesses to global memory
+RZ_DEV void fence_proxy_async_global() { asm volatile("fence.proxy.async.global;" ::: "memory"); }
+
+// ---------------------------------------------------------------------------
+// TMA: 3-D tiled tensor copies (x = column, y = row, z = shot slot)
+// ---------------------------------------------------------------------------
+RZ_DEV void tma_load_3d(void *smem_dst, const CUtensorMap *map, int x, int y, int z, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_u32(smem_dst)),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+RZ_DEV void tma_store_3d(const CUtensorMap *map, int x, int y, int z, const void *smem_src) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                     (uint64_t)map),
+                 "r"(x), "r"(y), "r"(z), "r"(smem_u32(smem_src))
+                 : "memory");
+}
+// the same copies with 32-bit shared-window addresses
+RZ_DEV void tma_load_3d_a(uint32_t smem_dst, const CUtensorMap *map, int x, int y, int z, uint32_t bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes"
+        " [%0], [%1, {%2, %3, %4}], [%5];" ::"r"(smem_dst),
+        "l"((uint64_t)map), "r"(x), "r"(y), "r"(z), "r"(bar)
+        : "memory");
+}
+RZ_DEV void tma_store_3d_a(const CUtensorMap *map, int x, int y, int z, uint32_t smem_src) {
+    asm volatile("cp.async.bulk.tensor.3d.global.shared::cta.tile.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+                     (uint64_t)map),
+                 "r"(x), "r"(y), "r"(z), "r"(smem_src)
+                 : "memory");
+}
+RZ_DEV void mbar_arrive_expect_tx_a(uint32_t bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+                 : "memory");
+}
+RZ_DEV void tma_store_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+// wait until at most N committed store groups are still reading shared memory
+template <int N>
+RZ_DEV void tma_store_wait_read() {
+    asm volatile("cp.async.bulk.wait_group.read %0;" ::"n"(N) : "memory");
+}
+// wait until at most N committed store groups are still incomplete
+template <int N>
+RZ_DEV void tma_store_wait_all() {
+    asm volatile("cp.async.bulk.wait_group %0;" ::"n"(N) : "memory");
+}
+RZ_DEV void tma_prefetch_desc(const CUtensorMap *map) {
+    asm volatile("prefetch.tensormap [%0];" ::"l"((uint64_t)map) : "memory");
+}
+
+// ---------------------------------------------------------------------------
+// release/acquire flags in this CTA's shared memory
+// ---------------------------------------------------------------------------
+RZ_DEV void st_release_smem(int *p, int v) {
+    asm volatile("st.release.cta.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(p)), "r"(v) : "memory");
+}
+RZ_DEV int ld_acquire_smem(const int *p) {
+    int v;
+    asm volatile("ld.acquire.cta.shared::cta.b32 %0, [%1];" : "=r"(v) : "r"(smem_u32(p)) : "memory");
+    return v;
+}
+// Bounded wait until *flag >= need.  Returns false on timeout or abort.
+// Hand-off waits are short and frequent (a consumer warp trails its producer
+// by a few dozen steps), so the first polls spin; only a long wait backs off
+// with __nanosleep, whose wake-up latency is microseconds.
+RZ_DEV bool wait_flag_ge(const int *flag, int need, volatile int *abort_word) {
+    for (int i = 0; i < 2048; ++i)
+        if (ld_acquire_smem(flag) >= need) return true;
+    uint32_t ns = 32;
+    for (uint32_t i = 0; i < kSpinLimit; ++i) {
+        __nanosleep(ns);
+        if (ns < 256) ns <<= 1;
+        if (ld_acquire_smem(flag) >= need) return true;
+        if (*abort_word) return false;
+    }
+    *abort_word = 1;
+    return false;
+}
+
+// read-only global load that bypasses L1 allocation rules for streaming data
+RZ_DEV float ldg_nc(const float *p) { return __ldg(p); }
+RZ_DEV uint32_t ldg_nc_u32(const uint32_t *p) { return __ldg(p); }
+
+// ---------------------------------------------------------------------------
+// Forward point update (sweep.c:89-97)
+//
+// Reference arithmetic: d = a-b and sh = S*DH in float; branch 1 is float;
+// branch 2 evaluates (a+b) in float and the rest in double:
+//   Tt = (float)(((double)(a+b) + sqrt(2*S^2*DH^2 - d^2)) / 2).
+// On GB300 double precision runs at a small fraction of the FP32 rate, so
+// branch 2 is evaluated in float-float arithmetic with a certified error
+// bound (about 2^-42 relative; the check uses 2^-38).  If the float-float
+// value is farther than the bound from every float rounding midpoint, the
+// reference's double computation (whose own error is below 2^-50) rounds to
+// the same float.  Otherwise the exact double path runs; that happens for
+// roughly one update in ten thousand.
+// ---------------------------------------------------------------------------
+RZ_DEV float godunov_branch2_f64(float sum, float d, float s, float dh) {
+    double sd = (double)s, hd = (double)dh, dd = (double)d;
+    double p = __dmul_rn(__dmul_rn(2.0, __dmul_rn(sd, sd)), __dmul_rn(hd, hd));
+    double q = __dsub_rn(p, __dmul_rn(dd, dd));
+    double u = __dadd_rn((double)sum, __dsqrt_rn(q));
+    return __double2float_rn(__dmul_rn(u, 0.5));
+}
+
+RZ_DEV float godunov_ref(float a, float b, float s, float dh) {
+    float d = __fsub_rn(a, b);
+    float sh = __fmul_rn(s, dh);
+    if (fabsf(d) >= sh) return __fadd_rn(fminf(a, b), sh);
+    float sum = __fadd_rn(a, b);
+    // S*h = sh + shl exactly
+    float shl = __fmaf_rn(s, dh, -sh);
+    // (S*h)^2 ~= p2 + p2l + 2*sh*shl  (shl^2 < 2^-48 relative is dropped)
+    float p2 = __fmul_rn(sh, sh);
+    float p2l = __fmaf_rn(sh, sh, -p2);
+    float cross = __fmaf_rn(__fmul_rn(2.0f, sh), shl, p2l);
+    // d^2 = d2 + d2l exactly
+    float d2 = __fmul_rn(d, d);
+    float d2l = __fmaf_rn(d, d, -d2);
+    // D = 2*(S h)^2 - d^2 with 2*p2 >= d2 (|d| < sh): fast two-sum
+    float P = __fmul_rn(2.0f, p2);
+    float Dh = __fsub_rn(P, d2);
+    float Dl = __fsub_rn(__fsub_rn(P, Dh), d2);
+    Dl = __fadd_rn(Dl, __fsub_rn(__fmul_rn(2.0f, cross), d2l));
+    // sqrt(D) ~= r0 + rl: one Newton correction on an rsqrt seed
+    float rs = rsqrtf(Dh);
+    float r0 = __fmul_rn(Dh, rs);
+    float res = __fmaf_rn(-r0, r0, Dh);
+    float rl = __fmul_rn(__fadd_rn(res, Dl), __fmul_rn(0.5f, rs));
+    // u = sum + r0 + rl (two-sum on the leading terms)
+    float uh = __fadd_rn(sum, r0);
+    float bb = __fsub_rn(uh, sum);
+    float ue = __fadd_rn(__fsub_rn(sum, __fsub_rn(uh, bb)), __fsub_rn(r0, bb));
+    float ul = __fadd_rn(ue, rl);
+    float z = __fadd_rn(uh, ul);
+    float zr = __fadd_rn(__fsub_rn(uh, z), ul);
+    // distance to the nearest rounding midpoint against the error bound; the
+    // spacing below z (smaller at a power of two) is the conservative one
+    float below = __fsub_rn(z, __int_as_float(__float_as_int(z) - 1));
+    float tol = __fmul_rn(z, 0x1p-38f);
+    bool safe = (fabsf(zr) < __fsub_rn(__fmul_rn(0.5f, below), tol)) && (Dh > 0x1p-100f) && (z < 0x1p+100f);
+    if (__builtin_expect(safe, 1)) return __fmul_rn(0.5f, z);
+    return godunov_branch2_f64(sum, d, s, dh);
+}
+
+// fast mode: FP32 arithmetic throughout (error ~1 ulp per update)
+RZ_DEV float godunov_fast(float a, float b, float s, float dh) {
+    float d = a - b;
+    float sh = s * dh;
+    if (fabsf(d) >= sh) return fminf(a, b) + sh;
+    float q = fmaf(2.0f * sh, sh, -d * d);
+    return 0.5f * (a + b + q * rsqrtf(q));
+}
+
+// ---------------------------------------------------------------------------
+// Adjoint point update (sweep_adj.c:33-68)
+//
+// All reference operations are float: differences, division by DH, the
+// upwind splits (x+|x|)/2, (x-|x|)/2 (exact), lhs, rhs, rhs/lhs, fminf.
+// Division by the constant DH uses Markstein's correction
+//   q = x*y, r = fma(-q, DH, x), q' = fma(r, y, q),  y = RN(1/DH),
+// which is correctly rounded for every x when it passes the exhaustive
+// per-DH check the host runs before enabling it (rz_check_div); otherwise
+// IEEE division is used.
+// ---------------------------------------------------------------------------
+struct DivDH {
+    float dh, rdh;
+    bool fast;
+    // numerators that are never tiny (differences of traveltimes): a zero
+    // numerator may come out as +0 instead of -0, which no later operation
+    // of the sweep can tell apart (no division by it, no sign test)
+    RZ_DEV float operator()(float x) const {
+        if (fast) {
+            float q = __fmul_rn(x, rdh);
+            float r = __fmaf_rn(-q, dh, x);
+            return __fmaf_rn(r, rdh, q);
+        }
+        return __fdiv_rn(x, dh);
+    }
+    // numerators built from lambda, which can be tiny: the exhaustive check
+    // covers normal quotients only, so tiny ones take IEEE division
+    RZ_DEV float checked(float x) const {
+        if (fast && fabsf(x) >= 0x1p-96f) {
+            float q = __fmul_rn(x, rdh);
+            float r = __fmaf_rn(-q, dh, x);
+            return __fmaf_rn(r, rdh, q);
+        }
+        return __fdiv_rn(x, dh);
+    }
+};
+
+RZ_DEV float pos_part(float x) { return x > 0.0f ? x : 0.0f; }   // (x+|x|)/2
+RZ_DEV float neg_part(float x) { return x <= 0.0f ? x : 0.0f; }  // (x-|x|)/2
+
+// tc: TT at the cell; te/tw/ts/tn: TT at (h+1,k), (h-1,k), (h,k+1), (h,k-1)
+// le/lw/ls/ln: lambda at the same neighbours; own: lambda at the cell.
+RZ_DEV float leung_qian_ref(float tc, float te, float tw, float ts, float tn, float le, float lw, float ls, float ln,
+                            float own, const DivDH &div, float eps_adj) {
+    float ap = div(-__fsub_rn(te, tc));
+    float am = div(-__fsub_rn(tc, tw));
+    float bp = div(-__fsub_rn(ts, tc));
+    float bm = div(-__fsub_rn(tc, tn));
+    float app = pos_part(ap), apm = neg_part(ap);
+    float amp = pos_part(am), amm = neg_part(am);
+    float bpp = pos_part(bp), bpm = neg_part(bp);
+    float bmp = pos_part(bm), bmm = neg_part(bm);
+    float lhs = __fadd_rn(div(__fsub_rn(app, amm)), div(__fsub_rn(bpp, bmm)));
+    float rhs = __fadd_rn(div.checked(__fsub_rn(__fmul_rn(amp, lw), __fmul_rn(apm, le))),
+                          div.checked(__fsub_rn(__fmul_rn(bmp, ln), __fmul_rn(bpm, ls))));
+    float lt = (lhs > eps_adj) ? __fdiv_rn(rhs, lhs) : 0.0f;
+    float r = fminf(own, lt);
+    const float kInf = 9999999.0f;  // INF of fd.h:30
+    if (tc >= kInf || ts >= kInf || tn >= kInf || te >= kInf || tw >= kInf) r = 0.0f;
+    return r;
+}
+
+RZ_DEV float leung_qian_fast(float tc, float te, float tw, float ts, float tn, float le, float lw, float ls, float ln,
+                             float own, float rdh, float eps_adj) {
+    float ap = (tc - te) * rdh, am = (tw - tc) * rdh;
+    float bp = (tc - ts) * rdh, bm = (tn - tc) * rdh;
+    float lhs = (fmaxf(ap, 0.0f) - fminf(am, 0.0f) + fmaxf(bp, 0.0f) - fminf(bm, 0.0f)) * rdh;
+    float rhs = (fmaxf(am, 0.0f) * lw - fminf(ap, 0.0f) * le + fmaxf(bm, 0.0f) * ln - fminf(bp, 0.0f) * ls) * rdh;
+    float lt = (lhs > eps_adj) ? __fdividef(rhs, lhs) : 0.0f;
+    return fminf(own, lt);
+}
+
+}  // namespace rz

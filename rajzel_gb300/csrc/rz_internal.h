@@ -1,0 +1,109 @@
+// rz_internal.h -- parameter blocks and launcher declarations shared by the
+// kernels (rz_shot.cu, rz_aux.cu) and the C-ABI implementation (rz_api.cu).
+#pragma once
+#include <cuda.h>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace rz {
+
+// Strips are 32 grid rows; one warp sweeps one strip at a time.
+constexpr int kStrip = 32;
+// Column blocks moved by TMA are 32 columns wide; a warp keeps a ring of
+// three blocks of its strip (+1 halo row) in shared memory.
+constexpr int kBlk = 32;
+constexpr int kRing = 3;
+constexpr int kBoxRows = kStrip + 1;
+constexpr int kSlotFloats = kBoxRows * kBlk;  // 1056 floats = 4224 B
+// warp-to-warp hand-off ring (values of the strip boundary row), guarded by
+// full/empty mbarrier pairs per group of kGroup columns
+constexpr int kHandoff = 128;
+constexpr int kGroup = 8;
+constexpr int kGroups = kHandoff / kGroup;
+constexpr int kMaxWarps = 16;
+constexpr int kTimelineSlots = 8;
+
+// Skewed ("diagonal-major") copy of a per-cell field for one sweep family:
+// X[s][q][j] holds the cell (row 32s+j, column h) with
+//   family A (sweeps with dx == dy): q = h + j
+//   family B (sweeps with dx != dy): q = h - j + 31
+// so that the 32 cells a warp updates at one wavefront step are 32
+// consecutive floats.  Line q is stored at index q + kSkewFront; qn =
+// 32*nxb + 64 lines per strip leave room for the prefetch running up to ten
+// lines past either end of a sweep.
+constexpr int kSkewFront = 16;
+__host__ __device__ inline int skew_lines(int nxb) { return 32 * nxb + 64; }
+// Rows bordering a strip (adjoint traveltime halo) are stored with kEdgePad
+// floats of padding on both sides of each row.
+constexpr int kEdgePad = 48;
+__host__ __device__ inline int edge_row(int nxp) { return nxp + 2 * kEdgePad; }
+
+enum Mode : int { kModeReference = 0, kModeFast = 1 };
+
+struct ShotParams {
+    // grid
+    int nx, ny, nxp;        // NX, NY, row pitch (floats) of field buffers
+    int nstrips, nxb, qn;   // ceil(NY/32), ceil(NX/32), skew lines per strip
+    float dh, time, ttnorm, eps_adj;
+    float dh_rcp;           // RN(1/DH)
+    int div_fast;           // Markstein division by DH verified for this DH
+    int max_passes;
+    int nshots;             // shots in this launch (blockIdx.x < nshots)
+    int do_residual;        // compute Tres and l2 from Tobs
+    int do_adjoint;         // 0: forward (+ residuals) only
+    int start_adjoint;      // 1: T and Tres are given; skip forward and residuals
+    // model (shared by all shots)
+    const float *SA, *SB;   // skewed slowness
+    const uint32_t *MA, *MB;  // skewed adjoint skip bits (frame | receiver | outside)
+    // per-shot fields; shot z at offset z*fstride (floats)
+    float *T;               // traveltime  [nshots][ny][nxp]
+    float *Told;            // reference-mode snapshot  [nshots][ny][nxp]
+    float *L;               // adjoint field lambda [nshots][ny][nxp]
+    float *TA, *TB;         // skewed traveltimes [nshots][nstrips][qn][32]
+    float *EU, *ED;         // rows above / below each strip [nshots][nstrips][edge_row(nxp)]
+    size_t fstride;         // ny*nxp
+    size_t sstride;         // nstrips*qn*32
+    size_t estride;         // nstrips*edge_row(nxp)
+    // sources (0-based grid indices) for the shots of this launch
+    const int *src_h, *src_k;
+    // receivers (0-based)
+    int ntr;
+    const int *rec_h, *rec_k;
+    // de-duplicated interior receiver cells and the receiver whose residual
+    // initialises lambda there ("last receiver wins", init_travel_adj.c:49-54)
+    int nrcell;
+    const int *rcell_h, *rcell_k, *rcell_rec;
+    const float *Tobs;      // [nshots][ntr]
+    float *Tmod, *Tres;     // [nshots][ntr]
+    double *l2;             // [nshots]
+    int *passes_fwd, *passes_adj, *status;  // [nshots]
+    unsigned long long *timeline;           // [nshots][kTimelineSlots] ns stamps, or null
+};
+
+// launchers (rz_shot.cu)
+size_t shot_kernel_smem(int nwarps);
+// mapT_tile: [shots][ny][nx] traveltimes, 32x33 box (adjoint preparation);
+// mapT_row / mapL_row: traveltime / lambda, 32x1 box (the sweeps)
+cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const CUtensorMap &mapT_tile, const CUtensorMap &mapT_row,
+                               const CUtensorMap &mapL_row, cudaStream_t st);
+
+// launchers (rz_aux.cu)
+cudaError_t launch_skew_field(const float *src, int nx, int ny, int pitch, int nstrips, int nxb, float *dstA,
+                              float *dstB, cudaStream_t st);
+cudaError_t launch_skip_masks(const uint8_t *skip, int nx, int ny, int nstrips, int nxb, uint32_t *MA, uint32_t *MB,
+                              cudaStream_t st);
+// gradient stack: grad = cp_grad_frame^2( sum_s  RN32(lam_s * cube) )
+//   mode reference: per-shot float contribution RN32(RN64(lam*cube64)) added
+//   in float in shot order; mode fast: contributions added in double.
+cudaError_t launch_stack(const float *L, size_t fstride, int nshots, const double *cube, const float *S, int nx,
+                         int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, cudaStream_t st);
+cudaError_t launch_cp_frame(float *A, double *A64, int nx, int ny, int pitch, int times, cudaStream_t st);
+cudaError_t launch_copy_rows(const float *src, int src_pitch, float *dst, int dst_pitch, int nx, int ny,
+                             size_t nbatch, size_t src_bstride, size_t dst_bstride, cudaStream_t st);
+cudaError_t launch_check_div(float dh, float rcp, unsigned int *bad, cudaStream_t st);
+// S = (float)(1.0/(double)vp) per cell (calc_S.c:21)
+cudaError_t launch_calc_s(const float *vp, float *S, long n, cudaStream_t st);
+// *out = 0.5 * sum_z l2[z], summed in shot order in double (grad_obj.c:28,42,61)
+cudaError_t launch_sum_l2(const double *l2, int n, double *out, cudaStream_t st);
+
+}  // namespace rz

@@ -1,0 +1,61 @@
+// rz_selftest.cu -- device self-tests of the point-update arithmetic, built
+// into librz_selftest.so for the GPU test-suite only.
+//
+// rz_selftest_godunov draws n seeded random update inputs (neighbour minima
+// a, b within a few cell-times of each other, slowness 1/6000..1/1400 s/m,
+// DH from the workload set) and compares the certified float-float evaluation
+// of the reference's double branch (godunov_ref) with a direct evaluation of
+// that branch in double.  Any mismatch is a defect.
+#include <cuda_runtime.h>
+
+#include "rz_device.cuh"
+
+namespace {
+
+__device__ __forceinline__ uint32_t mix(uint64_t x) {
+    x ^= x >> 33;
+    x *= 0xff51afd7ed558ccdULL;
+    x ^= x >> 33;
+    x *= 0xc4ceb9fe1a85ec53ULL;
+    x ^= x >> 33;
+    return (uint32_t)x;
+}
+__device__ __forceinline__ float unif(uint64_t seed, uint64_t i, int k) {
+    return (mix(seed * 0x9E3779B97F4A7C15ULL + i * 8 + k) >> 8) * (1.0f / 16777216.0f);
+}
+
+__global__ void godunov_check(uint64_t seed, long n, unsigned long long *bad, unsigned long long *slow) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float dhs[4] = {5.0f, 10.0f, 12.5f, 20.0f};
+    const float dh = dhs[mix(seed + 17 * i) & 3];
+    const float s = 1.0f / (1400.0f + 4600.0f * unif(seed, i, 0));
+    const float sh = s * dh;
+    const float a = 40.0f * unif(seed, i, 1);
+    // b within [-1.2 sh, 1.2 sh] of a to exercise both branches
+    float b = a + sh * (2.4f * unif(seed, i, 2) - 1.2f);
+    if (b < 0.f) b = 0.f;
+    const float got = rz::godunov_ref(a, b, s, dh);
+    float want;
+    const float d = __fsub_rn(a, b);
+    if (fabsf(d) >= __fmul_rn(s, dh)) want = __fadd_rn(fminf(a, b), __fmul_rn(s, dh));
+    else want = rz::godunov_branch2_f64(__fadd_rn(a, b), d, s, dh);
+    if (__float_as_uint(got) != __float_as_uint(want)) atomicAdd(bad, 1ull);
+    (void)slow;
+}
+
+}  // namespace
+
+extern "C" int rz_selftest_godunov(unsigned long long seed, long n, unsigned long long *bad_out) {
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) return 3;
+    cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+    godunov_check<<<(unsigned)((n + 255) / 256), 256>>>(seed, n, d, d + 1);
+    cudaError_t e = cudaDeviceSynchronize();
+    unsigned long long h[2] = {0, 0};
+    cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return 3;
+    *bad_out = h[0];
+    return 0;
+}

@@ -1,0 +1,734 @@
+// rz_shot.cu -- one CTA solves one shot end to end: forward Eikonal to
+// convergence (eikonal.c:31-57), receiver picks and scaled residuals
+// (calc_FA.c, calc_FA_res.c:34-72), and the adjoint field to convergence
+// (eikonal_adj.c:31-51, init_travel_adj.c:22-58).
+//
+// Wavefront decomposition.  A directional Gauss-Seidel sweep (sweep.c:24-102,
+// sweep_adj.c:25-75) updates cell (h,k) after its upstream neighbours
+// (h-dx,k), (h,k-dy) and before its downstream neighbours.  The grid is cut
+// into strips of 32 rows; warp g sweeps strip g (strip order reversed for
+// dy<0) with lane l owning one row and lagging lane l-1 by one step, so at
+// step t lane l updates sweep-local column t-l: an anti-diagonal.  The lane
+// above hands its fresh value down with a shuffle, the lane below hands its
+// still-old value up, and the last lane of a warp feeds the next warp through
+// a small shared-memory ring guarded by release/acquire progress counters.
+// Every update therefore sees exactly the neighbour values the reference's
+// sequential loop sees, and the result is the reference's, bit for bit, in
+// reference mode.
+//
+// Memory path.  The read-write field (T forward, lambda adjoint) streams
+// through a per-warp ring of three 33x32 shared-memory tiles filled by TMA
+// (cp.async.bulk.tensor) and written back by TMA; the extra row is the next
+// strip's first row (old values).  Read-only per-cell data (slowness,
+// converged traveltimes, adjoint skip bits) are stored pre-skewed so that the
+// 32 values one wavefront step needs are one 128-byte line: fully coalesced
+// and prefetched eight steps ahead into registers.
+#include "rz_device.cuh"
+#include "rz_internal.h"
+
+namespace rz {
+
+struct WarpShared {
+    float ring[kRing][kSlotFloats];  // TMA tiles: 3 x 33 rows x 32 columns
+    float hb[kHandoff];              // boundary row handed down by warp g-1
+    uint64_t full[kGroups];          // hand-off group written (producer -> this warp)
+    uint64_t empty[kGroups];         // hand-off group consumed (this warp -> producer)
+};
+static_assert(sizeof(WarpShared) % 128 == 0, "TMA destinations need 128-byte alignment");
+
+struct CtaShared {
+    WarpShared *w;
+    uint64_t *mbar;  // [W][kRing]
+    double *red;     // [W] reduction scratch
+    int *ctl;        // [8] broadcast words
+};
+
+__host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
+
+size_t shot_kernel_smem(int W) {
+    size_t o = sizeof(WarpShared) * W;
+    o = align_up(o, 8) + sizeof(uint64_t) * kRing * W;
+    o = align_up(o, 8) + sizeof(double) * W;
+    o += sizeof(int) * 8;
+    return align_up(o, 128);
+}
+
+struct Warp {
+    int g, l, z;
+    uint32_t phase;  // expected parity per ring slot
+    int err;
+    WarpShared *ws, *ws_down;
+    uint64_t *mbar;
+    volatile int *abort_word;  // CTA-wide: a bounded wait gave up
+};
+
+RZ_DEV int mod3(int v) { return v - 3 * (v / 3); }
+
+RZ_DEV float lds(uint32_t a) {
+    float v;
+    asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
+    return v;
+}
+RZ_DEV void sts(uint32_t a, float v) { asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v)); }
+
+RZ_DEV unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+// per-shot timeline (ns): 0 start, 1 forward done, 2 residuals done,
+// 3 adjoint prep done, 4 adjoint done, 5 first forward sweep done,
+// 6 first adjoint sweep done
+RZ_DEV void stamp(const ShotParams &P, int z, int slot) {
+    if (P.timeline && threadIdx.x == 0) P.timeline[(size_t)z * kTimelineSlots + slot] = global_ns();
+}
+
+RZ_DEV void ring_wait(Warp &w, int slot) {
+    uint32_t par = (w.phase >> slot) & 1u;
+    if (!mbar_wait(&w.mbar[slot], par, w.abort_word)) w.err |= ERR_TMA_TIMEOUT;
+    w.phase ^= 1u << slot;
+}
+
+// ---------------------------------------------------------------------------
+// one directional sweep of one warp over its strip
+//   ADJ=false: forward Godunov sweep of T      (sweep.c)
+//   ADJ=true : adjoint Leung-Qian sweep of lam (sweep_adj.c)
+//
+// Step t of the warp: lane l updates sweep-local column up = t - l of its row.
+// Shared layout during a sweep: each lane owns one row of 96 floats (three
+// 32-column blocks, a ring in sweep order), the halo row is a 33rd row.  Every
+// lane fills and drains its own row with 1-row TMA copies, so one warp
+// instruction moves a whole 33x32 block, and a lane's next cell is always its
+// current cell +-4 bytes (mod the ring).
+// ---------------------------------------------------------------------------
+constexpr int kRowFloats = kRing * kBlk;          // 96
+constexpr int kRowBytes = kRowFloats * 4;         // 384
+
+template <int DX, int DY, bool ADJ, int MODE>
+__device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mrow, float &acc) {
+    const int l = w.l, g = w.g;
+    if (g >= P.nstrips) return;
+    const int s = DY > 0 ? g : P.nstrips - 1 - g;
+    const int j = DY > 0 ? l : 31 - l;
+    const int row = kStrip * s + j;
+    const bool rowok = row < P.ny;
+    const int hrow = DY > 0 ? kStrip * s + 32 : kStrip * s - 1;  // next strip's first row (old values)
+    const int boxrow = DY > 0 ? l : 32 - l;
+    const int halorow = DY > 0 ? 32 : 0;
+    const bool hasUp = DY > 0 ? (row > 0) : (row < P.ny - 1);
+    const bool hasDn = DY > 0 ? (row < P.ny - 1) : (row > 0);
+    const int nxb = P.nxb, ncol = kBlk * nxb, nx = P.nx;
+    const bool is_producer_warp = (g + 1 < P.nstrips);
+    const bool is_consumer_warp = (g > 0);
+    const bool producer = (l == 31) && is_producer_warp;
+    const bool consumer = (l == 0) && is_consumer_warp;
+    const int ngrp = ncol >> 3;  // hand-off groups per sweep
+    float *ring = &w.ws->ring[0][0];
+    const uint32_t ring_s = smem_u32(ring);
+    const uint32_t row_s = ring_s + (uint32_t)boxrow * kRowBytes;
+    const uint32_t row_end = row_s + kRowBytes;
+    const int hoff = (halorow - boxrow) * kRowBytes;
+    const uint32_t hb_in = smem_u32(w.ws->hb);
+    const uint32_t hb_out = smem_u32(is_producer_warp ? w.ws_down->hb : w.ws->hb);
+    const int z = w.z;
+    const float dh = P.dh;
+    const float dh_rcp = P.dh_rcp, eps_adj = P.eps_adj;
+    const bool div_fast = P.div_fast != 0;
+    // valid sweep-local columns [lo, hi) of this lane's row
+    const int lo = DX > 0 ? 0 : ncol - nx;
+    const int hi = rowok ? (DX > 0 ? nx : ncol) : lo;
+    // everything the step loop touches lives in registers: shared-window
+    // addresses of the barriers, the phase bits, the error bits
+    const uint32_t abort_s = smem_u32((const void *)w.abort_word);
+    const uint32_t mbar_s = smem_u32(w.mbar);
+    const uint32_t full_in = smem_u32(w.ws->full), empty_in = smem_u32(w.ws->empty);
+    const uint32_t full_out = smem_u32(is_producer_warp ? w.ws_down->full : w.ws->full);
+    const uint32_t empty_out = smem_u32(is_producer_warp ? w.ws_down->empty : w.ws->empty);
+    uint32_t phase = w.phase;
+    int err = 0;
+    float acc_l = 0.f;  // fast-mode sum of |change| (the caller's acc lives in local memory)
+    auto ring_wait_l = [&](int slot) {
+        if (!mbar_wait_a(mbar_s + 8u * slot, (phase >> slot) & 1u, abort_s)) err |= ERR_TMA_TIMEOUT;
+        phase ^= 1u << slot;
+    };
+
+    // ring position (byte offset in a row) of sweep-local block k
+    auto slot_off = [&](int k) -> uint32_t {
+        const int m = mod3(k);
+        return (uint32_t)(DX > 0 ? m : 2 - m) * (kBlk * 4);
+    };
+    auto gblk = [&](int k) { return DX > 0 ? k : nxb - 1 - k; };
+    // all lanes: TMA-load block k of their own row; lane 0 also the halo row
+    auto issue = [&](int k) {
+        const int slot = mod3(k);
+        const uint32_t bar = mbar_s + 8u * slot;
+        if (l == 0) mbar_arrive_expect_tx_a(bar, kBoxRows * kBlk * 4);
+        __syncwarp();
+        const uint32_t so = slot_off(k);
+        const int x = kBlk * gblk(k);
+        tma_load_3d_a(row_s + so, mrow, x, row, z, bar);
+        if (l == 0) tma_load_3d_a(ring_s + (uint32_t)halorow * kRowBytes + so, mrow, x, hrow, z, bar);
+    };
+
+    // read-only per-cell streams, skewed so one step reads one 128-byte line
+    constexpr bool famA = (DX == DY);
+    constexpr int QS = DX > 0 ? 1 : -1;  // line step per wavefront step
+    constexpr int QOFF = ADJ ? 1 : 0;    // the adjoint streams the downstream traveltime
+    const float *xs;
+    const uint32_t *mk = nullptr;
+    const float *ep = nullptr;
+    {
+        const int q0 = (DX > 0 ? 0 : ncol + 30) + QS * QOFF + kSkewFront;
+        if (!ADJ) {
+            xs = (famA ? P.SA : P.SB) + ((size_t)s * P.qn + q0) * 32 + j;
+        } else {
+            xs = (famA ? P.TA : P.TB) + (size_t)z * P.sstride + ((size_t)s * P.qn + q0) * 32 + j;
+            mk = (famA ? P.MA : P.MB) + (size_t)s * P.qn + (q0 - QS * QOFF);
+            const float *erow = ((l == 31) == (DY > 0) ? P.ED : P.EU) + (size_t)z * P.estride +
+                                (size_t)s * edge_row(P.nxp) + kEdgePad;
+            ep = erow + (DX > 0 ? -l : ncol - 1 + l);  // column of this lane at step 0
+        }
+    }
+
+    float xq[8];
+    uint32_t mq[8];
+    float eq[8];
+#pragma unroll
+    for (int i = 0; i < 8; ++i) {
+        if (!ADJ) {
+            xq[i] = __ldg(xs + QS * 32 * i);
+        } else {
+            xq[i] = __ldca(xs + QS * 32 * i);
+            mq[i] = __ldg(mk + QS * i);
+            eq[i] = __ldca(ep + QS * i);
+        }
+    }
+    float c_tt = 0.f, w_tt = 0.f;
+    if (ADJ) c_tt = __ldca(xs - QS * 32);
+
+    issue(0);
+    if (nxb > 1) issue(1);
+    ring_wait_l(0);
+    if (is_consumer_warp && !mbar_wait_a(full_in, 0, abort_s)) err |= ERR_FLAG_TIMEOUT;
+
+    // ring address of this lane's cell at step t = 0 (column up = -l, which
+    // for l > 0 lies before the sweep: any ring cell serves, nothing reads it)
+    auto advance = [&](uint32_t a) -> uint32_t {
+        if (DX > 0) {
+            a += 4;
+            return a == row_end ? row_s : a;
+        } else {
+            return a == row_s ? row_end - 4 : a - 4;
+        }
+    };
+    uint32_t addr_c = row_s + slot_off(0) + (DX > 0 ? 0u : 31u * 4u);
+    for (int q = 0; q < l; ++q) addr_c = (DX > 0) ? (addr_c == row_s ? row_end - 4 : addr_c - 4) : (addr_c + 4 == row_end ? row_s : addr_c + 4);
+    uint32_t addr_e = advance(addr_c);
+    float own_next = lds(addr_c);
+    float ev_next = lds(addr_e);
+    float halo_next = lds(addr_c + hoff);
+    float hb_next = lds(hb_in);
+
+    float res_prev = 0.f;
+    for (int k = 0; k <= nxb; ++k) {
+        // refill: block k+1 goes where block k-2 was (written back last round)
+        if (k >= 1 && k + 1 < nxb) {
+            // generic accesses of the slot (including writes of lanes still
+            // outside the sweep) are ordered before the TMA refill
+            fence_proxy_async_smem();
+            tma_store_wait_read<0>();
+            issue(k + 1);
+        }
+#pragma unroll 1
+        for (int i0 = 0; i0 < 32; i0 += 8) {
+            const int t0 = kBlk * k + i0;
+            const int u0 = t0 - l;
+            const float *xr = xs + QS * 32 * t0;
+            const uint32_t *mr = ADJ ? mk + QS * t0 : nullptr;
+            const float *er = ADJ ? ep + QS * t0 : nullptr;
+            const uint32_t hb_g = hb_in + 4u * (uint32_t)(t0 & (kHandoff - 1));
+            const uint32_t hb_last = hb_in + 4u * (uint32_t)((t0 + 8) & (kHandoff - 1));
+#pragma unroll
+            for (int ii = 0; ii < 8; ++ii) {
+                const int t = t0 + ii;
+                const int up = u0 + ii;
+                const float own = own_next;
+                const float ev = ev_next;
+                const float halo = halo_next;
+                const float hbv = hb_next;
+                const uint32_t cur = addr_c;
+                // hand-off flow control and the TMA block lane 0 needs next
+                if (ii == 7) {
+                    if (is_consumer_warp) {
+                        const int G = (t + 1) >> 3;
+                        if (G < ngrp && !mbar_wait_a(full_in + 8u * (G & (kGroups - 1)), (G >> 4) & 1, abort_s))
+                            err |= ERR_FLAG_TIMEOUT;
+                    }
+                    if (is_producer_warp) {
+                        const int G = (t - 31) >> 3;
+                        if (G >= kGroups && G < ngrp &&
+                            !mbar_wait_a(empty_out + 8u * (G & (kGroups - 1)), ((G >> 4) - 1) & 1, abort_s))
+                            err |= ERR_FLAG_TIMEOUT;
+                    }
+                }
+                if (ii == 6 && i0 == 24 && k + 1 < nxb) ring_wait_l(mod3(k + 1));
+                // prefetch the next step's shared values
+                addr_c = addr_e;
+                addr_e = advance(addr_e);
+                own_next = ev;
+                ev_next = lds(addr_e);
+                halo_next = lds(addr_c + hoff);
+                hb_next = lds(ii < 7 ? hb_g + 4u * (ii + 1) : hb_last);
+
+                float nv = __shfl_up_sync(0xffffffffu, res_prev, 1);
+                float sv = __shfl_down_sync(0xffffffffu, ev, 1);
+                if (l == 0) nv = hbv;
+                if (l == 31) sv = halo;
+                const float xv = xq[ii];
+                const bool valid = (unsigned)(up - lo) < (unsigned)(hi - lo);
+                float r;
+                if (!ADJ) {
+                    xq[ii] = __ldg(xr + QS * 32 * (ii + 8));
+                    const bool hasW = up > lo;
+                    const bool hasE = up < hi - 1;
+                    const float tw = hasW ? res_prev : own;
+                    const float te = hasE ? ev : own;
+                    const float tn = hasUp ? nv : own;
+                    const float ts = hasDn ? sv : own;
+                    const float a = fminf(tw, te), b = fminf(tn, ts);
+                    const float tt =
+                        (MODE == kModeReference) ? godunov_ref(a, b, xv, dh) : godunov_fast(a, b, xv, dh);
+                    r = fminf(own, tt);
+                    if (!valid) r = own;
+                } else {
+                    xq[ii] = __ldca(xr + QS * 32 * (ii + 8));
+                    const uint32_t mword = mq[ii];
+                    mq[ii] = __ldg(mr + QS * (ii + 8));
+                    const float edge = eq[ii];
+                    eq[ii] = __ldca(er + QS * (ii + 8));
+                    const float e_tt = xv;  // traveltime one column downstream
+                    float n_tt = __shfl_up_sync(0xffffffffu, w_tt, 1);
+                    float s_tt = __shfl_down_sync(0xffffffffu, e_tt, 1);
+                    if (l == 0) n_tt = edge;
+                    if (l == 31) s_tt = edge;
+                    const float tE = DX > 0 ? e_tt : w_tt, tW = DX > 0 ? w_tt : e_tt;
+                    const float tS = DY > 0 ? s_tt : n_tt, tN = DY > 0 ? n_tt : s_tt;
+                    const float lE = DX > 0 ? ev : res_prev, lW = DX > 0 ? res_prev : ev;
+                    const float lS = DY > 0 ? sv : nv, lN = DY > 0 ? nv : sv;
+                    if (MODE == kModeReference) {
+                        DivDH div{dh, dh_rcp, div_fast};
+                        r = leung_qian_ref(c_tt, tE, tW, tS, tN, lE, lW, lS, lN, own, div, eps_adj);
+                    } else {
+                        r = leung_qian_fast(c_tt, tE, tW, tS, tN, lE, lW, lS, lN, own, dh_rcp, eps_adj);
+                    }
+                    const bool keep = !valid || ((mword >> j) & 1u);
+                    if (keep) r = own;
+                    w_tt = c_tt;
+                    c_tt = e_tt;
+                }
+                sts(cur, r);
+                if (MODE == kModeFast) acc_l += valid ? own - r : 0.0f;
+                if (producer) {
+                    const int upp = t - 31;  // lane 31's column at this step
+                    if (upp >= 0 && upp < ncol) sts(hb_out + 4u * (uint32_t)(upp & (kHandoff - 1)), r);
+                    if (ii == 6 && t >= 38 && ((t - 38) >> 3) < ngrp)
+                        mbar_arrive_a(full_out + 8u * (((t - 38) >> 3) & (kGroups - 1)));
+                }
+                if (consumer && ii == 7 && (t >> 3) < ngrp) mbar_arrive_a(empty_in + 8u * ((t >> 3) & (kGroups - 1)));
+                res_prev = r;
+            }
+        }
+        // block k-1 is complete: write it back (each lane its own row)
+        if (k >= 1) {
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (rowok) tma_store_3d_a(mrow, kBlk * gblk(k - 1), row, z, row_s + slot_off(k - 1));
+            tma_store_commit();
+        }
+    }
+    tma_store_wait_all<0>();
+    fence_proxy_async_global();
+    __syncwarp();
+    w.phase = phase;
+    w.err |= err;
+    acc += acc_l;
+}
+
+// ---------------------------------------------------------------------------
+// CTA-wide helpers
+// ---------------------------------------------------------------------------
+RZ_DEV double block_sum(double v, const CtaShared &sh) {
+    const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    __syncthreads();
+    if (l == 0) sh.red[g] = v;
+    __syncthreads();
+    double t = 0.0;
+    for (int i = 0; i < W; ++i) t += sh.red[i];
+    __syncthreads();
+    return t;
+}
+
+// (re)arm this warp's hand-off barriers; every sweep starts at group 0
+RZ_DEV void handoff_init(WarpShared *ws, bool reinit) {
+    if ((threadIdx.x & 31) == 0) {
+        for (int i = 0; i < kGroups; ++i) {
+            if (reinit) {
+                mbar_inval(&ws->full[i]);
+                mbar_inval(&ws->empty[i]);
+            }
+            mbar_init(&ws->full[i], 1);
+            mbar_init(&ws->empty[i], 1);
+        }
+    }
+}
+
+// between sweeps: all stores done, hand-off barriers re-armed
+RZ_DEV void sweep_barrier(const CtaShared &sh) {
+    __syncthreads();
+    handoff_init(&sh.w[threadIdx.x >> 5], true);
+    __syncthreads();
+}
+
+// Reference stopping rule (norm1.c:20-29, eikonal.c:44): continue while
+// mean|F-Fold| >= TTNORM, the mean being a sequential float sum in x-outer
+// order.  A parallel estimate decides whenever it is certain; within the
+// worst-case rounding window of the sequential sum the exact sequential sum
+// is replayed (rare).
+RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold, const CtaShared &sh) {
+    const int n = P.nx * P.ny;
+    float part = 0.f;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        int k = c / P.nx, h = c - k * P.nx;
+        size_t o = (size_t)k * P.nxp + h;
+        part += fabsf(__fsub_rn(__ldcg(F + o), __ldcg(Fold + o)));
+    }
+    double est = block_sum((double)part, sh);
+    if (threadIdx.x == 0) {
+        int decision;  // 1 continue, 0 stop, 2 undecided
+        if (est == 0.0) {
+            decision = 0;
+        } else {
+            double per = (double)(n / (int)blockDim.x + 2);
+            double gam = ((double)n + per + 4.0) * 0x1p-24 + 0x1p-20;
+            double thr = (double)P.ttnorm * (double)n;
+            if (est * (1.0 - gam) > thr * (1.0 + 0x1p-21)) decision = 1;
+            else if (est * (1.0 + gam) < thr * (1.0 - 0x1p-21)) decision = 0;
+            else decision = 2;
+        }
+        if (decision == 2) {
+            float sum = 0.f;
+            for (int h = 0; h < P.nx; ++h)
+                for (int k = 0; k < P.ny; ++k) {
+                    size_t o = (size_t)k * P.nxp + h;
+                    float d = fabsf(__fsub_rn(__ldcg(F + o), __ldcg(Fold + o)));
+                    sum = __double2float_rn(__dadd_rn((double)sum, (double)d));
+                }
+            float l1 = __fdiv_rn(sum, __int2float_rn(n));
+            decision = (l1 >= P.ttnorm) ? 1 : 0;
+        }
+        sh.ctl[0] = decision;
+    }
+    __syncthreads();
+    int d = sh.ctl[0];
+    __syncthreads();
+    return d != 0;
+}
+
+RZ_DEV void copy_field(const ShotParams &P, const float *src, float *dst) {
+    const int n = P.nx * P.ny;
+    for (int c = threadIdx.x; c < n; c += blockDim.x) {
+        int k = c / P.nx, h = c - k * P.nx;
+        size_t o = (size_t)k * P.nxp + h;
+        dst[o] = __ldcg(src + o);
+    }
+}
+
+// Skewed copies of the converged traveltimes for the adjoint sweeps, plus the
+// rows bordering each strip (TMA tiles in, coalesced skew lines out).
+template <int DUMMY>
+__device__ __noinline__ void relayout(const ShotParams &P, Warp &w, const CUtensorMap *mld) {
+    const int l = w.l, g = w.g, z = w.z;
+    if (g >= P.nstrips) return;
+    const int s = g;
+    float *ring = &w.ws->ring[0][0];
+    const int nxb = P.nxb;
+    float *ta = P.TA + (size_t)z * P.sstride + ((size_t)s * P.qn + kSkewFront) * 32;
+    float *tb = P.TB + (size_t)z * P.sstride + ((size_t)s * P.qn + kSkewFront) * 32;
+    const int er = edge_row(P.nxp);
+    float *ed = P.ED + (size_t)z * P.estride + (size_t)s * er + kEdgePad;
+    float *eu_next = (s + 1 < P.nstrips) ? P.EU + (size_t)z * P.estride + (size_t)(s + 1) * er + kEdgePad : nullptr;
+    // tile index G (column block, may be -1 or nxb: zero-filled) -> ring slot
+    auto slot_of = [&](int G) { return mod3(G + 1); };
+    auto issue = [&](int G) {
+        int sl = slot_of(G);
+        mbar_arrive_expect_tx(&w.mbar[sl], kSlotFloats * 4);
+        tma_load_3d(ring + sl * kSlotFloats, mld, kBlk * G, kStrip * s, z, &w.mbar[sl]);
+    };
+    if (l == 0) {
+        issue(-1);
+        issue(0);
+    }
+    __syncwarp();
+    ring_wait(w, slot_of(-1));
+    for (int G = 0; G <= nxb; ++G) {
+        ring_wait(w, slot_of(G));
+        if (l == 0 && G + 1 <= nxb) issue(G + 1);  // slot of G-2: all its reads ended last iteration
+        __syncwarp();
+        const float *t_prev = ring + slot_of(G - 1) * kSlotFloats;
+        const float *t_cur = ring + slot_of(G) * kSlotFloats;
+        // skew lines q in [32G, 32G+32): family A column q-j, family B column q+j-31
+        for (int qq = 0; qq < 32; ++qq) {
+            const int q = kBlk * G + qq;
+            const int ca = qq - l;       // column offset relative to tile G (lane = j)
+            const int cb = qq + l - 31;
+            float va = ca >= 0 ? t_cur[l * kBlk + ca] : t_prev[l * kBlk + ca + 32];
+            float vb = cb >= 0 ? t_cur[l * kBlk + cb] : t_prev[l * kBlk + cb + 32];
+            ta[(size_t)q * 32 + l] = va;
+            tb[(size_t)q * 32 + l] = vb;
+        }
+        if (G < nxb) {
+            ed[kBlk * G + l] = t_cur[32 * kBlk + l];                   // row 32s+32 (zero beyond the grid)
+            if (eu_next) eu_next[kBlk * G + l] = t_cur[31 * kBlk + l];  // row 32(s+1)-1
+        }
+        __syncwarp();
+    }
+}
+
+// ---------------------------------------------------------------------------
+// the shot kernel
+// ---------------------------------------------------------------------------
+template <int MODE>
+__global__ void __launch_bounds__(kMaxWarps * 32, 1)
+    shot_kernel(const __grid_constant__ ShotParams P, const __grid_constant__ CUtensorMap mTld,
+                const __grid_constant__ CUtensorMap mTrow, const __grid_constant__ CUtensorMap mLrow) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int W = blockDim.x >> 5;
+    const int tid = threadIdx.x, g = tid >> 5, l = tid & 31;
+    const int z = blockIdx.x;
+    if (z >= P.nshots) return;
+
+    CtaShared sh;
+    {
+        size_t o = 0;
+        sh.w = reinterpret_cast<WarpShared *>(smem_raw);
+        o = sizeof(WarpShared) * W;
+        o = align_up(o, 8);
+        sh.mbar = reinterpret_cast<uint64_t *>(smem_raw + o);
+        o += sizeof(uint64_t) * kRing * W;
+        o = align_up(o, 8);
+        sh.red = reinterpret_cast<double *>(smem_raw + o);
+        o += sizeof(double) * W;
+        sh.ctl = reinterpret_cast<int *>(smem_raw + o);
+    }
+    if (l == 0) {
+        for (int i = 0; i < kRing; ++i) mbar_init(&sh.mbar[g * kRing + i], 1);
+    }
+    handoff_init(&sh.w[g], false);
+    if (tid < 8) sh.ctl[tid] = 0;
+    if (tid == 0) tma_prefetch_desc(&mTld), tma_prefetch_desc(&mTrow), tma_prefetch_desc(&mLrow);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    __syncthreads();
+
+    Warp w;
+    w.g = g;
+    w.l = l;
+    w.z = z;
+    w.phase = 0;
+    w.err = 0;
+    w.ws = &sh.w[g];
+    w.ws_down = (g + 1 < W) ? &sh.w[g + 1] : nullptr;
+    w.mbar = &sh.mbar[g * kRing];
+    w.abort_word = &sh.ctl[1];
+
+    stamp(P, z, 0);
+    float *T = P.T + (size_t)z * P.fstride;
+    float *Told = P.Told + (size_t)z * P.fstride;
+    float *L = P.L + (size_t)z * P.fstride;
+    const int n = P.nx * P.ny;
+    int cta_err = 0;
+
+    if (!P.start_adjoint) {
+        // ---------------- forward ----------------
+        const int hs = P.src_h[z], ks = P.src_k[z];
+        const float tinit = (float)(2.0 * (double)P.time);  // zero_travel.c:22
+        for (int c = tid; c < n; c += blockDim.x) {
+            int k = c / P.nx, h = c - k * P.nx;
+            T[(size_t)k * P.nxp + h] = (h == hs && k == ks) ? 0.0f : tinit;
+        }
+        fence_proxy_async_global();
+        __syncthreads();
+
+        int pass = 0;
+        bool go = true;
+        while (go) {
+            if (pass >= P.max_passes) {
+                cta_err |= ERR_NOCONV_FWD;
+                break;
+            }
+            if (MODE == kModeReference) {
+                copy_field(P, T, Told);
+                fence_proxy_async_global();
+                __syncthreads();
+            }
+            float acc = 0.f;
+            sweep<+1, +1, false, MODE>(P, w, &mTrow, acc);
+            sweep_barrier(sh);
+            if (pass == 0) stamp(P, z, 5);
+            sweep<-1, +1, false, MODE>(P, w, &mTrow, acc);
+            sweep_barrier(sh);
+            sweep<-1, -1, false, MODE>(P, w, &mTrow, acc);
+            sweep_barrier(sh);
+            sweep<+1, -1, false, MODE>(P, w, &mTrow, acc);
+            sweep_barrier(sh);
+            ++pass;
+            if (*w.abort_word) break;
+            if (MODE == kModeReference) {
+                go = ref_continue(P, T, Told, sh);
+            } else {
+                double tot = block_sum((double)acc, sh);
+                go = (tot / (double)n) >= (double)P.ttnorm;
+            }
+        }
+        if (tid == 0) P.passes_fwd[z] = pass;
+        stamp(P, z, 1);
+
+        // ---------------- receivers: picks, residuals, misfit ----------------
+        // calc_FA.c:15-18 and calc_FA_res.c:34-72; a muted pick (Tobs<0) gives a
+        // zero residual and no misfit contribution.
+        {
+            float *sq = &sh.w[0].ring[0][0];  // scratch: W*3*1056 >= 3168 floats
+            const int chunk = kRing * kSlotFloats;
+            double l2 = 0.0;
+            for (int base = 0; base < P.ntr; base += chunk) {
+                const int m = min(chunk, P.ntr - base);
+                for (int i = tid; i < m; i += blockDim.x) {
+                    const int r = base + i;
+                    const int h = P.rec_h[r], k = P.rec_k[r];
+                    const float tm = __ldcg(T + (size_t)k * P.nxp + h);
+                    P.Tmod[(size_t)z * P.ntr + r] = tm;
+                    const float tob = P.do_residual ? P.Tobs[(size_t)z * P.ntr + r] : -1.0f;
+                    float tr = 0.f, q = 0.f;
+                    if (tob >= 0.0f) {
+                        tr = __fsub_rn(tm, tob);
+                        q = __fmul_rn(tr, tr);
+                        float gt;
+                        bool have = true;
+                        if (k <= P.ny - 2) gt = __fsub_rn(__ldcg(T + (size_t)(k + 1) * P.nxp + h), tm);
+                        else if (k == P.ny - 1) gt = __fsub_rn(tm, __ldcg(T + (size_t)(k - 1) * P.nxp + h));
+                        else have = false;
+                        if (have) {
+                            gt = __fdiv_rn(gt, P.dh);
+                            tr = (fabsf(gt) > 0.0f) ? __fdiv_rn(tr, gt) : 0.0f;
+                        }
+                    }
+                    if (P.do_residual) P.Tres[(size_t)z * P.ntr + r] = tr;
+                    sq[i] = q;
+                }
+                __syncthreads();
+                if (MODE == kModeReference) {
+                    if (tid == 0)
+                        for (int i = 0; i < m; ++i) l2 = __dadd_rn(l2, (double)sq[i]);
+                } else {
+                    double part = 0.0;
+                    for (int i = tid; i < m; i += blockDim.x) part += (double)sq[i];
+                    l2 += block_sum(part, sh);
+                }
+                __syncthreads();
+            }
+            if (tid == 0 && P.do_residual) P.l2[z] = l2;
+        }
+        stamp(P, z, 2);
+
+
+    }
+
+    if (!P.do_adjoint) {
+        __syncthreads();
+        if (l == 0) atomicOr(&P.status[z], w.err);
+        if (tid == 0) atomicOr(&P.status[z], cta_err);
+        return;
+    }
+
+    // ---------------- adjoint preparation ----------------
+    __syncthreads();
+    if (*w.abort_word) {
+        if (l == 0) atomicOr(&P.status[z], w.err);
+        if (tid == 0) atomicOr(&P.status[z], cta_err);
+        return;
+    }
+    relayout<0>(P, w, &mTld);
+    // lambda: 0 on the frame, 10*TIME inside, residuals at receiver cells
+    const float linit = (float)(10.0 * (double)P.time);
+    for (int c = tid; c < n; c += blockDim.x) {
+        int k = c / P.nx, h = c - k * P.nx;
+        bool in = (h > 0 && h < P.nx - 1 && k > 0 && k < P.ny - 1);
+        L[(size_t)k * P.nxp + h] = in ? linit : 0.0f;
+    }
+    __syncthreads();
+    for (int i = tid; i < P.nrcell; i += blockDim.x)
+        L[(size_t)P.rcell_k[i] * P.nxp + P.rcell_h[i]] = P.Tres[(size_t)z * P.ntr + P.rcell_rec[i]];
+    fence_proxy_async_global();
+    __syncthreads();
+    stamp(P, z, 3);
+
+    // ---------------- adjoint ----------------
+    int pass = 0;
+    bool go = true;
+    while (go) {
+        if (pass >= P.max_passes) {
+            cta_err |= ERR_NOCONV_ADJ;
+            break;
+        }
+        if (MODE == kModeReference) {
+            copy_field(P, L, Told);
+            fence_proxy_async_global();
+            __syncthreads();
+        }
+        float acc = 0.f;
+        sweep<+1, +1, true, MODE>(P, w, &mLrow, acc);
+        sweep_barrier(sh);
+        if (pass == 0) stamp(P, z, 6);
+        sweep<+1, -1, true, MODE>(P, w, &mLrow, acc);
+        sweep_barrier(sh);
+        sweep<-1, +1, true, MODE>(P, w, &mLrow, acc);
+        sweep_barrier(sh);
+        sweep<-1, -1, true, MODE>(P, w, &mLrow, acc);
+        sweep_barrier(sh);
+        ++pass;
+        if (*w.abort_word) break;
+        if (MODE == kModeReference) {
+            go = ref_continue(P, L, Told, sh);
+        } else {
+            double tot = block_sum((double)acc, sh);
+            go = (tot / (double)n) >= (double)P.ttnorm;
+        }
+    }
+    if (tid == 0) P.passes_adj[z] = pass;
+    stamp(P, z, 4);
+    __syncthreads();
+    if (l == 0) atomicOr(&P.status[z], w.err);
+    if (tid == 0) atomicOr(&P.status[z], cta_err);
+}
+
+cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const CUtensorMap &mTld, const CUtensorMap &mTrow,
+                               const CUtensorMap &mLrow, cudaStream_t st) {
+    const int W = P.nstrips;
+    if (W < 1 || W > kMaxWarps) return cudaErrorInvalidValue;
+    const size_t smem = shot_kernel_smem(W);
+    dim3 grid(P.nshots), block(32 * W);
+    cudaError_t e;
+    if (mode == kModeReference) {
+        e = cudaFuncSetAttribute(shot_kernel<kModeReference>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        shot_kernel<kModeReference><<<grid, block, smem, st>>>(P, mTld, mTrow, mLrow);
+    } else {
+        e = cudaFuncSetAttribute(shot_kernel<kModeFast>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        shot_kernel<kModeFast><<<grid, block, smem, st>>>(P, mTld, mTrow, mLrow);
+    }
+    return cudaGetLastError();
+}
+
+}  // namespace rz
