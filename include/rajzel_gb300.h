@@ -117,6 +117,11 @@ int rz_shot_info(rz_context *ctx, int shot, int *fwd_passes, int *adj_passes, in
    Tres [ntr] (scaled residuals as passed to eikonal_adj). */
 int rz_shot_fields(rz_context *ctx, int shot, float *TT, float *lam, float *Tres, int flags);
 
+/* Accounting: kernels this context has launched so far, and the summed
+   device time (CUDA events on the context stream) of the shot kernels
+   launched since the previous call (the list is cleared by this call). */
+int rz_kernel_stats(rz_context *ctx, long long *launches, double *shot_kernel_ms, int *shot_kernel_calls);
+
 /* Diagnostics: device time stamps (ns, %globaltimer) of shot `shot` in the
    last batch: [0] start, [1] forward converged, [2] residuals done,
    [3] adjoint prepared, [4] adjoint converged, [5] first forward sweep done,

@@ -77,10 +77,11 @@ def load_library(path: str = LIB_PATH):
     lib.rz_shot_fields.argtypes = [vp, C.c_int, vp, vp, vp, C.c_int]
     lib.rz_eikonal.argtypes = [vp, C.c_float, C.c_float, vp, vp, vp, C.c_int]
     lib.rz_shot_timeline.argtypes = [vp, C.c_int, vp]
+    lib.rz_kernel_stats.argtypes = [vp, vp, vp, vp]
     lib.rz_eikonal_adj.argtypes = [vp, vp, vp, vp, vp, C.c_int]
     for name in ("rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
                  "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
-                 "rz_eikonal_adj", "rz_shot_timeline"):
+                 "rz_eikonal_adj", "rz_shot_timeline", "rz_kernel_stats"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
@@ -213,6 +214,12 @@ class Context:
         a, b, s = C.c_int(0), C.c_int(0), C.c_int(0)
         self._check(self.lib.rz_shot_info(self.h, int(shot), C.byref(a), C.byref(b), C.byref(s)), "rz_shot_info")
         return a.value, b.value, s.value
+
+    def kernel_stats(self):
+        """(kernels launched so far, summed shot-kernel ms since the last call, shot-kernel calls)."""
+        n, ms, calls = C.c_longlong(0), C.c_double(0), C.c_int(0)
+        self._check(self.lib.rz_kernel_stats(self.h, C.byref(n), C.byref(ms), C.byref(calls)), "rz_kernel_stats")
+        return n.value, ms.value, calls.value
 
     def shot_timeline(self, shot):
         """Device time stamps (ns) of one shot of the last batch (see rz_shot_timeline)."""

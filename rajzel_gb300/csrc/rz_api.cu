@@ -68,6 +68,10 @@ struct rz_context {
 
     int last_n = 0;
     bool last_adj = false;
+
+    // accounting: kernels launched, and CUDA-event timing of every shot-kernel launch
+    long long launches = 0;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> shot_events;
 };
 
 // ---------------------------------------------------------------------------
@@ -315,7 +319,14 @@ static int run_batch(rz_context *c, int n, bool adjoint, bool residual, bool sta
     CK(cudaMemsetAsync(c->dTl, 0, (size_t)n * kTimelineSlots * sizeof(unsigned long long), c->st));
     CK(cudaMemsetAsync(c->dPf, 0, n * sizeof(int), c->st));
     CK(cudaMemsetAsync(c->dPa, 0, n * sizeof(int), c->st));
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, c->st));
     CK(launch_shot_kernel(P, c->mode, c->mTld, c->mTrow, c->mLrow, c->st));
+    CK(cudaEventRecord(e1, c->st));
+    c->shot_events.emplace_back(e0, e1);
+    c->launches += 1;
     c->last_n = n;
     c->last_adj = adjoint;
     return RZ_OK;
@@ -374,6 +385,7 @@ void rz_destroy(rz_context *c) {
     cudaSetDevice(c->device);
     if (c->st) cudaStreamSynchronize(c->st);
     free_batch(c);
+    for (auto &pr : c->shot_events) cudaEventDestroy(pr.first), cudaEventDestroy(pr.second);
     dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dVp), dfree(c->dCube), dfree(c->dGrad), dfree(c->dL2);
     dfree(c->dRecH), dfree(c->dRecK), dfree(c->dRcH), dfree(c->dRcK), dfree(c->dRcRec), dfree(c->dSkip);
     dfree(c->dMA), dfree(c->dMB);
@@ -580,6 +592,7 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
     CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, c->st));
     if (!c->dL2) CK(dalloc(&c->dL2, 1));
     CK(launch_sum_l2(c->dl2, nshots, c->dL2, c->st));
+    c->launches += 3;
     if (have_dev(flags)) {
         if (L2) CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
         return RZ_OK;
@@ -616,6 +629,27 @@ int rz_shot_fields(rz_context *c, int shot, float *TT, float *lam, float *Tres, 
         CK(cudaMemcpyAsync(Tres, c->dTres + (size_t)shot * c->ntr, c->ntr * 4,
                            have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
+    return RZ_OK;
+}
+
+int rz_kernel_stats(rz_context *c, long long *launches, double *shot_kernel_ms, int *shot_kernel_calls) {
+    if (!c) return RZ_EINVAL;
+    cudaSetDevice(c->device);
+    double tot = 0.0;
+    int n = 0;
+    for (auto &pr : c->shot_events) {
+        CK(cudaEventSynchronize(pr.second));
+        float ms = 0.f;
+        CK(cudaEventElapsedTime(&ms, pr.first, pr.second));
+        tot += ms;
+        ++n;
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    c->shot_events.clear();
+    if (launches) *launches = c->launches;
+    if (shot_kernel_ms) *shot_kernel_ms = tot;
+    if (shot_kernel_calls) *shot_kernel_calls = n;
     return RZ_OK;
 }
 

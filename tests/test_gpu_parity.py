@@ -1,0 +1,264 @@
+"""GPU parity tests: the CUDA path (through the C ABI) against the oracle.
+
+Reference mode must reproduce the reference bit for bit (fields compared as
+values: +0 and -0 count as equal).  Fast mode must stay within 1e-5 relative
+of the FP64 oracle on traveltimes; on gradients it must be no further from the
+FP64 oracle than twice the reference's own float arithmetic plus 1e-4
+(relative L2), because the reference's float gradient itself sits ~1e-3 away.
+"""
+import ctypes as C
+import glob
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+import oracle as O
+from rajzel_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+TT_TOL = 1e-5
+GRAD_TOL = 1e-4
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, np.float32).tobytes()).hexdigest()
+
+
+@pytest.fixture(scope="module")
+def R(gpu_lib):
+    O.build(ref=False)
+    return gpu_lib
+
+
+def make_ctx(R, w, mode="reference", max_passes=500, ttnorm=None):
+    ctx = R.Context(0, mode)
+    ctx.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm if ttnorm is None else ttnorm, w.eps_adj, max_passes=max_passes)
+    ctx.set_slowness(synth.slowness(w.vp_true))
+    ctx.set_receivers(w.recx, w.recz)
+    return ctx
+
+
+def params(w):
+    return O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+
+
+# ---------------------------------------------------------------------------
+# golden fixtures (made by the reference's own code)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "fwd_*.npz"))))
+def test_forward_matches_golden(R, path):
+    d = np.load(path)
+    if str(d["kind"]) == "forward_digest":
+        w = synth.fwd_500x174()
+        ctx = make_ctx(R, w)
+        TT, Tmod, passes = ctx.eikonal(w.srcx[0], w.srcz[0])
+        assert digest(TT) == str(d["TT_sha256"])
+        assert np.array_equal(Tmod, d["Tmod"]) and passes == int(d["passes"])
+        return
+    w = synth.Workload("g", int(d["nx"]), int(d["ny"]), float(d["dh"]), float(d["time"]), float(d["ttnorm"]),
+                       float(d["eps_adj"]), d["vp"], d["vp"], d["srcx"], d["srcz"], d["recx"], d["recz"])
+    ctx = make_ctx(R, w)
+    TT, Tmod, passes = ctx.forward(w.srcx, w.srcz)
+    for i in range(len(w.srcx)):
+        assert digest(TT[i]) == str(d["TT_sha256"][i])
+        assert np.array_equal(Tmod[i], d["Tmod"][i])
+        assert passes[i] == d["passes"][i]
+
+
+@pytest.mark.parametrize("path", [p for p in sorted(glob.glob(os.path.join(GOLDEN, "grad_*.npz"))) if "muted" not in p])
+def test_gradient_matches_golden(R, path):
+    d = np.load(path)
+    w = synth.Workload("g", int(d["nx"]), int(d["ny"]), float(d["dh"]), float(d["time"]), float(d["ttnorm"]),
+                       float(d["eps_adj"]), d["vp"], d["vp"], d["srcx"], d["srcz"], d["recx"], d["recz"])
+    ctx = make_ctx(R, w)
+    grad, L2 = ctx.grad_obj(w.srcx, w.srcz, d["Tobs"])
+    assert np.array_equal(grad, d["grad"])
+    assert L2 == float(d["L2"])
+    TT, lam, Tres = ctx.shot_fields(0)
+    assert np.array_equal(Tres, d["shot0_Tres"])
+    assert np.array_equal(lam, d["shot0_lam"])
+    assert ctx.shot_info(0)[1] == int(d["shot0_adj_passes"])
+
+
+# ---------------------------------------------------------------------------
+# reference mode against the oracle on varied shapes
+# ---------------------------------------------------------------------------
+SHAPES = [(3, 3), (5, 40), (40, 30), (64, 64), (33, 97), (100, 77), (257, 130), (70, 512), (511, 33)]
+
+
+@pytest.mark.parametrize("nx,ny", SHAPES)
+def test_forward_reference_mode_bit_exact(R, nx, ny):
+    w = synth.small_case(nx * 1000 + ny, nx, ny, nshots=3)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    ctx = make_ctx(R, w)
+    TT, Tmod, passes = ctx.forward(w.srcx, w.srcz)
+    for i in range(3):
+        to, po = O.eikonal(p, S, w.srcx[i], w.srcz[i])
+        assert np.array_equal(TT[i], to), f"shot {i}: {int((TT[i] != to).sum())} cells differ"
+        assert passes[i] == po
+        assert np.array_equal(Tmod[i], O.calc_fa(p, to, w.recx, w.recz))
+
+
+def test_forward_sources_on_borders_and_corners(R):
+    nx, ny, dh = 70, 45, 10.0
+    w = synth.small_case(7, nx, ny, dh=dh, nshots=1)
+    xs = np.array([dh, nx * dh, dh, nx * dh, 35 * dh, dh, 35 * dh], np.float32)
+    zs = np.array([dh, dh, ny * dh, ny * dh, dh, 20 * dh, ny * dh], np.float32)
+    ctx = make_ctx(R, w)
+    TT, _, passes = ctx.forward(xs, zs)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    for i in range(len(xs)):
+        to, po = O.eikonal(p, S, xs[i], zs[i])
+        assert np.array_equal(TT[i], to) and passes[i] == po
+
+
+@pytest.mark.parametrize("nx,ny,dh", [(40, 30, 10.0), (100, 77, 12.5), (150, 130, 5.0), (90, 200, 20.0)])
+def test_gradient_reference_mode_bit_exact(R, nx, ny, dh):
+    w = synth.small_case(nx + 7 * ny, nx, ny, dh=dh, nshots=4)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    rng = np.random.default_rng(nx)
+    Tobs = np.empty((4, w.ntr), np.float32)
+    for i in range(4):
+        to, _ = O.eikonal(p, S * np.float32(0.97), w.srcx[i], w.srcz[i])
+        Tobs[i] = O.calc_fa(p, to, w.recx, w.recz) * (1 + 0.01 * rng.standard_normal(w.ntr)).astype(np.float32)
+    ctx = make_ctx(R, w)
+    grad, L2 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    go, L2o, fp, ap, _ = O.grad_obj(p, S, w.srcx, w.srcz, w.recx, w.recz, Tobs)
+    assert np.array_equal(grad, go), f"{int((grad != go).sum())} gradient cells differ"
+    assert L2 == L2o
+    for i in range(4):
+        assert ctx.shot_info(i)[:2] == (fp[i], ap[i])
+
+
+def test_eikonal_adj_entry_point(R):
+    w = synth.small_case(99, 80, 70, nshots=1)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    to, _ = O.eikonal(p, S, w.srcx[0], w.srcz[0])
+    Tmod = O.calc_fa(p, to, w.recx, w.recz)
+    Tres, _ = O.calc_res(p, to, Tmod, Tmod * np.float32(1.02), w.recx, w.recz)
+    ctx = make_ctx(R, w)
+    lam, passes = ctx.eikonal_adj(to, Tres)
+    lo, po = O.eikonal_adj(p, to, Tres, w.recx, w.recz)
+    assert np.array_equal(lam, lo) and passes == po
+
+
+def test_batched_equals_single_shot(R):
+    w = synth.small_case(5, 120, 90, nshots=5)
+    ctx = make_ctx(R, w)
+    TT, _, _ = ctx.forward(w.srcx, w.srcz)
+    for i in range(5):
+        t1, _, _ = ctx.eikonal(w.srcx[i], w.srcz[i])
+        assert np.array_equal(TT[i], t1)
+
+
+# ---------------------------------------------------------------------------
+# fast mode against the FP64 oracle
+# ---------------------------------------------------------------------------
+def test_fast_mode_traveltimes_within_tolerance(R):
+    w = synth.small_case(31, 200, 150, nshots=3)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    ctx = make_ctx(R, w, mode="fast")
+    TT, _, _ = ctx.forward(w.srcx, w.srcz)
+    for i in range(3):
+        t64, _ = O.eikonal_f64(p, S.astype(np.float64), w.srcx[i], w.srcz[i])
+        assert np.abs(TT[i] - t64).max() / np.abs(t64).max() <= TT_TOL
+
+
+def rel_l2(a, b):
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+
+def test_fast_mode_gradient_within_tolerance(R):
+    """The receiver scaling Tres/(dT/dz) (calc_FA_res.c:52-69) differences
+    neighbouring float traveltimes, so even the reference's own float
+    arithmetic sits ~1e-3 from the FP64 oracle on gradients.  Fast mode must
+    be no worse than that, plus GRAD_TOL."""
+    w = synth.small_case(32, 160, 100, nshots=4)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    rng = np.random.default_rng(3)
+    Tobs = np.empty((4, w.ntr), np.float32)
+    for i in range(4):
+        to, _ = O.eikonal(p, S * np.float32(0.97), w.srcx[i], w.srcz[i])
+        Tobs[i] = O.calc_fa(p, to, w.recx, w.recz) * (1 + 0.01 * rng.standard_normal(w.ntr)).astype(np.float32)
+    ctx = make_ctx(R, w, mode="fast")
+    grad, L2 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    g64, L64 = O.grad_obj_f64(p, S.astype(np.float64), w.srcx.astype(np.float64), w.srcz.astype(np.float64),
+                              w.recx, w.recz, Tobs.astype(np.float64))
+    g32, L32, _, _, _ = O.grad_obj(p, S, w.srcx, w.srcz, w.recx, w.recz, Tobs)
+    err_ref = rel_l2(g32, g64)
+    assert rel_l2(grad, g64) <= 2.0 * err_ref + GRAD_TOL
+    assert abs(L2 - L64) / abs(L64) <= 2.0 * abs(L32 - L64) / abs(L64) + GRAD_TOL
+
+
+# ---------------------------------------------------------------------------
+# arithmetic self-test and error handling
+# ---------------------------------------------------------------------------
+def test_certified_godunov_branch_matches_double(R):
+    lib = C.CDLL(os.path.join(os.path.dirname(R.__file__), "librz_selftest.so"))
+    lib.rz_selftest_godunov.argtypes = [C.c_ulonglong, C.c_long, C.POINTER(C.c_ulonglong)]
+    bad = C.c_ulonglong(1)
+    assert lib.rz_selftest_godunov(12345, 20_000_000, C.byref(bad)) == 0
+    assert bad.value == 0
+
+
+def test_errors_are_status_codes(R):
+    w = synth.small_case(1, 30, 20, nshots=1)
+    ctx = R.Context(0)
+    with pytest.raises(R.RajzelError) as e:
+        ctx.set_grid(30, 20, 10.0, 40.0, ttnorm=0.0)  # the reference would loop forever
+    assert e.value.status == R.RZ_EINVAL
+    with pytest.raises(R.RajzelError) as e:
+        ctx.set_grid(30, 600, 10.0, 40.0)
+    assert e.value.status == R.RZ_EUNSUPPORTED
+    ctx = make_ctx(R, w)
+    with pytest.raises(R.RajzelError) as e:
+        ctx.eikonal(-50.0, 10.0)  # source index 0 would be out of bounds in the reference
+    assert e.value.status == R.RZ_EINVAL
+    with pytest.raises(R.RajzelError) as e:
+        ctx.set_receivers(np.array([31], np.int32), np.array([2], np.int32))
+    assert e.value.status == R.RZ_EINVAL
+    ctx2 = make_ctx(R, w, max_passes=1)
+    with pytest.raises(R.RajzelError) as e:
+        ctx2.eikonal(w.srcx[0], w.srcz[0])
+    assert e.value.status == R.RZ_ENOCONV
+    # the context stays usable after errors
+    TT, _, _ = ctx.eikonal(w.srcx[0], w.srcz[0])
+    assert np.isfinite(TT).all()
+
+
+# ---------------------------------------------------------------------------
+# full-size workload: size-independent properties
+# ---------------------------------------------------------------------------
+def test_full_size_gradient_properties(R):
+    w = synth.grad_1700x350(nshots=8, ntr=850)
+    ctx_t = make_ctx(R, w, mode="fast")
+    _, Tobs, _ = ctx_t.forward(w.srcx, w.srcz, want_tt=False)
+    results = {}
+    for mode in ("reference", "fast"):
+        ctx = R.Context(0, mode)
+        ctx.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+        ctx.set_velocity(w.vp_start)
+        ctx.set_receivers(w.recx, w.recz)
+        results[mode] = ctx.grad_obj(w.srcx, w.srcz, Tobs) + (ctx,)
+    (gr, Lr, ctx_r), (gf, Lf, _) = results["reference"], results["fast"]
+    assert np.isfinite(gr).all() and np.isfinite(gf).all()
+    # two float evaluations of a gradient whose float error vs FP64 is ~1e-3
+    assert rel_l2(gf, gr) <= 5e-3
+    assert abs(Lf - Lr) / Lr <= 5e-3
+    TT, lam, _ = ctx_r.shot_fields(0)
+    hs, ks = synth.grid_index(w.srcx[0], w.dh) - 1, synth.grid_index(w.srcz[0], w.dh) - 1
+    assert TT[ks, hs] == 0.0 and (TT >= 0).all() and TT.max() < 2 * w.time
+    # reference mode at full size against the oracle for one shot
+    p = params(w)
+    S = synth.slowness(w.vp_start)
+    to, _ = O.eikonal(p, S, w.srcx[0], w.srcz[0])
+    assert np.array_equal(TT, to)

@@ -1,0 +1,135 @@
+"""CPU tests of the oracle: the C restatement against the reference's own
+compiled code and against the committed golden fixtures."""
+import ctypes as C
+import glob
+import hashlib
+import os
+
+import numpy as np
+import pytest
+
+from rajzel_gb300 import synth
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def digest(a):
+    return hashlib.sha256(np.ascontiguousarray(a, np.float32).tobytes()).hexdigest()
+
+
+def _params(O, d):
+    return O.Params(int(d["nx"]), int(d["ny"]), float(d["dh"]), float(d["time"]), float(d["ttnorm"]),
+                    float(d["eps_adj"]))
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "fwd_*.npz"))))
+def test_port_forward_matches_golden(oracle_mod, path):
+    O = oracle_mod
+    d = np.load(path)
+    if str(d["kind"]) == "forward_digest":
+        w = synth.fwd_500x174()
+        p = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+        TT, it = O.eikonal(p, synth.slowness(w.vp_true), w.srcx[0], w.srcz[0])
+        assert digest(TT) == str(d["TT_sha256"])
+        assert np.array_equal(O.calc_fa(p, TT, w.recx, w.recz), d["Tmod"])
+        assert it == int(d["passes"])
+        return
+    p = _params(O, d)
+    S = synth.slowness(d["vp"])
+    for i in range(len(d["srcx"])):
+        TT, it = O.eikonal(p, S, d["srcx"][i], d["srcz"][i])
+        assert digest(TT) == str(d["TT_sha256"][i])
+        if "TT" in d:
+            assert np.array_equal(TT, d["TT"][i])
+        assert np.array_equal(O.calc_fa(p, TT, d["recx"], d["recz"]), d["Tmod"][i])
+        assert it == d["passes"][i]
+
+
+@pytest.mark.parametrize("path", sorted(glob.glob(os.path.join(GOLDEN, "grad_*.npz"))))
+def test_port_gradient_matches_golden(oracle_mod, path):
+    O = oracle_mod
+    d = np.load(path)
+    p = _params(O, d)
+    S = synth.slowness(d["vp"])
+    grad, L2, fp, ap, Tres_last = O.grad_obj(p, S, d["srcx"], d["srcz"], d["recx"], d["recz"], d["Tobs"])
+    assert digest(grad) == str(d["grad_sha256"])
+    assert L2 == float(d["L2"])
+    assert np.array_equal(Tres_last, d["Tres_last"])
+    TT, _ = O.eikonal(p, S, d["srcx"][0], d["srcz"][0])
+    Tmod = O.calc_fa(p, TT, d["recx"], d["recz"])
+    Tres, _ = O.calc_res(p, TT, Tmod, d["Tobs"][0], d["recx"], d["recz"])
+    assert np.array_equal(Tres, d["shot0_Tres"])
+    lam, it = O.eikonal_adj(p, TT, Tres, d["recx"], d["recz"])
+    assert digest(lam) == str(d["shot0_lam_sha256"])
+    assert it == int(d["shot0_adj_passes"])
+
+
+def _random_case(rng):
+    nx, ny = int(rng.integers(4, 70)), int(rng.integers(4, 50))
+    dh = float(rng.choice([5.0, 10.0, 12.5, 20.0]))
+    w = synth.small_case(int(rng.integers(1 << 30)), nx, ny, dh=dh, nshots=3)
+    return w
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_port_equals_reference_random(oracle_mod, seed):
+    """The restatement and the reference's compiled sources agree bit for bit."""
+    O = oracle_mod
+    if not O.ref_available():
+        pytest.skip("reference sources not present on this machine")
+    rng = np.random.default_rng(100 + seed)
+    w = _random_case(rng)
+    ttnorm = float(rng.choice([1e-6, 1e-10]))
+    p = O.Params(w.nx, w.ny, w.dh, w.time, ttnorm, w.eps_adj)
+    S = synth.slowness(w.vp_true)
+    ref = O.Ref(p)
+    for i in range(3):
+        TTr, Tm, itr = ref.eikonal(S, w.srcx[i], w.srcz[i], w.recx, w.recz)
+        TTp, itp = O.eikonal(p, S, w.srcx[i], w.srcz[i])
+        assert np.array_equal(TTr, TTp) and itr == itp
+        Tobs = (Tm * (1 + 0.02 * rng.standard_normal(w.ntr))).astype(np.float32)
+        Tobs[rng.random(w.ntr) < 0.1] = -1.0
+        Tr_r, _ = ref.calc_res(TTr, Tm, Tobs, w.recx, w.recz)
+        Tr_p, _ = O.calc_res(p, TTp, Tm, Tobs, w.recx, w.recz)
+        assert np.array_equal(Tr_r, Tr_p)
+        Lr, itr = ref.eikonal_adj(TTr, Tr_r, w.recx, w.recz)
+        Lp, itp = O.eikonal_adj(p, TTp, Tr_p, w.recx, w.recz)
+        assert np.array_equal(Lr, Lp) and itr == itp
+    Tobs = np.abs(rng.normal(1.0, 0.5, (3, w.ntr))).astype(np.float32)
+    Tobs[rng.random(Tobs.shape) < 0.1] = -1.0  # muted picks: Tres carries over between shots
+    gr, L2r, Tres_r = ref.grad_obj(S, w.srcx, w.srcz, w.recx, w.recz, Tobs)
+    gp, L2p, _, _, Tres_p = O.grad_obj(p, S, w.srcx, w.srcz, w.recx, w.recz, Tobs)
+    assert np.array_equal(gr, gp) and L2r == L2p and np.array_equal(Tres_r, Tres_p)
+
+
+def test_fp64_oracle_close_to_float(oracle_mod):
+    O = oracle_mod
+    w = synth.small_case(5, 60, 40, nshots=1)
+    p = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    S = synth.slowness(w.vp_true)
+    t32, _ = O.eikonal(p, S, w.srcx[0], w.srcz[0])
+    t64, _ = O.eikonal_f64(p, S.astype(np.float64), w.srcx[0], w.srcz[0])
+    assert np.abs(t32 - t64).max() / np.abs(t64).max() < 1e-5
+
+
+def test_pow_cube_pin(oracle_mod):
+    """ass_grad.c:23 uses libm pow(S,3.0); it is faithful but not always the
+    correctly rounded cube, which is why the reference-mode GPU stack takes
+    the per-cell cube from the host C library.  The count is recorded."""
+    O = oracle_mod
+    lib = C.CDLL(O.PORT_SO)
+    lib.rzo_pin_cube.argtypes = [C.c_float, C.c_float]
+    lib.rzo_pin_cube.restype = C.c_long
+    n = lib.rzo_pin_cube(1.0 / 5000.0, 1.0 / 4000.0)
+    assert n >= 0
+
+
+def test_shot_partition_matches_init_mpishot(oracle_mod):
+    """init_MPIshot.c:19-30: contiguous blocks, the first nshots%NP ranks get one more."""
+    O = oracle_mod
+    for nshots, np_ in [(100, 8), (7, 3), (5, 5), (3, 4)]:
+        spans = [O.shot_partition(nshots, np_, r) for r in range(np_)]
+        assert spans[0][0] == 1 and spans[-1][1] == nshots + 1
+        assert all(spans[i][1] == spans[i + 1][0] for i in range(np_ - 1))
+        sizes = [b - a for a, b in spans]
+        assert max(sizes) - min(sizes) <= 1 and sizes == sorted(sizes, reverse=True)
