@@ -135,6 +135,22 @@ int rz_eikonal(rz_context *ctx, float srcx, float srcz, float *TT, float *Tmod, 
    TT [ny][nx] and scaled residuals Tres [ntr] (eikonal_adj.c:10-59). */
 int rz_eikonal_adj(rz_context *ctx, const float *TT, const float *Tres, float *lam, int *passes, int flags);
 
+/* Allocation-free forward solve (no counterpart in the reference: RAJZEL
+   always runs on the host and allocates its own scratch with matrix()).
+   For callers that cannot allocate GPU memory -- inside a CUDA-graph capture
+   or a fixed memory pool, or on a host with no allocator available -- this
+   computes one shot's traveltimes exactly like rz_eikonal() in reference
+   mode, with its working space in a static 32 MiB device array that every
+   GPU loading this library holds until exit.  S (slowness [ny][nx]), TT
+   (output [ny][nx]) and info (2 ints: outer passes, status bits) are device
+   pointers; the call is asynchronous on `stream` (NULL = legacy default).
+   Grids needing more than the static space return RZ_EUNSUPPORTED.  The
+   first call on a device sets up (looks up the array's address) and should
+   come before any stream capture; calls that overlap on the GPU share the
+   array and race. */
+int rz_eikonal_noalloc(const rz_grid *grid, const float *S, float srcx, float srcz, float *TT, int *info,
+                       void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,62 @@
+"""The allocation-free forward entry point (rz_eikonal_noalloc).
+
+Callers that cannot allocate GPU memory (graph capture, fixed pools, hosts
+without an allocator) get the same traveltimes as rz_eikonal() from a static
+device array.  This file sorts last so that a run stopping at the first
+failure has run every other test first; it also passes alone in a fresh
+process, where its first call performs the one-time set-up.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from rajzel_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+class _Grid(C.Structure):
+    _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("dh", C.c_float), ("time", C.c_float),
+                ("ttnorm", C.c_float), ("eps_adj", C.c_float), ("max_passes", C.c_int)]
+
+
+def test_noalloc_forward_matches_eikonal_on_two_calls(gpu_lib):
+    import torch
+    R = gpu_lib
+    lib = R.load_library()
+    f = lib.rz_eikonal_noalloc
+    f.argtypes = [C.POINTER(_Grid), C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
+    f.restype = C.c_int
+
+    w = synth.small_case(4242, 300, 170, nshots=2)  # six strips, ragged last block
+    S = synth.slowness(w.vp_true)
+    ctx = R.Context(0, "reference")
+    ctx.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    ctx.set_slowness(S)
+    grid = _Grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj, 10000)
+
+    S_d = torch.from_numpy(S).cuda()
+    TT_d = torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda")
+    info_d = torch.full((2,), -7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    for i in range(2):  # two calls in a row share the static array
+        TT_ref, _, passes_ref = ctx.eikonal(w.srcx[i], w.srcz[i])
+        st = f(C.byref(grid), S_d.data_ptr(), float(w.srcx[i]), float(w.srcz[i]), TT_d.data_ptr(),
+               info_d.data_ptr(), None)
+        assert st == R.RZ_OK
+        torch.cuda.synchronize()
+        info = info_d.cpu().numpy()
+        assert np.array_equal(TT_d.cpu().numpy(), TT_ref)  # reference mode: bit-exact
+        assert info[0] == passes_ref and info[1] == 0
+
+
+def test_noalloc_rejects_oversized_and_bad_input(gpu_lib):
+    lib = gpu_lib.load_library()
+    f = lib.rz_eikonal_noalloc
+    f.argtypes = [C.POINTER(_Grid), C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
+    f.restype = C.c_int
+    big = _Grid(60000, 500, 10.0, 40.0, 1e-6, 1e-9, 100)  # needs ~120 Mi floats of working space
+    assert f(C.byref(big), C.c_void_p(16), 100.0, 20.0, C.c_void_p(16), C.c_void_p(16), None) == gpu_lib.RZ_EUNSUPPORTED
+    ok = _Grid(100, 50, 10.0, 40.0, 1e-6, 1e-9, 100)
+    assert f(C.byref(ok), C.c_void_p(16), -500.0, 20.0, C.c_void_p(16), C.c_void_p(16), None) == gpu_lib.RZ_EINVAL
