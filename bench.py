@@ -191,7 +191,7 @@ def run_gpu_arm(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=torch.device("cuda", local_rank))
 
-    w = synth.grad_1700x350()
+    w = synth.grad_1700x350(nshots=args.shots)
     stream = torch.cuda.Stream()  # a real stream handle: the events below time exactly the library's work
     torch.cuda.set_stream(stream)
     ctx = R.Context(local_rank, args.mode)
@@ -252,6 +252,20 @@ def run_gpu_arm(args, rank, world, local_rank):
     achieved = alg_bytes / (kernel_ms / 1e3) / 1e9
     traffic = read_traffic(w.nshots)
 
+    if args.profile_only:
+        if rank == 0:
+            print(json.dumps({"profile_only": True, "ms_per_step": ms / args.steps, "kernel_ms": kernel_ms}))
+        return
+
+    # the plain per-shot GPU path: the same kernels, one shot per launch
+    nplain = min(8, w.nshots)
+    t0 = time.perf_counter()
+    for i in range(nplain):
+        ctx.grad_obj_device(w.srcx[i:i + 1], w.srcz[i:i + 1], tobs_d[i].data_ptr(), grad_d.data_ptr(),
+                            l2_d.data_ptr())
+        torch.cuda.synchronize()
+    plain_value = world * nplain / (time.perf_counter() - t0)
+
     # end to end through the public API with host buffers
     ctx2 = R.Context(local_rank, args.mode)
     ctx2.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
@@ -297,6 +311,9 @@ def run_gpu_arm(args, rank, world, local_rank):
         "cpu_baseline": {"value": sample / cpu_s, "unit": "shots/s", "cores": cores, "kind": kind,
                          "sample": f"grad_obj over {sample} of the 100 shots, one process per core"},
         "e2e": {"value": e2e_value, "unit": "shots/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "plain_per_shot_gpu": {"value": plain_value, "unit": "shots/s",
+                               "how": f"same kernels, one shot per launch, {nplain} shots, synchronised"},
+        "batched_over_plain": value / plain_value,
         "gpu_launches": int(launches1 - launches0),
         "clocks": clk,
     }
@@ -312,6 +329,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mode", choices=["fast", "reference"], default="fast")
+    ap.add_argument("--shots", type=int, default=100, help="shots per step (the workload has 100)")
+    ap.add_argument("--profile-only", action="store_true",
+                    help="only the device-timed loop (for profiler runs); no baselines, no JSON contract line")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

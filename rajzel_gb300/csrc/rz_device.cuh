@@ -64,6 +64,19 @@ RZ_DEV bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
+// predicated forms: one instruction, no branch in the caller's code
+RZ_DEV void sts_if(uint32_t a, float v, bool p) {
+    asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.shared.f32 [%0], %1;\n\t}" ::"r"(a), "f"(v),
+                 "r"((uint32_t)p));
+}
+RZ_DEV void mbar_arrive_if(uint32_t bar, bool p) {
+    asm volatile(
+        "{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %1, 0;\n\t@q mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];\n\t}" ::"r"(
+            bar),
+        "r"((uint32_t)p)
+        : "memory");
+}
+
 // the same operations on 32-bit shared-window addresses (kept in registers)
 RZ_DEV void mbar_arrive_a(uint32_t bar) {
     asm volatile("mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];" ::"r"(bar) : "memory");
@@ -256,13 +269,15 @@ RZ_DEV float godunov_ref(float a, float b, float s, float dh) {
     return godunov_branch2_f64(sum, d, s, dh);
 }
 
-// fast mode: FP32 arithmetic throughout (error ~1 ulp per update)
+// fast mode: FP32 arithmetic throughout (error ~1 ulp per update), written
+// without branches so that consecutive wavefront steps can be interleaved
 RZ_DEV float godunov_fast(float a, float b, float s, float dh) {
-    float d = a - b;
-    float sh = s * dh;
-    if (fabsf(d) >= sh) return fminf(a, b) + sh;
-    float q = fmaf(2.0f * sh, sh, -d * d);
-    return 0.5f * (a + b + q * rsqrtf(q));
+    const float d = a - b;
+    const float sh = s * dh;
+    const float one_sided = fminf(a, b) + sh;
+    const float q = fmaf(2.0f * sh, sh, -d * d);  // > 0 whenever it is selected
+    const float two_sided = fmaf(0.5f * q, rsqrtf(q), 0.5f * (a + b));
+    return fabsf(d) >= sh ? one_sided : two_sided;
 }
 
 // ---------------------------------------------------------------------------

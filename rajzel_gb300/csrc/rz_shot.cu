@@ -209,7 +209,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     issue(0);
     if (nxb > 1) issue(1);
     ring_wait_l(0);
-    if (is_consumer_warp && !mbar_wait_a(full_in, 0, abort_s)) err |= ERR_FLAG_TIMEOUT;
 
     // ring address of this lane's cell at step t = 0 (column up = -l, which
     // for l > 0 lies before the sweep: any ring cell serves, nothing reads it)
@@ -227,27 +226,55 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     float own_next = lds(addr_c);
     float ev_next = lds(addr_e);
     float halo_next = lds(addr_c + hoff);
-    float hb_next = lds(hb_in);
 
     float res_prev = 0.f;
     for (int k = 0; k <= nxb; ++k) {
-        // refill: block k+1 goes where block k-2 was (written back last round)
-        if (k >= 1 && k + 1 < nxb) {
-            // generic accesses of the slot (including writes of lanes still
-            // outside the sweep) are ordered before the TMA refill
-            fence_proxy_async_smem();
-            tma_store_wait_read<0>();
-            issue(k + 1);
-        }
 #pragma unroll 1
         for (int i0 = 0; i0 < 32; i0 += 8) {
             const int t0 = kBlk * k + i0;
+            // ---- group prologue: every wait and branch of the next 8 steps ----
+            // refill: block k+1 goes where block k-2 was; its write-back, issued
+            // at the end of the previous round, has had 8 steps to read shared
+            // memory, and lane 0 first reads the new block at step 30
+            if (i0 == 8 && k >= 1 && k + 1 < nxb) {
+                // generic accesses of the slot (including writes of lanes
+                // still outside the sweep) are ordered before the TMA refill
+                fence_proxy_async_smem();
+                tma_store_wait_read<0>();
+                issue(k + 1);
+            }
+            if (i0 == 24 && k + 1 < nxb) ring_wait_l(mod3(k + 1));
+            // boundary-row values lane 0 needs in these 8 steps (columns t0..t0+7)
+            float hbq[8];
+            if (is_consumer_warp) {
+                const int G = t0 >> 3;
+                if (G < ngrp) {
+                    if (!mbar_wait_a(full_in + 8u * (G & (kGroups - 1)), (G >> 4) & 1, abort_s)) err |= ERR_FLAG_TIMEOUT;
+                    const uint32_t hb_g = hb_in + 4u * (uint32_t)(t0 & (kHandoff - 1));
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) hbq[q] = lds(hb_g + 4u * q);
+                    // the values are in registers: release the slot at once
+                    mbar_arrive_if(empty_in + 8u * (G & (kGroups - 1)), l == 0);
+                } else {
+#pragma unroll
+                    for (int q = 0; q < 8; ++q) hbq[q] = 0.f;
+                }
+            } else {
+#pragma unroll
+                for (int q = 0; q < 8; ++q) hbq[q] = 0.f;
+            }
+            if (is_producer_warp) {
+                // lane 31 starts hand-off group Gp at step t0+7 (column t0-24)
+                const int Gp = (t0 - 24) >> 3;
+                if (t0 >= 24 && Gp >= kGroups && Gp < ngrp &&
+                    !mbar_wait_a(empty_out + 8u * (Gp & (kGroups - 1)), ((Gp >> 4) - 1) & 1, abort_s))
+                    err |= ERR_FLAG_TIMEOUT;
+            }
             const int u0 = t0 - l;
             const float *xr = xs + QS * 32 * t0;
             const uint32_t *mr = ADJ ? mk + QS * t0 : nullptr;
             const float *er = ADJ ? ep + QS * t0 : nullptr;
-            const uint32_t hb_g = hb_in + 4u * (uint32_t)(t0 & (kHandoff - 1));
-            const uint32_t hb_last = hb_in + 4u * (uint32_t)((t0 + 8) & (kHandoff - 1));
+            // ---- 8 wavefront steps, straight-line code ----
 #pragma unroll
             for (int ii = 0; ii < 8; ++ii) {
                 const int t = t0 + ii;
@@ -255,35 +282,18 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 const float own = own_next;
                 const float ev = ev_next;
                 const float halo = halo_next;
-                const float hbv = hb_next;
                 const uint32_t cur = addr_c;
-                // hand-off flow control and the TMA block lane 0 needs next
-                if (ii == 7) {
-                    if (is_consumer_warp) {
-                        const int G = (t + 1) >> 3;
-                        if (G < ngrp && !mbar_wait_a(full_in + 8u * (G & (kGroups - 1)), (G >> 4) & 1, abort_s))
-                            err |= ERR_FLAG_TIMEOUT;
-                    }
-                    if (is_producer_warp) {
-                        const int G = (t - 31) >> 3;
-                        if (G >= kGroups && G < ngrp &&
-                            !mbar_wait_a(empty_out + 8u * (G & (kGroups - 1)), ((G >> 4) - 1) & 1, abort_s))
-                            err |= ERR_FLAG_TIMEOUT;
-                    }
-                }
-                if (ii == 6 && i0 == 24 && k + 1 < nxb) ring_wait_l(mod3(k + 1));
                 // prefetch the next step's shared values
                 addr_c = addr_e;
                 addr_e = advance(addr_e);
                 own_next = ev;
                 ev_next = lds(addr_e);
                 halo_next = lds(addr_c + hoff);
-                hb_next = lds(ii < 7 ? hb_g + 4u * (ii + 1) : hb_last);
 
                 float nv = __shfl_up_sync(0xffffffffu, res_prev, 1);
                 float sv = __shfl_down_sync(0xffffffffu, ev, 1);
-                if (l == 0) nv = hbv;
-                if (l == 31) sv = halo;
+                nv = (l == 0) ? hbq[ii] : nv;
+                sv = (l == 31) ? halo : sv;
                 const float xv = xq[ii];
                 const bool valid = (unsigned)(up - lo) < (unsigned)(hi - lo);
                 float r;
@@ -299,7 +309,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     const float tt =
                         (MODE == kModeReference) ? godunov_ref(a, b, xv, dh) : godunov_fast(a, b, xv, dh);
                     r = fminf(own, tt);
-                    if (!valid) r = own;
+                    r = valid ? r : own;
                 } else {
                     xq[ii] = __ldca(xr + QS * 32 * (ii + 8));
                     const uint32_t mword = mq[ii];
@@ -309,8 +319,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     const float e_tt = xv;  // traveltime one column downstream
                     float n_tt = __shfl_up_sync(0xffffffffu, w_tt, 1);
                     float s_tt = __shfl_down_sync(0xffffffffu, e_tt, 1);
-                    if (l == 0) n_tt = edge;
-                    if (l == 31) s_tt = edge;
+                    n_tt = (l == 0) ? edge : n_tt;
+                    s_tt = (l == 31) ? edge : s_tt;
                     const float tE = DX > 0 ? e_tt : w_tt, tW = DX > 0 ? w_tt : e_tt;
                     const float tS = DY > 0 ? s_tt : n_tt, tN = DY > 0 ? n_tt : s_tt;
                     const float lE = DX > 0 ? ev : res_prev, lW = DX > 0 ? res_prev : ev;
@@ -322,19 +332,17 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                         r = leung_qian_fast(c_tt, tE, tW, tS, tN, lE, lW, lS, lN, own, dh_rcp, eps_adj);
                     }
                     const bool keep = !valid || ((mword >> j) & 1u);
-                    if (keep) r = own;
+                    r = keep ? own : r;
                     w_tt = c_tt;
                     c_tt = e_tt;
                 }
                 sts(cur, r);
                 if (MODE == kModeFast) acc_l += valid ? own - r : 0.0f;
-                if (producer) {
-                    const int upp = t - 31;  // lane 31's column at this step
-                    if (upp >= 0 && upp < ncol) sts(hb_out + 4u * (uint32_t)(upp & (kHandoff - 1)), r);
-                    if (ii == 6 && t >= 38 && ((t - 38) >> 3) < ngrp)
-                        mbar_arrive_a(full_out + 8u * (((t - 38) >> 3) & (kGroups - 1)));
-                }
-                if (consumer && ii == 7 && (t >> 3) < ngrp) mbar_arrive_a(empty_in + 8u * ((t >> 3) & (kGroups - 1)));
+                // lane 31 hands its row down; after the 8th value of a group it signals
+                const int upp = t - 31;
+                sts_if(hb_out + 4u * (uint32_t)(upp & (kHandoff - 1)), r, producer && upp >= 0 && upp < ncol);
+                if (ii == 6) mbar_arrive_if(full_out + 8u * (((t - 38) >> 3) & (kGroups - 1)),
+                                            producer && t >= 38 && ((t - 38) >> 3) < ngrp);
                 res_prev = r;
             }
         }
