@@ -31,9 +31,6 @@ RZ_OK, RZ_EINVAL, RZ_ENOCONV, RZ_ECUDA, RZ_ENOMEM, RZ_ETIMEOUT, RZ_ESTATE, RZ_EU
 RZ_MODE_REFERENCE, RZ_MODE_FAST = 0, 1
 RZ_DEVICE_PTRS = 1
 
-MAX_NY = 512  # rows per shot handled by one CTA in this build
-
-
 class RajzelError(RuntimeError):
     def __init__(self, status: int, msg: str):
         super().__init__(f"[{status}] {msg}")

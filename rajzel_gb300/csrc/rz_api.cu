@@ -416,8 +416,6 @@ int rz_set_grid(rz_context *c, const rz_grid *g) {
         return fail(c, RZ_EINVAL, "TTNORM must be > 0 (the reference never terminates otherwise)");
     if (!std::isfinite(g->time) || !std::isfinite(g->eps_adj)) return fail(c, RZ_EINVAL, "TIME/EPS_ADJ not finite");
     const int nstrips = (g->ny + kStrip - 1) / kStrip;
-    if (nstrips > kMaxWarps)
-        return fail(c, RZ_EUNSUPPORTED, "NY=%d exceeds %d rows per shot in this build", g->ny, kMaxWarps * kStrip);
     cudaSetDevice(c->device);
     const bool same_shape = c->grid_set && c->g.nx == g->nx && c->g.ny == g->ny;
     c->g = *g;

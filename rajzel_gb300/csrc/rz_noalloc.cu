@@ -96,7 +96,6 @@ extern "C" int rz_eikonal_noalloc(const rz_grid *grid, const float *S, float src
     const rz_grid g = *grid;
     if (g.nx < 3 || g.ny < 3 || !(g.dh > 0.f) || !(g.ttnorm > 0.f) || !std::isfinite(g.time)) return RZ_EINVAL;
     const int nstrips = (g.ny + kStrip - 1) / kStrip;
-    if (nstrips > kMaxWarps) return RZ_EUNSUPPORTED;
     const int hs = (int)std::floor((double)(srcx / g.dh) + 0.5) - 1;
     const int ks = (int)std::floor((double)(srcz / g.dh) + 0.5) - 1;
     if (!std::isfinite(srcx) || !std::isfinite(srcz) || hs < 0 || hs >= g.nx || ks < 0 || ks >= g.ny)

@@ -105,10 +105,15 @@ constexpr int kRowFloats = kRing * kBlk;          // 96
 constexpr int kRowBytes = kRowFloats * 4;         // 384
 
 template <int DX, int DY, bool ADJ, int MODE>
-__device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mrow, float &acc) {
+__device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mrow, float &acc, int band,
+                                   int W) {
     const int l = w.l, g = w.g;
-    if (g >= P.nstrips) return;
-    const int s = DY > 0 ? g : P.nstrips - 1 - g;
+    // strips are swept in bands of W (one strip per warp); sig is the strip's
+    // position in sweep order, s its index from the top of the grid
+    const int sig = band * W + g;
+    if (sig >= P.nstrips) return;
+    const int z = w.z;
+    const int s = DY > 0 ? sig : P.nstrips - 1 - sig;
     const int j = DY > 0 ? l : 31 - l;
     const int row = kStrip * s + j;
     const bool rowok = row < P.ny;
@@ -118,8 +123,16 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const bool hasUp = DY > 0 ? (row > 0) : (row < P.ny - 1);
     const bool hasDn = DY > 0 ? (row < P.ny - 1) : (row > 0);
     const int nxb = P.nxb, ncol = kBlk * nxb, nx = P.nx;
-    const bool is_producer_warp = (g + 1 < P.nstrips);
+    const bool is_producer_warp = (g + 1 < W) && (sig + 1 < P.nstrips);
     const bool is_consumer_warp = (g > 0);
+    // the first warp of a later band reads its upstream row (final for this
+    // sweep: the previous band is complete) from global memory
+    const bool reads_prev_band = (g == 0) && (band > 0);
+    const float *prev_row = nullptr;
+    if (reads_prev_band) {
+        const int rup = DY > 0 ? kStrip * s - 1 : kStrip * s + kStrip;
+        prev_row = (ADJ ? P.L : P.T) + (size_t)z * P.fstride + (size_t)rup * P.nxp;
+    }
     const bool producer = (l == 31) && is_producer_warp;
     const bool consumer = (l == 0) && is_consumer_warp;
     const int ngrp = ncol >> 3;  // hand-off groups per sweep
@@ -130,7 +143,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const int hoff = (halorow - boxrow) * kRowBytes;
     const uint32_t hb_in = smem_u32(w.ws->hb);
     const uint32_t hb_out = smem_u32(is_producer_warp ? w.ws_down->hb : w.ws->hb);
-    const int z = w.z;
     const float dh = P.dh;
     const float dh_rcp = P.dh_rcp, eps_adj = P.eps_adj;
     const bool div_fast = P.div_fast != 0;
@@ -258,6 +270,14 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 } else {
 #pragma unroll
                     for (int q = 0; q < 8; ++q) hbq[q] = 0.f;
+                }
+            } else if (reads_prev_band) {
+                // lane 0's columns t0..t0+7 of the row above the band (written by
+                // TMA earlier in this launch: read through L2)
+#pragma unroll
+                for (int q = 0; q < 8; ++q) {
+                    const int uq = min(max(t0 + q, 0), ncol - 1);
+                    hbq[q] = __ldcg(prev_row + (DX > 0 ? uq : ncol - 1 - uq));
                 }
             } else {
 #pragma unroll
@@ -456,10 +476,8 @@ RZ_DEV void copy_field(const ShotParams &P, const float *src, float *dst) {
 // Skewed copies of the converged traveltimes for the adjoint sweeps, plus the
 // rows bordering each strip (TMA tiles in, coalesced skew lines out).
 template <int DUMMY>
-__device__ __noinline__ void relayout(const ShotParams &P, Warp &w, const CUtensorMap *mld) {
-    const int l = w.l, g = w.g, z = w.z;
-    if (g >= P.nstrips) return;
-    const int s = g;
+__device__ __noinline__ void relayout_strip(const ShotParams &P, Warp &w, const CUtensorMap *mld, int s) {
+    const int l = w.l, z = w.z;
     float *ring = &w.ws->ring[0][0];
     const int nxb = P.nxb;
     float *ta = P.TA + (size_t)z * P.sstride + ((size_t)s * P.qn + kSkewFront) * 32;
@@ -555,6 +573,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
     float *Told = P.Told + (size_t)z * P.fstride;
     float *L = P.L + (size_t)z * P.fstride;
     const int n = P.nx * P.ny;
+    const int nbands = (P.nstrips + W - 1) / W;
     int cta_err = 0;
 
     if (!P.start_adjoint) {
@@ -581,15 +600,23 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
                 __syncthreads();
             }
             float acc = 0.f;
-            sweep<+1, +1, false, MODE>(P, w, &mTrow, acc);
-            sweep_barrier(sh);
+            for (int b = 0; b < nbands; ++b) {
+                sweep<+1, +1, false, MODE>(P, w, &mTrow, acc, b, W);
+                sweep_barrier(sh);
+            }
             if (pass == 0) stamp(P, z, 5);
-            sweep<-1, +1, false, MODE>(P, w, &mTrow, acc);
-            sweep_barrier(sh);
-            sweep<-1, -1, false, MODE>(P, w, &mTrow, acc);
-            sweep_barrier(sh);
-            sweep<+1, -1, false, MODE>(P, w, &mTrow, acc);
-            sweep_barrier(sh);
+            for (int b = 0; b < nbands; ++b) {
+                sweep<-1, +1, false, MODE>(P, w, &mTrow, acc, b, W);
+                sweep_barrier(sh);
+            }
+            for (int b = 0; b < nbands; ++b) {
+                sweep<-1, -1, false, MODE>(P, w, &mTrow, acc, b, W);
+                sweep_barrier(sh);
+            }
+            for (int b = 0; b < nbands; ++b) {
+                sweep<+1, -1, false, MODE>(P, w, &mTrow, acc, b, W);
+                sweep_barrier(sh);
+            }
             ++pass;
             if (*w.abort_word) break;
             if (MODE == kModeReference) {
@@ -666,7 +693,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
         if (tid == 0) atomicOr(&P.status[z], cta_err);
         return;
     }
-    relayout<0>(P, w, &mTld);
+    for (int s = g; s < P.nstrips; s += W) relayout_strip<0>(P, w, &mTld, s);
     // lambda: 0 on the frame, 10*TIME inside, residuals at receiver cells
     const float linit = (float)(10.0 * (double)P.time);
     for (int c = tid; c < n; c += blockDim.x) {
@@ -695,15 +722,23 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
             __syncthreads();
         }
         float acc = 0.f;
-        sweep<+1, +1, true, MODE>(P, w, &mLrow, acc);
-        sweep_barrier(sh);
+        for (int b = 0; b < nbands; ++b) {
+                sweep<+1, +1, true, MODE>(P, w, &mLrow, acc, b, W);
+                sweep_barrier(sh);
+            }
         if (pass == 0) stamp(P, z, 6);
-        sweep<+1, -1, true, MODE>(P, w, &mLrow, acc);
-        sweep_barrier(sh);
-        sweep<-1, +1, true, MODE>(P, w, &mLrow, acc);
-        sweep_barrier(sh);
-        sweep<-1, -1, true, MODE>(P, w, &mLrow, acc);
-        sweep_barrier(sh);
+        for (int b = 0; b < nbands; ++b) {
+                sweep<+1, -1, true, MODE>(P, w, &mLrow, acc, b, W);
+                sweep_barrier(sh);
+            }
+        for (int b = 0; b < nbands; ++b) {
+                sweep<-1, +1, true, MODE>(P, w, &mLrow, acc, b, W);
+                sweep_barrier(sh);
+            }
+        for (int b = 0; b < nbands; ++b) {
+                sweep<-1, -1, true, MODE>(P, w, &mLrow, acc, b, W);
+                sweep_barrier(sh);
+            }
         ++pass;
         if (*w.abort_word) break;
         if (MODE == kModeReference) {
@@ -722,8 +757,9 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
 
 cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const CUtensorMap &mTld, const CUtensorMap &mTrow,
                                const CUtensorMap &mLrow, cudaStream_t st) {
-    const int W = P.nstrips;
-    if (W < 1 || W > kMaxWarps) return cudaErrorInvalidValue;
+    if (P.nstrips < 1) return cudaErrorInvalidValue;
+    const int nb = (P.nstrips + kMaxWarps - 1) / kMaxWarps;  // bands per sweep
+    const int W = (P.nstrips + nb - 1) / nb;                  // warps per CTA, bands balanced
     const size_t smem = shot_kernel_smem(W);
     dim3 grid(P.nshots), block(32 * W);
     cudaError_t e;

@@ -86,7 +86,9 @@ def test_gradient_matches_golden(R, path):
 # ---------------------------------------------------------------------------
 # reference mode against the oracle on varied shapes
 # ---------------------------------------------------------------------------
-SHAPES = [(3, 3), (5, 40), (40, 30), (64, 64), (33, 97), (100, 77), (257, 130), (70, 512), (511, 33)]
+# 70x512 fills 16 warps; 40x600 and 37x1100 are swept in 2 and 3 bands of strips
+SHAPES = [(3, 3), (5, 40), (40, 30), (64, 64), (33, 97), (100, 77), (257, 130), (70, 512), (511, 33), (40, 600),
+          (37, 1100)]
 
 
 @pytest.mark.parametrize("nx,ny", SHAPES)
@@ -117,7 +119,8 @@ def test_forward_sources_on_borders_and_corners(R):
         assert np.array_equal(TT[i], to) and passes[i] == po
 
 
-@pytest.mark.parametrize("nx,ny,dh", [(40, 30, 10.0), (100, 77, 12.5), (150, 130, 5.0), (90, 200, 20.0)])
+@pytest.mark.parametrize("nx,ny,dh", [(40, 30, 10.0), (100, 77, 12.5), (150, 130, 5.0), (90, 200, 20.0),
+                                      (50, 700, 10.0)])
 def test_gradient_reference_mode_bit_exact(R, nx, ny, dh):
     w = synth.small_case(nx + 7 * ny, nx, ny, dh=dh, nshots=4)
     p = params(w)
@@ -216,9 +219,6 @@ def test_errors_are_status_codes(R):
     with pytest.raises(R.RajzelError) as e:
         ctx.set_grid(30, 20, 10.0, 40.0, ttnorm=0.0)  # the reference would loop forever
     assert e.value.status == R.RZ_EINVAL
-    with pytest.raises(R.RajzelError) as e:
-        ctx.set_grid(30, 600, 10.0, 40.0)
-    assert e.value.status == R.RZ_EUNSUPPORTED
     ctx = make_ctx(R, w)
     with pytest.raises(R.RajzelError) as e:
         ctx.eikonal(-50.0, 10.0)  # source index 0 would be out of bounds in the reference
