@@ -322,6 +322,150 @@ def run_gpu_arm(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+# ---------------------------------------------------------------------------
+# the other named workloads (one JSON line each; the default run is the one above)
+# ---------------------------------------------------------------------------
+def _events_ms(fn, stream, steps):
+    import torch
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(steps):
+        fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1) / steps
+
+
+def _context(R, w, mode, stream, vp):
+    ctx = R.Context(torch_device_index(), mode)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    ctx.set_receivers(w.recx, w.recz)
+    ctx.set_velocity(vp)
+    return ctx
+
+
+def torch_device_index():
+    import torch
+    return torch.cuda.current_device()
+
+
+def run_workload(args, local_rank):
+    """fwd_500x174: one forward solve (latency); uneven: 256 shots over three
+    grids, forward + adjoint gradient; stress: 1024 shots on 8192 x 2048
+    under a 120 GB cap on the field slots."""
+    import numpy as np
+    import torch
+    import rajzel_gb300 as R
+    from rajzel_gb300 import build as B
+    from rajzel_gb300 import synth
+    B.build()
+    torch.cuda.set_device(local_rank)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    out = {"workload": args.workload, "mode": args.mode, "data": "synthetic (seeded)"}
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.3)
+    t_wall0 = time.time()
+    if args.workload == "fwd_500x174":
+        w = synth.fwd_500x174()
+        ctx = _context(R, w, args.mode, stream, w.vp_true)
+        tt = torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda")
+        step = lambda: ctx.forward_device(w.srcx, w.srcz, tt.data_ptr(), 0)  # noqa: E731
+        for _ in range(max(args.warmup, 3)):
+            step()
+        ms = _events_ms(step, stream, args.steps)
+        passes = ctx.shot_info(0)[0]
+        import oracle as O
+        O.build(ref=False)
+        p = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+        S = synth.slowness(w.vp_true)
+        t0 = time.perf_counter()
+        reps = 5
+        for _ in range(reps):
+            O.eikonal(p, S, w.srcx[0], w.srcz[0])
+        cpu_ms = 1e3 * (time.perf_counter() - t0) / reps
+        out.update({"metric": "forward solve latency", "value": ms, "unit": "ms", "higher_is_better": False,
+                    "passes": passes, "point_updates_per_s": passes * 4 * w.nx * w.ny / (ms / 1e3),
+                    "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": 1, "kind": "port",
+                                     "sample": "the same solve, one core (the reference solves a shot on one rank)"}})
+    elif args.workload == "uneven":
+        grids = [synth.uneven_grid(i) for i in range(3)]
+        ctxs, bufs, streams = [], [], []
+        for w in grids:
+            st = torch.cuda.Stream()
+            ctx = _context(R, w, args.mode, st, w.vp_true)
+            Tobs = np.empty((w.nshots, w.ntr), np.float32)
+            ctx.set_velocity(w.vp_true * np.float32(1.03))
+            _, Tobs, _ = ctx.forward(w.srcx, w.srcz, want_tt=False)
+            ctx.set_velocity(w.vp_true)
+            bufs.append((torch.from_numpy(np.ascontiguousarray(Tobs)).cuda(),
+                         torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda"),
+                         torch.empty(1, dtype=torch.float64, device="cuda")))
+            ctxs.append(ctx)
+            streams.append(st)
+
+        def launch(i):
+            w, (to, g, l2) = grids[i], bufs[i]
+            ctxs[i].grad_obj_device(w.srcx, w.srcz, to.data_ptr(), g.data_ptr(), l2.data_ptr())
+
+        def concurrent():
+            for i in range(3):
+                launch(i)
+
+        for _ in range(max(args.warmup, 3)):
+            concurrent()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            concurrent()
+        torch.cuda.synchronize()
+        conc_ms = 1e3 * (time.perf_counter() - t0) / args.steps
+        per_grid = []
+        for i, w in enumerate(grids):
+            ms_i = _events_ms(lambda: launch(i), streams[i], max(1, args.steps // 2))
+            pf = sum(ctxs[i].shot_info(s)[0] for s in range(w.nshots))
+            pa = sum(ctxs[i].shot_info(s)[1] for s in range(w.nshots))
+            per_grid.append({"grid": [w.nx, w.ny], "shots": w.nshots, "ms": ms_i,
+                             "point_updates": 4 * (pf * w.nx * w.ny + pa * (w.nx - 2) * (w.ny - 2))})
+        nsh = sum(w.nshots for w in grids)
+        pu = sum(g["point_updates"] for g in per_grid)
+        out.update({"metric": "fwd+adjoint shots/s", "value": nsh / (conc_ms / 1e3), "unit": "shots/s",
+                    "higher_is_better": True, "ms_per_step": conc_ms, "shots": nsh,
+                    "point_updates_per_s": pu / (conc_ms / 1e3), "per_grid": per_grid,
+                    "how": "three grids' batches on three streams, host-timed around a full sync"})
+    elif args.workload == "stress":
+        w = synth.stress_8192x2048(nshots=args.shots if args.shots != 100 else 1024)
+        ctx = _context(R, w, args.mode, stream, w.vp_true)
+        ctx.set_memory_cap(120 << 30)
+        to = torch.empty((w.nshots, w.ntr), dtype=torch.float32, device="cuda")
+        t0 = time.perf_counter()
+        ctx.forward_device(w.srcx, w.srcz, 0, to.data_ptr())
+        torch.cuda.synchronize()
+        fwd_s = time.perf_counter() - t0
+        vstart = np.where(w.vp_true == 4500.0, np.float32(3500.0), w.vp_true).astype(np.float32)
+        ctx.set_velocity(vstart)
+        g = torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda")
+        l2 = torch.empty(1, dtype=torch.float64, device="cuda")
+        step = lambda: ctx.grad_obj_device(w.srcx, w.srcz, to.data_ptr(), g.data_ptr(), l2.data_ptr())  # noqa
+        ms = _events_ms(step, stream, max(1, args.steps))
+        pf = sum(ctx.shot_info(s)[0] for s in range(w.nshots))
+        pa = sum(ctx.shot_info(s)[1] for s in range(w.nshots))
+        pu = 4 * (pf * w.nx * w.ny + pa * (w.nx - 2) * (w.ny - 2))
+        out.update({"metric": "fwd+adjoint shots/s", "value": w.nshots / (ms / 1e3), "unit": "shots/s",
+                    "higher_is_better": True, "ms_per_step": ms, "shots": w.nshots,
+                    "forward_only_s": fwd_s, "passes_fwd_adj": [pf, pa],
+                    "point_updates_per_s": pu / (ms / 1e3), "memory_cap_bytes": 120 << 30,
+                    "peak_allocated_note": "field slots sized to the cap, chunks of a multiple of the SM count"})
+    t_wall1 = time.time()
+    time.sleep(0.15)
+    clocks.stop()
+    out["clocks"] = clocks.summary(t_wall0, t_wall1)
+    print(json.dumps(out), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     ap.add_argument("--gpus", type=int, default=1)
@@ -330,6 +474,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mode", choices=["fast", "reference"], default="fast")
     ap.add_argument("--shots", type=int, default=100, help="shots per step (the workload has 100)")
+    ap.add_argument("--workload", choices=["grad_1700x350", "fwd_500x174", "uneven", "stress"],
+                    default="grad_1700x350", help="the benchmark workload (default) or another named one")
     ap.add_argument("--profile-only", action="store_true",
                     help="only the device-timed loop (for profiler runs); no baselines, no JSON contract line")
     args = ap.parse_args()
@@ -338,6 +484,8 @@ def main():
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference_arm(args, rank)
+    elif args.workload != "grad_1700x350":
+        run_workload(args, local_rank)
     else:
         run_gpu_arm(args, rank, world, local_rank)
 

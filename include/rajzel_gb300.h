@@ -29,6 +29,8 @@
 #ifndef RAJZEL_GB300_H
 #define RAJZEL_GB300_H
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -90,6 +92,14 @@ int rz_set_velocity(rz_context *ctx, const float *vp, int flags);
    indices (recpos[1..2][1..ntr] of receiver.c).  Host pointers. */
 int rz_set_receivers(rz_context *ctx, int ntr, const int *recx, const int *recz);
 
+/* Device memory the per-shot field slots (traveltimes, lambda, pass
+   snapshot, skewed copies: about 28 bytes per padded cell) may occupy.
+   A batch whose slots exceed it runs in chunks of as many shots as fit, in
+   shot order, stacking each chunk onto the previous ones; results do not
+   depend on the chunk size.  0 (the default) = 90% of free device memory.
+   Not in the reference, whose MPI ranks each hold one shot's fields. */
+int rz_set_memory_cap(rz_context *ctx, size_t bytes);
+
 /* forward(): traveltimes for nshots sources (forward.c:19-24 over
    eikonal(), eikonal.c:10-76).
      srcx, srcz : [nshots] metres (host pointers)
@@ -114,7 +124,9 @@ int rz_grad_obj(rz_context *ctx, int nshots, const float *srcx, const float *src
 int rz_shot_info(rz_context *ctx, int shot, int *fwd_passes, int *adj_passes, int *status);
 
 /* Fields of shot `shot` from the last rz_grad_obj: TT, lambda [ny][nx],
-   Tres [ntr] (scaled residuals as passed to eikonal_adj). */
+   Tres [ntr] (scaled residuals as passed to eikonal_adj).  TT and lambda
+   are kept only for the shots of the last chunk (all shots when the batch
+   fit the memory cap); Tres is kept for every shot. */
 int rz_shot_fields(rz_context *ctx, int shot, float *TT, float *lam, float *Tres, int flags);
 
 /* Accounting: kernels this context has launched so far, and the summed

@@ -76,7 +76,8 @@ def load_library(path: str = LIB_PATH):
     lib.rz_shot_timeline.argtypes = [vp, C.c_int, vp]
     lib.rz_kernel_stats.argtypes = [vp, vp, vp, vp]
     lib.rz_eikonal_adj.argtypes = [vp, vp, vp, vp, vp, C.c_int]
-    for name in ("rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
+    lib.rz_set_memory_cap.argtypes = [vp, C.c_size_t]
+    for name in ("rz_set_memory_cap", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
                  "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
                  "rz_eikonal_adj", "rz_shot_timeline", "rz_kernel_stats"):
         getattr(lib, name).restype = C.c_int
@@ -162,6 +163,10 @@ class Context:
         self._check(self.lib.rz_set_receivers(self.h, len(recx), _ptr(recx), _ptr(recz)), "rz_set_receivers")
         self.ntr = len(recx)
 
+    def set_memory_cap(self, nbytes: int):
+        """Bytes of device memory the per-shot field slots may use (0 = automatic)."""
+        self._check(self.lib.rz_set_memory_cap(self.h, int(nbytes)), "rz_set_memory_cap")
+
     # -- the hot path -------------------------------------------------------
     def eikonal(self, srcx, srcz):
         TT = np.empty((self.ny, self.nx), np.float32)
@@ -198,6 +203,13 @@ class Context:
         self._check(self.lib.rz_grad_obj(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(Tobs), _ptr(grad), C.byref(L2), 0),
                     "rz_grad_obj")
         return grad, L2.value
+
+    def forward_device(self, srcx, srcz, tt_ptr: int = 0, tmod_ptr: int = 0):
+        """Asynchronous forward on device buffers (RZ_DEVICE_PTRS): TT
+        [n][ny][nx] and Tmod [n][ntr] float32, either may be 0."""
+        srcx, srcz = _f32(srcx), _f32(srcz)
+        self._check(self.lib.rz_forward(self.h, len(srcx), _ptr(srcx), _ptr(srcz), C.c_void_p(tt_ptr or None),
+                                        C.c_void_p(tmod_ptr or None), None, RZ_DEVICE_PTRS), "rz_forward(device)")
 
     def grad_obj_device(self, srcx, srcz, tobs_ptr: int, grad_ptr: int, l2_ptr: int):
         """Asynchronous variant on device buffers (RZ_DEVICE_PTRS): Tobs

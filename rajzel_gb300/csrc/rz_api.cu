@@ -55,18 +55,23 @@ struct rz_context {
     uint8_t *dSkip = nullptr;
     uint32_t *dMA = nullptr, *dMB = nullptr;
 
-    // per-shot buffers
-    int cap = 0;
+    // per-shot field slots (a batch larger than cap_f runs in chunks of cap_f shots)
+    int cap_f = 0;
+    size_t memcap = 0;  // bytes the field slots may occupy; 0 = 90% of free device memory
     float *dT = nullptr, *dTold = nullptr, *dL = nullptr, *dTA = nullptr, *dTB = nullptr, *dEU = nullptr,
           *dED = nullptr;
+    CUtensorMap mTld{}, mTrow{}, mLrow{};
+    // per-shot scalars and receiver arrays, sized for the whole batch
+    int cap_s = 0;
     float *dTobs = nullptr, *dTmod = nullptr, *dTres = nullptr;
     double *dl2 = nullptr, *dL2 = nullptr;
     int *dPf = nullptr, *dPa = nullptr, *dStat = nullptr, *dSrcH = nullptr, *dSrcK = nullptr;
     unsigned long long *dTl = nullptr;
     float *dGrad = nullptr;
-    CUtensorMap mTld{}, mTrow{}, mLrow{};
+    double *dGrad64 = nullptr;
 
-    int last_n = 0;
+    int last_n = 0;           // shots of the last batch
+    int last_first = 0;       // first shot whose fields are still in the slots
     bool last_adj = false;
 
     // accounting: kernels launched, and CUDA-event timing of every shot-kernel launch
@@ -134,7 +139,7 @@ static EncodeTiledFn encode_fn() {
 static int make_map(rz_context *c, CUtensorMap *m, float *base, int box_rows) {
     EncodeTiledFn enc = encode_fn();
     if (!enc) return fail(c, RZ_ECUDA, "cuTensorMapEncodeTiled entry point unavailable");
-    cuuint64_t dims[3] = {(cuuint64_t)c->g.nx, (cuuint64_t)c->g.ny, (cuuint64_t)c->cap};
+    cuuint64_t dims[3] = {(cuuint64_t)c->g.nx, (cuuint64_t)c->g.ny, (cuuint64_t)c->cap_f};
     cuuint64_t strides[2] = {(cuuint64_t)c->nxp * 4, (cuuint64_t)c->nxp * c->g.ny * 4};
     cuuint32_t box[3] = {(cuuint32_t)kBlk, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
@@ -145,18 +150,34 @@ static int make_map(rz_context *c, CUtensorMap *m, float *base, int box_rows) {
     return RZ_OK;
 }
 
-static void free_batch(rz_context *c) {
+static void free_fields(rz_context *c) {
     dfree(c->dT), dfree(c->dTold), dfree(c->dL), dfree(c->dTA), dfree(c->dTB), dfree(c->dEU), dfree(c->dED);
-    dfree(c->dTobs), dfree(c->dTmod), dfree(c->dTres), dfree(c->dl2), dfree(c->dPf), dfree(c->dPa);
-    dfree(c->dStat), dfree(c->dSrcH), dfree(c->dSrcK), dfree(c->dTl);
-    c->cap = 0;
+    c->cap_f = 0;
 }
 
-static int ensure_batch(rz_context *c, int n) {
-    if (n <= c->cap) return RZ_OK;
-    free_batch(c);
+static void free_shots(rz_context *c) {
+    dfree(c->dTobs), dfree(c->dTmod), dfree(c->dTres), dfree(c->dl2), dfree(c->dPf), dfree(c->dPa);
+    dfree(c->dStat), dfree(c->dSrcH), dfree(c->dSrcK), dfree(c->dTl);
+    c->cap_s = 0;
+}
+
+static void free_batch(rz_context *c) {
+    free_fields(c);
+    free_shots(c);
+}
+
+// device bytes of one field slot: T, pass snapshot, lambda, two skewed T copies, border rows
+static size_t slot_bytes(const rz_context *c) {
     const size_t fs = (size_t)c->g.ny * c->nxp, ss = (size_t)c->nstrips * c->qn * 32,
-                 es = (size_t)c->nstrips * edge_row(c->nxp), nt = (size_t)(c->ntr > 0 ? c->ntr : 1);
+                 es = (size_t)c->nstrips * edge_row(c->nxp);
+    return 4 * (3 * fs + 2 * ss + 2 * es);
+}
+
+static int ensure_fields(rz_context *c, int n) {
+    if (n <= c->cap_f) return RZ_OK;
+    free_fields(c);
+    const size_t fs = (size_t)c->g.ny * c->nxp, ss = (size_t)c->nstrips * c->qn * 32,
+                 es = (size_t)c->nstrips * edge_row(c->nxp);
     CK(dalloc(&c->dT, fs * n));
     CK(dalloc(&c->dTold, fs * n));
     CK(dalloc(&c->dL, fs * n));
@@ -166,6 +187,18 @@ static int ensure_batch(rz_context *c, int n) {
     CK(dalloc(&c->dED, es * n));
     CK(cudaMemsetAsync(c->dEU, 0, es * n * 4, c->st));
     CK(cudaMemsetAsync(c->dED, 0, es * n * 4, c->st));
+    c->cap_f = n;
+    int r;
+    if ((r = make_map(c, &c->mTld, c->dT, kBoxRows))) return r;
+    if ((r = make_map(c, &c->mTrow, c->dT, 1))) return r;
+    if ((r = make_map(c, &c->mLrow, c->dL, 1))) return r;
+    return RZ_OK;
+}
+
+static int ensure_shots(rz_context *c, int n) {
+    if (n <= c->cap_s) return RZ_OK;
+    free_shots(c);
+    const size_t nt = (size_t)(c->ntr > 0 ? c->ntr : 1);
     CK(dalloc(&c->dTobs, nt * n));
     CK(dalloc(&c->dTmod, nt * n));
     CK(dalloc(&c->dTres, nt * n));
@@ -176,11 +209,34 @@ static int ensure_batch(rz_context *c, int n) {
     CK(dalloc(&c->dSrcH, (size_t)n));
     CK(dalloc(&c->dSrcK, (size_t)n));
     CK(dalloc(&c->dTl, (size_t)n * kTimelineSlots));
-    c->cap = n;
+    c->cap_s = n;
+    return RZ_OK;
+}
+
+// Shots per chunk for a batch of n: all of them when their field slots fit
+// the memory cap, else as many as fit (at least one).  Allocates the slots.
+static int plan_chunks(rz_context *c, int n, int *chunk) {
+    const size_t per = slot_bytes(c);
+    size_t limit = c->memcap;
+    if (limit == 0) {
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        limit = (size_t)(0.9 * (double)(fr + per * (size_t)c->cap_f));
+    }
+    size_t fit = limit / per;
+    if (fit < 1) fit = 1;
+    int m = (size_t)n < fit ? n : (int)fit;
+    if (m < n) {
+        // whole waves: a chunk of a multiple of the SM count leaves no SM idle
+        int sms = 0;
+        CK(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device));
+        if (sms > 0 && m > sms) m -= m % sms;
+    }
+    // keep existing slots when they already hold a whole chunk
+    if (c->cap_f > m && (size_t)c->cap_f <= fit) m = n < c->cap_f ? n : c->cap_f;
     int r;
-    if ((r = make_map(c, &c->mTld, c->dT, kBoxRows))) return r;
-    if ((r = make_map(c, &c->mTrow, c->dT, 1))) return r;
-    if ((r = make_map(c, &c->mLrow, c->dL, 1))) return r;
+    if ((r = ensure_fields(c, m))) return r;
+    *chunk = m;
     return RZ_OK;
 }
 
@@ -215,7 +271,8 @@ static int ensure_cube(rz_context *c) {
 
 static bool have_dev(int flags) { return (flags & RZ_DEVICE_PTRS) != 0; }
 
-static void fill_params(rz_context *c, ShotParams &P, int n) {
+// parameters for shots first..first+n-1 of the batch, their fields in slots 0..n-1
+static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     memset(&P, 0, sizeof P);
     P.nx = c->g.nx;
     P.ny = c->g.ny;
@@ -245,8 +302,8 @@ static void fill_params(rz_context *c, ShotParams &P, int n) {
     P.fstride = (size_t)c->g.ny * c->nxp;
     P.sstride = (size_t)c->nstrips * c->qn * 32;
     P.estride = (size_t)c->nstrips * edge_row(c->nxp);
-    P.src_h = c->dSrcH;
-    P.src_k = c->dSrcK;
+    P.src_h = c->dSrcH + first;
+    P.src_k = c->dSrcK + first;
     P.ntr = c->ntr;
     P.rec_h = c->dRecH;
     P.rec_k = c->dRecK;
@@ -254,14 +311,14 @@ static void fill_params(rz_context *c, ShotParams &P, int n) {
     P.rcell_h = c->dRcH;
     P.rcell_k = c->dRcK;
     P.rcell_rec = c->dRcRec;
-    P.Tobs = c->dTobs;
-    P.Tmod = c->dTmod;
-    P.Tres = c->dTres;
-    P.l2 = c->dl2;
-    P.passes_fwd = c->dPf;
-    P.passes_adj = c->dPa;
-    P.status = c->dStat;
-    P.timeline = c->dTl;
+    P.Tobs = c->dTobs + (size_t)first * c->ntr;
+    P.Tmod = c->dTmod + (size_t)first * c->ntr;
+    P.Tres = c->dTres + (size_t)first * c->ntr;
+    P.l2 = c->dl2 + first;
+    P.passes_fwd = c->dPf + first;
+    P.passes_adj = c->dPa + first;
+    P.status = c->dStat + first;
+    P.timeline = c->dTl + (size_t)first * kTimelineSlots;
 }
 
 static int status_to_code(int bits) {
@@ -307,18 +364,14 @@ static int copy_out_fields(rz_context *c, const float *src, float *dst, int n, i
     return RZ_OK;
 }
 
-static int run_batch(rz_context *c, int n, bool adjoint, bool residual, bool start_adj) {
+static int run_batch(rz_context *c, int first, int n, bool adjoint, bool residual, bool start_adj) {
     int r;
     if ((r = ensure_div(c))) return r;
     ShotParams P;
-    fill_params(c, P, n);
+    fill_params(c, P, first, n);
     P.do_residual = residual ? 1 : 0;
     P.do_adjoint = adjoint ? 1 : 0;
     P.start_adjoint = start_adj ? 1 : 0;
-    CK(cudaMemsetAsync(c->dStat, 0, n * sizeof(int), c->st));
-    CK(cudaMemsetAsync(c->dTl, 0, (size_t)n * kTimelineSlots * sizeof(unsigned long long), c->st));
-    CK(cudaMemsetAsync(c->dPf, 0, n * sizeof(int), c->st));
-    CK(cudaMemsetAsync(c->dPa, 0, n * sizeof(int), c->st));
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -327,8 +380,18 @@ static int run_batch(rz_context *c, int n, bool adjoint, bool residual, bool sta
     CK(cudaEventRecord(e1, c->st));
     c->shot_events.emplace_back(e0, e1);
     c->launches += 1;
-    c->last_n = n;
+    c->last_first = first;
     c->last_adj = adjoint;
+    return RZ_OK;
+}
+
+// clear the per-shot counters of a whole batch before its chunks run
+static int reset_shots(rz_context *c, int n) {
+    CK(cudaMemsetAsync(c->dStat, 0, n * sizeof(int), c->st));
+    CK(cudaMemsetAsync(c->dTl, 0, (size_t)n * kTimelineSlots * sizeof(unsigned long long), c->st));
+    CK(cudaMemsetAsync(c->dPf, 0, n * sizeof(int), c->st));
+    CK(cudaMemsetAsync(c->dPa, 0, n * sizeof(int), c->st));
+    c->last_n = n;
     return RZ_OK;
 }
 
@@ -542,8 +605,19 @@ int rz_set_receivers(rz_context *c, int ntr, const int *recx, const int *recz) {
     CK(dalloc(&c->dMB, lines));
     CK(launch_skip_masks(c->dSkip, nx, ny, c->nstrips, c->nxb, c->dMA, c->dMB, c->st));
     CK(cudaStreamSynchronize(c->st));
-    free_batch(c);  // receiver-sized buffers follow ntr
+    free_shots(c);  // receiver-sized buffers follow ntr
     c->rec_set = true;
+    return RZ_OK;
+}
+
+int rz_set_memory_cap(rz_context *c, size_t bytes) {
+    if (!c) return RZ_EINVAL;
+    c->memcap = bytes;
+    if (bytes && c->cap_f && slot_bytes(c) * (size_t)c->cap_f > bytes) {
+        cudaSetDevice(c->device);
+        cudaStreamSynchronize(c->st);
+        free_fields(c);
+    }
     return RZ_OK;
 }
 
@@ -556,10 +630,17 @@ int rz_forward(rz_context *c, int nshots, const float *srcx, const float *srcz, 
     if (!c->rec_set) {
         if ((r = rz_set_receivers(c, 0, nullptr, nullptr))) return r;
     }
-    if ((r = ensure_batch(c, nshots))) return r;
+    int chunk = 0;
+    if ((r = ensure_shots(c, nshots))) return r;
+    if ((r = plan_chunks(c, nshots, &chunk))) return r;
     if ((r = set_sources(c, nshots, srcx, srcz))) return r;
-    if ((r = run_batch(c, nshots, false, false, false))) return r;
-    if (TT && (r = copy_out_fields(c, c->dT, TT, nshots, flags))) return r;
+    if ((r = reset_shots(c, nshots))) return r;
+    const size_t fpts = (size_t)c->g.nx * c->g.ny;
+    for (int first = 0; first < nshots; first += chunk) {
+        const int m = nshots - first < chunk ? nshots - first : chunk;
+        if ((r = run_batch(c, first, m, false, false, false))) return r;
+        if (TT && (r = copy_out_fields(c, c->dT, TT + (size_t)first * fpts, m, flags))) return r;
+    }
     if (Tmod && c->ntr > 0)
         CK(cudaMemcpyAsync(Tmod, c->dTmod, (size_t)nshots * c->ntr * 4,
                            have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
@@ -574,23 +655,33 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
     if ((r = ready(c, true))) return r;
     if (nshots < 1 || !Tobs || !grad) return fail(c, RZ_EINVAL, "bad arguments");
     cudaSetDevice(c->device);
-    if ((r = ensure_batch(c, nshots))) return r;
+    int chunk = 0;
+    if ((r = ensure_shots(c, nshots))) return r;
+    if ((r = plan_chunks(c, nshots, &chunk))) return r;
     if ((r = set_sources(c, nshots, srcx, srcz))) return r;
     if (c->mode == RZ_MODE_REFERENCE && (r = ensure_cube(c))) return r;
     const size_t nt = (size_t)nshots * c->ntr;
     if (nt) CK(cudaMemcpyAsync(c->dTobs, Tobs, nt * 4, have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
-    if ((r = run_batch(c, nshots, true, true, false))) return r;
+    if ((r = reset_shots(c, nshots))) return r;
     float *gdst = grad;
     if (!have_dev(flags)) {
         if (!c->dGrad) CK(dalloc(&c->dGrad, (size_t)c->g.nx * c->g.ny));
         gdst = c->dGrad;
     }
-    CK(launch_stack(c->dL, (size_t)c->g.ny * c->nxp, nshots, c->dCube, c->dS, c->g.nx, c->g.ny, c->nxp, c->mode, gdst,
-                    c->g.nx, nullptr, c->st));
+    if (c->mode == RZ_MODE_FAST && !c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
+    // chunks run in shot order; each stack continues the previous chunk's sums,
+    // so the result does not depend on the chunk size
+    for (int first = 0; first < nshots; first += chunk) {
+        const int m = nshots - first < chunk ? nshots - first : chunk;
+        if ((r = run_batch(c, first, m, true, true, false))) return r;
+        CK(launch_stack(c->dL, (size_t)c->g.ny * c->nxp, m, c->dCube, c->dS, c->g.nx, c->g.ny, c->nxp, c->mode, gdst,
+                        c->g.nx, c->mode == RZ_MODE_FAST ? c->dGrad64 : nullptr, first > 0, c->st));
+        c->launches += 1;
+    }
     CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, c->st));
     if (!c->dL2) CK(dalloc(&c->dL2, 1));
     CK(launch_sum_l2(c->dl2, nshots, c->dL2, c->st));
-    c->launches += 3;
+    c->launches += 2;
     if (have_dev(flags)) {
         if (L2) CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
         return RZ_OK;
@@ -620,9 +711,13 @@ int rz_shot_fields(rz_context *c, int shot, float *TT, float *lam, float *Tres, 
     if (shot < 0 || shot >= c->last_n) return fail(c, RZ_EINVAL, "shot %d not in the last batch", shot);
     cudaSetDevice(c->device);
     const size_t fs = (size_t)c->g.ny * c->nxp;
+    const int slot = shot - c->last_first;
+    if ((TT || lam) && slot < 0)
+        return fail(c, RZ_EINVAL, "fields of shot %d were not kept: the batch ran in chunks of %d shots", shot,
+                    c->cap_f);
     int r;
-    if (TT && (r = copy_out_fields(c, c->dT + shot * fs, TT, 1, flags))) return r;
-    if (lam && (r = copy_out_fields(c, c->dL + shot * fs, lam, 1, flags))) return r;
+    if (TT && (r = copy_out_fields(c, c->dT + slot * fs, TT, 1, flags))) return r;
+    if (lam && (r = copy_out_fields(c, c->dL + slot * fs, lam, 1, flags))) return r;
     if (Tres && c->ntr)
         CK(cudaMemcpyAsync(Tres, c->dTres + (size_t)shot * c->ntr, c->ntr * 4,
                            have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
@@ -670,11 +765,12 @@ int rz_eikonal_adj(rz_context *c, const float *TT, const float *Tres, float *lam
     if ((r = ready(c, true))) return r;
     if (!TT || !lam || (c->ntr > 0 && !Tres)) return fail(c, RZ_EINVAL, "bad arguments");
     cudaSetDevice(c->device);
-    if ((r = ensure_batch(c, 1))) return r;
+    if ((r = ensure_shots(c, 1)) || (r = ensure_fields(c, 1))) return r;
     const cudaMemcpyKind kin = have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
     CK(cudaMemcpy2DAsync(c->dT, (size_t)c->nxp * 4, TT, (size_t)c->g.nx * 4, (size_t)c->g.nx * 4, c->g.ny, kin, c->st));
     if (c->ntr) CK(cudaMemcpyAsync(c->dTres, Tres, c->ntr * 4, kin, c->st));
-    if ((r = run_batch(c, 1, true, false, true))) return r;
+    if ((r = reset_shots(c, 1))) return r;
+    if ((r = run_batch(c, 0, 1, true, false, true))) return r;
     if ((r = copy_out_fields(c, c->dL, lam, 1, flags))) return r;
     if (passes) CK(cudaMemcpyAsync(passes, c->dPa, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     return collect_status(c, 1);

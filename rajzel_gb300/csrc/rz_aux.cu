@@ -72,8 +72,10 @@ cudaError_t launch_skip_masks(const uint8_t *skip, int nx, int ny, int nstrips, 
 //   reference: per shot RN32(RN64(lam * cube)) with cube = pow(S,3) from the
 //              host C library, summed in float in shot order
 //   fast:      lam * S^3 summed in double (grad64), rounded into grad
+// With `accumulate` the sums continue from grad (reference) / grad64 (fast),
+// so a batch stacked chunk by chunk in shot order gives the same result.
 __global__ void stack_kernel(const float *L, size_t fstride, int nshots, const double *cube, const float *S, int nx,
-                             int ny, int nxp, int mode, float *grad, int gpitch, double *grad64) {
+                             int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, bool accumulate) {
     const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= (long)nx * ny) return;
     const int k = (int)(c / nx), h = (int)(c - (long)k * nx);
@@ -81,7 +83,7 @@ __global__ void stack_kernel(const float *L, size_t fstride, int nshots, const d
     const size_t og = (size_t)k * gpitch + h;
     const bool interior = (h > 0 && h < nx - 1 && k > 0 && k < ny - 1);
     if (mode == kModeReference) {
-        float acc = 0.f;
+        float acc = accumulate ? grad[og] : 0.f;
         if (interior) {
             const double cb = cube[(size_t)k * nx + h];
             for (int z = 0; z < nshots; ++z) {
@@ -98,16 +100,18 @@ __global__ void stack_kernel(const float *L, size_t fstride, int nshots, const d
             for (int z = 0; z < nshots; ++z) acc += (double)__ldg(L + (size_t)z * fstride + o);
             acc *= cb;
         }
+        if (accumulate && grad64) acc += grad64[og];
         if (grad64) grad64[og] = acc;
         grad[og] = (float)acc;
     }
 }
 
 cudaError_t launch_stack(const float *L, size_t fstride, int nshots, const double *cube, const float *S, int nx,
-                         int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, cudaStream_t st) {
+                         int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, bool accumulate,
+                         cudaStream_t st) {
     const long n = (long)nx * ny;
     stack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(L, fstride, nshots, cube, S, nx, ny, nxp, mode, grad,
-                                                           gpitch, grad64);
+                                                           gpitch, grad64, accumulate);
     return cudaGetLastError();
 }
 

@@ -95,8 +95,10 @@ cudaError_t launch_skip_masks(const uint8_t *skip, int nx, int ny, int nstrips, 
 // gradient stack: grad = cp_grad_frame^2( sum_s  RN32(lam_s * cube) )
 //   mode reference: per-shot float contribution RN32(RN64(lam*cube64)) added
 //   in float in shot order; mode fast: contributions added in double.
+//   accumulate: continue the sums already in grad / grad64 (chunked batches)
 cudaError_t launch_stack(const float *L, size_t fstride, int nshots, const double *cube, const float *S, int nx,
-                         int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, cudaStream_t st);
+                         int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, bool accumulate,
+                         cudaStream_t st);
 cudaError_t launch_cp_frame(float *A, double *A64, int nx, int ny, int pitch, int times, cudaStream_t st);
 cudaError_t launch_copy_rows(const float *src, int src_pitch, float *dst, int dst_pitch, int nx, int ny,
                              size_t nbatch, size_t src_bstride, size_t dst_bstride, cudaStream_t st);

@@ -156,6 +156,43 @@ def fatt_2000x500(seed=99, nshots=200, ntr=1000):
                     start.astype(np.float32), srcx, srcz, recx.astype(np.int32), recz)
 
 
+def _polygon_mask(rng, nx, ny, dh, cx, cz, r_mean, nvert=9):
+    """Cells inside a seeded random star-shaped polygon (even-odd ray casting)."""
+    ang = np.sort(rng.uniform(0, 2 * np.pi, nvert))
+    rad = r_mean * rng.uniform(0.55, 1.0, nvert)
+    px, pz = cx + rad * np.cos(ang), cz + 0.6 * rad * np.sin(ang)
+    X = (np.arange(nx) * dh)[None, :]
+    Z = (np.arange(ny) * dh)[:, None]
+    inside = np.zeros((ny, nx), bool)
+    for i in range(nvert):
+        x0, z0, x1, z1 = px[i], pz[i], px[(i + 1) % nvert], pz[(i + 1) % nvert]
+        if z0 == z1:
+            continue
+        cross = ((z0 > Z) != (z1 > Z))
+        xint = x0 + (Z - z0) * (x1 - x0) / (z1 - z0)
+        inside ^= cross & (X < xint)
+    return inside
+
+
+def stress_8192x2048(seed=4096, nshots=1024, ntr=4096):
+    """High-contrast stress case: 1500 m/s water layer over an 1800->5000 m/s
+    gradient with an embedded 4500 m/s random-polygon block; dh = 5 m."""
+    rng = np.random.default_rng(seed)
+    nx, ny, dh = 8192, 2048, 5.0
+    z = np.arange(ny) * dh
+    water = 300.0
+    v = np.where(z < water, 1500.0, 1800.0 + (5000.0 - 1800.0) * (z - water) / (z[-1] - water))
+    vp = np.repeat(v[:, None], nx, axis=1).astype(np.float32)
+    mask = _polygon_mask(rng, nx, ny, dh, 0.5 * nx * dh, 0.55 * ny * dh, 0.3 * ny * dh * 1.4)
+    vp[mask] = 4500.0
+    srcx = (dh * (2.0 + (nx - 4) * (np.arange(nshots) + 0.5) / nshots)).astype(np.float32)
+    srcz = np.full(nshots, 2 * dh, np.float32)
+    recx = grid_index(dh * (1.0 + np.linspace(1, nx - 2, ntr)), dh)
+    recz = np.full(ntr, 2, np.int32)
+    return Workload("stress_8192x2048", nx, ny, dh, 30.0, 1e-6, 1e-9, vp, vp, srcx, srcz, recx.astype(np.int32),
+                    recz)
+
+
 def small_case(seed, nx, ny, dh=10.0, nshots=3, ntr=None, vmin=1500.0, vmax=4500.0):
     """Small seeded case for parity tests: smooth-ish random velocity."""
     rng = np.random.default_rng(seed)

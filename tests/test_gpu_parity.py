@@ -161,6 +161,44 @@ def test_batched_equals_single_shot(R):
         assert np.array_equal(TT[i], t1)
 
 
+def _noisy_picks(p, w, S, n, seed):
+    rng = np.random.default_rng(seed)
+    Tobs = np.empty((n, w.ntr), np.float32)
+    for i in range(n):
+        to, _ = O.eikonal(p, S * np.float32(0.97), w.srcx[i], w.srcz[i])
+        Tobs[i] = O.calc_fa(p, to, w.recx, w.recz) * (1 + 0.01 * rng.standard_normal(w.ntr)).astype(np.float32)
+    return Tobs
+
+
+@pytest.mark.parametrize("mode", ["reference", "fast"])
+def test_memory_cap_chunks_do_not_change_results(R, mode):
+    """A memory cap smaller than the batch's field slots makes the batch run
+    in chunks (here 2+2+1 shots); every result must equal the unchunked run
+    bit for bit, and in reference mode also the oracle."""
+    w = synth.small_case(77, 90, 70, nshots=5)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    Tobs = _noisy_picks(p, w, S, 5, 11)
+    ctx = make_ctx(R, w, mode=mode)
+    g_all, l_all = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    TT_all, Tm_all, pf_all = ctx.forward(w.srcx, w.srcz)
+    nxp = 32 * ((w.nx + 31) // 32)
+    nst = (w.ny + 31) // 32
+    slot = 4 * (3 * w.ny * nxp + 2 * nst * (32 * (nxp // 32) + 64) * 32 + 2 * nst * (nxp + 96))
+    ctx.set_memory_cap(2 * slot + slot // 2)
+    g_c, l_c = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    assert np.array_equal(g_c, g_all) and l_c == l_all
+    TT_c, Tm_c, pf_c = ctx.forward(w.srcx, w.srcz)
+    assert np.array_equal(TT_c, TT_all) and np.array_equal(Tm_c, Tm_all) and np.array_equal(pf_c, pf_all)
+    # fields are kept for the last chunk only
+    with pytest.raises(R.RajzelError):
+        ctx.shot_fields(0)
+    ctx.shot_fields(4)
+    if mode == "reference":
+        go, L2o, _, _, _ = O.grad_obj(p, S, w.srcx, w.srcz, w.recx, w.recz, Tobs)
+        assert np.array_equal(g_c, go) and l_c == L2o
+
+
 # ---------------------------------------------------------------------------
 # fast mode against the FP64 oracle
 # ---------------------------------------------------------------------------
