@@ -51,6 +51,10 @@ extern "C" {
 #define RZ_MODE_REFERENCE 0  /* bit-identical to the reference's float/double arithmetic */
 #define RZ_MODE_FAST 1       /* FP32 sweeps, FP64 misfit and gradient stack */
 
+/* gradient kinds (rz_set_gradient) */
+#define RZ_GRADIENT_REFERENCE 0 /* Leung-Qian adjoint, lambda*S^3 + frame copy (ass_grad.c) */
+#define RZ_GRADIENT_EXACT 1     /* exact discrete adjoint: dJ/dVp of the float misfit */
+
 /* flags */
 #define RZ_DEVICE_PTRS 1
 
@@ -79,6 +83,18 @@ const char *rz_last_error(const rz_context *ctx);
 int rz_set_stream(rz_context *ctx, void *cuda_stream);
 /* RZ_MODE_REFERENCE (default) or RZ_MODE_FAST. */
 int rz_set_mode(rz_context *ctx, int mode);
+
+/* Which gradient rz_grad_obj returns (not in the reference, which has only
+   the first):
+     RZ_GRADIENT_REFERENCE  the reference's: Leung-Qian adjoint state
+                            (sweep_adj.c), lambda*S^3 stacked and
+                            frame-copied (ass_grad.c, cp_grad_frame.c);
+     RZ_GRADIENT_EXACT      the exact derivative dJ/dVp of the discrete
+                            misfit J = 0.5 sum (Tmod - Tobs)^2 over unmuted
+                            picks: the adjoint of the Godunov update
+                            linearised at the converged traveltimes, solved
+                            by the same wavefront sweeps; no frame copy. */
+int rz_set_gradient(rz_context *ctx, int kind);
 
 /* Grid and solver constants (replaces the globals NX..EPS_ADJ). */
 int rz_set_grid(rz_context *ctx, const rz_grid *grid);
@@ -118,6 +134,16 @@ int rz_forward(rz_context *ctx, int nshots, const float *srcx, const float *srcz
    A muted pick contributes a zero residual. */
 int rz_grad_obj(rz_context *ctx, int nshots, const float *srcx, const float *srcz, const float *Tobs, float *grad,
                 double *L2, int flags);
+
+/* Backward of the forward map Vp -> Tmod (vector-Jacobian product, not in
+   the reference): grad[ny][nx] = sum over shots of (dTmod/dVp)^T dTmod_s,
+   with dTmod [nshots][ntr] the cotangents of the picks.  The forward fields
+   are recomputed inside the call from the model and the sources (chunk by
+   chunk under the memory cap); no earlier rz_forward is needed.
+   rz_grad_obj with RZ_GRADIENT_EXACT equals rz_backward with
+   dTmod = Tmod - Tobs (0 for muted picks). */
+int rz_backward(rz_context *ctx, int nshots, const float *srcx, const float *srcz, const float *dTmod, float *grad,
+                int flags);
 
 /* Per-shot results of the last rz_forward/rz_grad_obj (host pointers, any
    may be NULL): outer passes of forward/adjoint, device status bits. */

@@ -82,6 +82,10 @@ def _load_port():
         lib.rzo_grad_obj_f64.argtypes = [G, _f64p, C.c_int, _f64p, _f64p, C.c_int, _i32p, _i32p, _f64p, _f64p,
                                          C.POINTER(C.c_double)]
         lib.rzo_shot_partition.argtypes = [C.c_int, C.c_int, C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int)]
+        lib.rzo_grad_exact_f64.argtypes = [G, _f64p, C.c_int, _f64p, _f64p, C.c_int, _i32p, _i32p, _f64p, _f64p,
+                                           C.POINTER(C.c_double)]
+        lib.rzo_misfit_f64.argtypes = [G, _f64p, C.c_int, _f64p, _f64p, C.c_int, _i32p, _i32p, _f64p,
+                                       C.POINTER(C.c_double)]
         lib.rzo_shot_partition.restype = None
         _port = lib
     return _port
@@ -230,6 +234,28 @@ def grad_obj_f64(p: Params, S, srcx, srcz, recx, recz, Tobs):
     _check(lib.rzo_grad_obj_f64(C.byref(p.grid()), _f64(S).reshape(-1), ns, _f64(srcx), _f64(srcz), ntr, recx,
                                 recz, _f64(Tobs).reshape(-1), grad, C.byref(L2)), "grad_obj_f64")
     return grad.reshape(p.ny, p.nx), L2.value
+
+
+def grad_exact_f64(p: Params, S, srcx, srcz, recx, recz, Tobs):
+    """Exact discrete adjoint gradient dJ/dVp (FP64), J = 0.5 sum (Tmod-Tobs)^2."""
+    lib = _load_port()
+    recx, recz = _i32(recx), _i32(recz)
+    ns, ntr = len(srcx), len(recx)
+    grad = np.empty(p.nx * p.ny, np.float64)
+    L2 = C.c_double(0)
+    _check(lib.rzo_grad_exact_f64(C.byref(p.grid()), _f64(S).reshape(-1), ns, _f64(srcx), _f64(srcz), ntr, recx,
+                                  recz, _f64(Tobs).reshape(-1), grad, C.byref(L2)), "grad_exact_f64")
+    return grad.reshape(p.ny, p.nx), L2.value
+
+
+def misfit_f64(p: Params, S, srcx, srcz, recx, recz, Tobs):
+    """J = 0.5 sum (Tmod-Tobs)^2 over unmuted picks, FP64 forward."""
+    lib = _load_port()
+    recx, recz = _i32(recx), _i32(recz)
+    L2 = C.c_double(0)
+    _check(lib.rzo_misfit_f64(C.byref(p.grid()), _f64(S).reshape(-1), len(srcx), _f64(srcx), _f64(srcz), len(recx),
+                              recx, recz, _f64(Tobs).reshape(-1), C.byref(L2)), "misfit_f64")
+    return L2.value
 
 
 def ass_grad(p: Params, grad, S, lam):

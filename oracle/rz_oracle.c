@@ -503,6 +503,116 @@ int rzo_forward(const rzo_grid *g, const float *S, int nshots, const float *srcx
     return RZO_OK;
 }
 
+/* ------------------------------------------------------------------------ */
+/* exact discrete adjoint (FP64; not in the reference)                       */
+/* ------------------------------------------------------------------------ */
+/* The converged forward field satisfies T_c = G(a_c, b_c, S_c) at every cell
+   but the source, with a_c / b_c the smaller x / z neighbour (sweep.c:89-97).
+   Linearising G: one-sided (|a-b| >= S*DH): dT_c = dT_argmin + DH dS_c;
+   two-sided with r = sqrt(2 S^2 DH^2 - (a-b)^2):
+   dT_c = (r-d)/(2r) dT_a + (r+d)/(2r) dT_b + S DH^2 / r dS_c,  d = a - b.
+   Every dependency points to a strictly earlier-arriving cell, so the adjoint
+   system mu = R + W^T mu is solved exactly by visiting cells in order of
+   decreasing traveltime.  dJ/dVp = -S^2 dJ/dS (S = 1/Vp). */
+typedef struct {
+    double t;
+    size_t c;
+} rzo_tc;
+
+static int cmp_desc(const void *x, const void *y) {
+    double a = ((const rzo_tc *)x)->t, b = ((const rzo_tc *)y)->t;
+    return (a < b) - (a > b);
+}
+
+static void exact_coef_f64(const rzo_grid *g, const double *T, const double *S, int h, int k, long *xn, double *wx,
+                           long *zn, double *wz, double *gs) {
+    const int nx = g->nx, ny = g->ny;
+    const double inf = 1e300;
+    double tw = h > 0 ? T[IDX(g, h - 1, k)] : inf, te = h < nx - 1 ? T[IDX(g, h + 1, k)] : inf;
+    double tn = k > 0 ? T[IDX(g, h, k - 1)] : inf, ts = k < ny - 1 ? T[IDX(g, h, k + 1)] : inf;
+    long ia = tw <= te ? (long)IDX(g, h - 1, k) : (long)IDX(g, h + 1, k);
+    long ib = tn <= ts ? (long)IDX(g, h, k - 1) : (long)IDX(g, h, k + 1);
+    double a = tw <= te ? tw : te, b = tn <= ts ? tn : ts;
+    double s = S[IDX(g, h, k)], sh = s * g->dh, d = a - b;
+    *xn = -1, *zn = -1, *wx = 0.0, *wz = 0.0;
+    if (fabs(d) >= sh) {
+        if (a <= b) *xn = ia, *wx = 1.0;
+        else *zn = ib, *wz = 1.0;
+        *gs = g->dh;
+    } else {
+        double r = sqrt(2.0 * sh * sh - d * d);
+        *xn = ia, *wx = (r - d) / (2.0 * r);
+        *zn = ib, *wz = (r + d) / (2.0 * r);
+        *gs = s * (double)g->dh * (double)g->dh / r;
+    }
+}
+
+int rzo_grad_exact_f64(const rzo_grid *g, const double *S, int nshots, const double *srcx, const double *srcz,
+                       int ntr, const int *recx, const int *recz, const double *Tobs, double *grad_vp, double *L2) {
+    if (check_grid(g)) return RZO_EINVAL;
+    const size_t n = (size_t)g->nx * g->ny;
+    double *T = (double *)malloc(n * sizeof(double));
+    double *mu = (double *)malloc(n * sizeof(double));
+    double *gS = (double *)calloc(n, sizeof(double));
+    rzo_tc *ord = (rzo_tc *)malloc(n * sizeof(rzo_tc));
+    int status = RZO_OK;
+    double l2 = 0.0;
+    for (int sh = 0; sh < nshots && status == RZO_OK; sh++) {
+        status = rzo_eikonal_f64(g, S, srcx[sh], srcz[sh], T, NULL);
+        if (status) break;
+        const size_t src = IDX(g, grid_index_f64(srcx[sh], g->dh) - 1, grid_index_f64(srcz[sh], g->dh) - 1);
+        memset(mu, 0, n * sizeof(double));
+        for (int i = 0; i < ntr; i++) {
+            const double tob = Tobs[(size_t)sh * ntr + i];
+            if (tob < 0.0) continue; /* muted pick */
+            const size_t c = IDX(g, recx[i] - 1, recz[i] - 1);
+            const double res = T[c] - tob;
+            mu[c] += res;
+            l2 += res * res;
+        }
+        for (size_t c = 0; c < n; c++) ord[c].t = T[c], ord[c].c = c;
+        qsort(ord, n, sizeof(rzo_tc), cmp_desc);
+        for (size_t i = 0; i < n; i++) {
+            const size_t c = ord[i].c;
+            if (c == src) continue;
+            long xn, zn;
+            double wx, wz, gs;
+            exact_coef_f64(g, T, S, (int)(c % g->nx), (int)(c / g->nx), &xn, &wx, &zn, &wz, &gs);
+            if (xn >= 0) mu[xn] += wx * mu[c];
+            if (zn >= 0) mu[zn] += wz * mu[c];
+            gS[c] += mu[c] * gs;
+        }
+    }
+    if (status == RZO_OK) {
+        for (size_t c = 0; c < n; c++) grad_vp[c] = -S[c] * S[c] * gS[c];
+        if (L2) *L2 = 0.5 * l2;
+    }
+    free(T); free(mu); free(gS); free(ord);
+    return status;
+}
+
+/* misfit 0.5 * sum (Tmod - Tobs)^2 over unmuted picks, FP64 forward */
+int rzo_misfit_f64(const rzo_grid *g, const double *S, int nshots, const double *srcx, const double *srcz, int ntr,
+                   const int *recx, const int *recz, const double *Tobs, double *L2) {
+    if (check_grid(g)) return RZO_EINVAL;
+    const size_t n = (size_t)g->nx * g->ny;
+    double *T = (double *)malloc(n * sizeof(double));
+    double l2 = 0.0;
+    int status = RZO_OK;
+    for (int sh = 0; sh < nshots && status == RZO_OK; sh++) {
+        status = rzo_eikonal_f64(g, S, srcx[sh], srcz[sh], T, NULL);
+        for (int i = 0; i < ntr && status == RZO_OK; i++) {
+            const double tob = Tobs[(size_t)sh * ntr + i];
+            if (tob < 0.0) continue;
+            const double res = T[IDX(g, recx[i] - 1, recz[i] - 1)] - tob;
+            l2 += res * res;
+        }
+    }
+    free(T);
+    if (status == RZO_OK && L2) *L2 = 0.5 * l2;
+    return status;
+}
+
 void rzo_shot_partition(int nshots, int np, int myid, int *s1, int *s2) {
     int a = (nshots / np) * myid, b;
     if (nshots % np > myid) {

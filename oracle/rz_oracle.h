@@ -79,6 +79,13 @@ int rzo_forward(const rzo_grid *g, const float *S, int nshots, const float *srcx
                 const int *recx, const int *recz, float *TT_all, float *Tmod_all, int *passes);
 
 /* init_MPIshot's block partition (init_MPIshot.c:19-30): 1-based [*s1,*s2). */
+/* Exact discrete adjoint gradient dJ/dVp of J = 0.5 sum (Tmod-Tobs)^2 over
+   unmuted picks (Tobs >= 0), FP64 forward; not in the reference. */
+int rzo_grad_exact_f64(const rzo_grid *g, const double *S, int nshots, const double *srcx, const double *srcz,
+                       int ntr, const int *recx, const int *recz, const double *Tobs, double *grad_vp, double *L2);
+int rzo_misfit_f64(const rzo_grid *g, const double *S, int nshots, const double *srcx, const double *srcz, int ntr,
+                   const int *recx, const int *recz, const double *Tobs, double *L2);
+
 void rzo_shot_partition(int nshots, int np, int myid, int *s1, int *s2);
 
 /* count floats in [lo,hi] where pow(s,3.0) != the once-rounded cube. */

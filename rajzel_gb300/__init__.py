@@ -30,6 +30,7 @@ LIB_PATH = os.path.join(_HERE, "librajzel_gb300.so")
 RZ_OK, RZ_EINVAL, RZ_ENOCONV, RZ_ECUDA, RZ_ENOMEM, RZ_ETIMEOUT, RZ_ESTATE, RZ_EUNSUPPORTED = range(8)
 RZ_MODE_REFERENCE, RZ_MODE_FAST = 0, 1
 RZ_DEVICE_PTRS = 1
+RZ_GRADIENT_REFERENCE, RZ_GRADIENT_EXACT = 0, 1
 
 class RajzelError(RuntimeError):
     def __init__(self, status: int, msg: str):
@@ -77,7 +78,9 @@ def load_library(path: str = LIB_PATH):
     lib.rz_kernel_stats.argtypes = [vp, vp, vp, vp]
     lib.rz_eikonal_adj.argtypes = [vp, vp, vp, vp, vp, C.c_int]
     lib.rz_set_memory_cap.argtypes = [vp, C.c_size_t]
-    for name in ("rz_set_memory_cap", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
+    lib.rz_set_gradient.argtypes = [vp, C.c_int]
+    lib.rz_backward.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
+    for name in ("rz_set_memory_cap", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
                  "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
                  "rz_eikonal_adj", "rz_shot_timeline", "rz_kernel_stats"):
         getattr(lib, name).restype = C.c_int
@@ -162,6 +165,21 @@ class Context:
         recx, recz = _i32(recx), _i32(recz)
         self._check(self.lib.rz_set_receivers(self.h, len(recx), _ptr(recx), _ptr(recz)), "rz_set_receivers")
         self.ntr = len(recx)
+
+    def set_gradient(self, kind: str):
+        """'reference' (Leung-Qian, the reference's gradient) or 'exact' (dJ/dVp of the discrete misfit)."""
+        k = {"reference": RZ_GRADIENT_REFERENCE, "exact": RZ_GRADIENT_EXACT}[kind]
+        self._check(self.lib.rz_set_gradient(self.h, k), "rz_set_gradient")
+
+    def backward(self, srcx, srcz, dTmod):
+        """sum over shots of (dTmod/dVp)^T dTmod: the vector-Jacobian product of the forward map."""
+        srcx, srcz = _f32(srcx), _f32(srcz)
+        n = len(srcx)
+        dTmod = _f32(dTmod).reshape(n, self.ntr) if self.ntr else np.zeros((n, 1), np.float32)
+        grad = np.empty((self.ny, self.nx), np.float32)
+        self._check(self.lib.rz_backward(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(dTmod), _ptr(grad), 0),
+                    "rz_backward")
+        return grad
 
     def set_memory_cap(self, nbytes: int):
         """Bytes of device memory the per-shot field slots may use (0 = automatic)."""

@@ -50,8 +50,9 @@ struct rz_context {
 
     // receivers
     bool rec_set = false;
-    int ntr = 0, nrcell = 0;
+    int ntr = 0, nrcell = 0, nxcell = 0;
     int *dRecH = nullptr, *dRecK = nullptr, *dRcH = nullptr, *dRcK = nullptr, *dRcRec = nullptr;
+    int *dXcH = nullptr, *dXcK = nullptr, *dXcOff = nullptr, *dXcRec = nullptr;  // all receiver cells
     uint8_t *dSkip = nullptr;
     uint32_t *dMA = nullptr, *dMB = nullptr;
 
@@ -60,7 +61,10 @@ struct rz_context {
     size_t memcap = 0;  // bytes the field slots may occupy; 0 = 90% of free device memory
     float *dT = nullptr, *dTold = nullptr, *dL = nullptr, *dTA = nullptr, *dTB = nullptr, *dEU = nullptr,
           *dED = nullptr;
+    float *dWZA = nullptr, *dWZB = nullptr, *dRA = nullptr, *dRB = nullptr;  // exact adjoint only
+    bool fields_exact = false;
     CUtensorMap mTld{}, mTrow{}, mLrow{};
+    int grad_kind = RZ_GRADIENT_REFERENCE;
     // per-shot scalars and receiver arrays, sized for the whole batch
     int cap_s = 0;
     float *dTobs = nullptr, *dTmod = nullptr, *dTres = nullptr;
@@ -152,6 +156,8 @@ static int make_map(rz_context *c, CUtensorMap *m, float *base, int box_rows) {
 
 static void free_fields(rz_context *c) {
     dfree(c->dT), dfree(c->dTold), dfree(c->dL), dfree(c->dTA), dfree(c->dTB), dfree(c->dEU), dfree(c->dED);
+    dfree(c->dWZA), dfree(c->dWZB), dfree(c->dRA), dfree(c->dRB);
+    c->fields_exact = false;
     c->cap_f = 0;
 }
 
@@ -167,14 +173,18 @@ static void free_batch(rz_context *c) {
 }
 
 // device bytes of one field slot: T, pass snapshot, lambda, two skewed T copies, border rows
+// (the exact adjoint adds skewed z weights and receiver terms, two copies each)
 static size_t slot_bytes(const rz_context *c) {
     const size_t fs = (size_t)c->g.ny * c->nxp, ss = (size_t)c->nstrips * c->qn * 32,
                  es = (size_t)c->nstrips * edge_row(c->nxp);
-    return 4 * (3 * fs + 2 * ss + 2 * es);
+    const size_t extra = c->grad_kind == RZ_GRADIENT_EXACT ? 4 * ss : 0;
+    return 4 * (3 * fs + 2 * ss + 2 * es + extra);
 }
 
 static int ensure_fields(rz_context *c, int n) {
-    if (n <= c->cap_f) return RZ_OK;
+    const bool exact = c->grad_kind == RZ_GRADIENT_EXACT;
+    if (n <= c->cap_f && (!exact || c->fields_exact)) return RZ_OK;
+    if (n < c->cap_f) n = c->cap_f;
     free_fields(c);
     const size_t fs = (size_t)c->g.ny * c->nxp, ss = (size_t)c->nstrips * c->qn * 32,
                  es = (size_t)c->nstrips * edge_row(c->nxp);
@@ -187,6 +197,13 @@ static int ensure_fields(rz_context *c, int n) {
     CK(dalloc(&c->dED, es * n));
     CK(cudaMemsetAsync(c->dEU, 0, es * n * 4, c->st));
     CK(cudaMemsetAsync(c->dED, 0, es * n * 4, c->st));
+    if (exact) {
+        CK(dalloc(&c->dWZA, ss * n));
+        CK(dalloc(&c->dWZB, ss * n));
+        CK(dalloc(&c->dRA, ss * n));
+        CK(dalloc(&c->dRB, ss * n));
+        c->fields_exact = true;
+    }
     c->cap_f = n;
     int r;
     if ((r = make_map(c, &c->mTld, c->dT, kBoxRows))) return r;
@@ -234,6 +251,7 @@ static int plan_chunks(rz_context *c, int n, int *chunk) {
     }
     // keep existing slots when they already hold a whole chunk
     if (c->cap_f > m && (size_t)c->cap_f <= fit) m = n < c->cap_f ? n : c->cap_f;
+    if (c->cap_f > 0 && (size_t)c->cap_f > fit) free_fields(c);  // slots of a larger kind no longer fit
     int r;
     if ((r = ensure_fields(c, m))) return r;
     *chunk = m;
@@ -311,6 +329,15 @@ static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     P.rcell_h = c->dRcH;
     P.rcell_k = c->dRcK;
     P.rcell_rec = c->dRcRec;
+    P.nxcell = c->nxcell;
+    P.xcell_h = c->dXcH;
+    P.xcell_k = c->dXcK;
+    P.xcell_off = c->dXcOff;
+    P.xcell_rec = c->dXcRec;
+    P.WZA = c->dWZA;
+    P.WZB = c->dWZB;
+    P.RA = c->dRA;
+    P.RB = c->dRB;
     P.Tobs = c->dTobs + (size_t)first * c->ntr;
     P.Tmod = c->dTmod + (size_t)first * c->ntr;
     P.Tres = c->dTres + (size_t)first * c->ntr;
@@ -364,7 +391,8 @@ static int copy_out_fields(rz_context *c, const float *src, float *dst, int n, i
     return RZ_OK;
 }
 
-static int run_batch(rz_context *c, int first, int n, bool adjoint, bool residual, bool start_adj) {
+static int run_batch(rz_context *c, int first, int n, bool adjoint, bool residual, bool start_adj, bool exact = false,
+                     bool cotangent = false) {
     int r;
     if ((r = ensure_div(c))) return r;
     ShotParams P;
@@ -372,6 +400,8 @@ static int run_batch(rz_context *c, int first, int n, bool adjoint, bool residua
     P.do_residual = residual ? 1 : 0;
     P.do_adjoint = adjoint ? 1 : 0;
     P.start_adjoint = start_adj ? 1 : 0;
+    P.exact = exact ? 1 : 0;
+    P.cotangent = cotangent ? 1 : 0;
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
@@ -403,6 +433,20 @@ static int collect_status(rz_context *c, int n) {
     for (int i = 0; i < n; ++i) worst |= st[i];
     int code = status_to_code(worst);
     if (code != RZ_OK) return fail(c, code, "device status bits 0x%x", worst);
+    return RZ_OK;
+}
+
+// gradient contribution of the shots first..first+m-1 (fields in slots 0..m-1)
+static int stack_chunk(rz_context *c, int first, int m, float *gdst) {
+    const size_t fs = (size_t)c->g.ny * c->nxp;
+    if (c->grad_kind == RZ_GRADIENT_EXACT) {
+        CK(launch_stack_exact(c->dT, c->dL, fs, m, c->dSrcH + first, c->dSrcK + first, c->dS, c->g.nx, c->g.ny,
+                              c->nxp, c->g.dh, gdst, c->dGrad64, first > 0, c->st));
+    } else {
+        CK(launch_stack(c->dL, fs, m, c->dCube, c->dS, c->g.nx, c->g.ny, c->nxp, c->mode, gdst, c->g.nx,
+                        c->mode == RZ_MODE_FAST ? c->dGrad64 : nullptr, first > 0, c->st));
+    }
+    c->launches += 1;
     return RZ_OK;
 }
 
@@ -451,7 +495,8 @@ void rz_destroy(rz_context *c) {
     for (auto &pr : c->shot_events) cudaEventDestroy(pr.first), cudaEventDestroy(pr.second);
     dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dVp), dfree(c->dCube), dfree(c->dGrad), dfree(c->dL2);
     dfree(c->dRecH), dfree(c->dRecK), dfree(c->dRcH), dfree(c->dRcK), dfree(c->dRcRec), dfree(c->dSkip);
-    dfree(c->dMA), dfree(c->dMB);
+    dfree(c->dMA), dfree(c->dMB), dfree(c->dGrad64);
+    dfree(c->dXcH), dfree(c->dXcK), dfree(c->dXcOff), dfree(c->dXcRec);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
 }
@@ -582,6 +627,16 @@ int rz_set_receivers(rz_context *c, int ntr, const int *recx, const int *recz) {
         rh.push_back((int)(kv.first % nx));
         rr.push_back(kv.second);
     }
+    // every receiver cell with its receivers in index order (exact adjoint)
+    std::map<long, std::vector<int>> cells;
+    for (int i = 0; i < ntr; ++i) cells[(long)kk[i] * nx + hh[i]].push_back(i);
+    std::vector<int> xh, xk, xoff(1, 0), xrec;
+    for (auto &kv : cells) {
+        xk.push_back((int)(kv.first / nx));
+        xh.push_back((int)(kv.first % nx));
+        for (int i : kv.second) xrec.push_back(i);
+        xoff.push_back((int)xrec.size());
+    }
     c->ntr = ntr;
     c->nrcell = (int)rr.size();
     CK(dalloc(&c->dRecH, (size_t)ntr));
@@ -599,6 +654,17 @@ int rz_set_receivers(rz_context *c, int ntr, const int *recx, const int *recz) {
         CK(cudaMemcpyAsync(c->dRcK, rk.data(), rr.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
         CK(cudaMemcpyAsync(c->dRcRec, rr.data(), rr.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
     }
+    c->nxcell = (int)xh.size();
+    CK(dalloc(&c->dXcH, xh.size()));
+    CK(dalloc(&c->dXcK, xk.size()));
+    CK(dalloc(&c->dXcOff, xoff.size()));
+    CK(dalloc(&c->dXcRec, xrec.size()));
+    if (!xh.empty()) {
+        CK(cudaMemcpyAsync(c->dXcH, xh.data(), xh.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(c->dXcK, xk.data(), xk.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
+        CK(cudaMemcpyAsync(c->dXcRec, xrec.data(), xrec.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
+    }
+    CK(cudaMemcpyAsync(c->dXcOff, xoff.data(), xoff.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(c->dSkip, skip.data(), skip.size(), cudaMemcpyHostToDevice, c->st));
     const size_t lines = (size_t)c->nstrips * c->qn;
     CK(dalloc(&c->dMA, lines));
@@ -668,26 +734,75 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
         if (!c->dGrad) CK(dalloc(&c->dGrad, (size_t)c->g.nx * c->g.ny));
         gdst = c->dGrad;
     }
-    if (c->mode == RZ_MODE_FAST && !c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
+    const bool exact = c->grad_kind == RZ_GRADIENT_EXACT;
+    if ((c->mode == RZ_MODE_FAST || exact) && !c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
     // chunks run in shot order; each stack continues the previous chunk's sums,
     // so the result does not depend on the chunk size
     for (int first = 0; first < nshots; first += chunk) {
         const int m = nshots - first < chunk ? nshots - first : chunk;
-        if ((r = run_batch(c, first, m, true, true, false))) return r;
-        CK(launch_stack(c->dL, (size_t)c->g.ny * c->nxp, m, c->dCube, c->dS, c->g.nx, c->g.ny, c->nxp, c->mode, gdst,
-                        c->g.nx, c->mode == RZ_MODE_FAST ? c->dGrad64 : nullptr, first > 0, c->st));
+        if ((r = run_batch(c, first, m, true, true, false, exact))) return r;
+        if ((r = stack_chunk(c, first, m, gdst))) return r;
+    }
+    if (!exact) {
+        CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, c->st));
         c->launches += 1;
     }
-    CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, c->st));
     if (!c->dL2) CK(dalloc(&c->dL2, 1));
     CK(launch_sum_l2(c->dl2, nshots, c->dL2, c->st));
-    c->launches += 2;
+    c->launches += 1;
     if (have_dev(flags)) {
         if (L2) CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
         return RZ_OK;
     }
     CK(cudaMemcpyAsync(grad, gdst, (size_t)c->g.nx * c->g.ny * 4, cudaMemcpyDeviceToHost, c->st));
     if (L2) CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    return collect_status(c, nshots);
+}
+
+int rz_set_gradient(rz_context *c, int kind) {
+    if (!c) return RZ_EINVAL;
+    if (kind != RZ_GRADIENT_REFERENCE && kind != RZ_GRADIENT_EXACT)
+        return fail(c, RZ_EINVAL, "unknown gradient kind %d", kind);
+    c->grad_kind = kind;
+    return RZ_OK;
+}
+
+int rz_backward(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *dTmod, float *grad,
+                int flags) {
+    int r;
+    if ((r = ready(c, true))) return r;
+    if (nshots < 1 || !grad || (c->ntr > 0 && !dTmod)) return fail(c, RZ_EINVAL, "bad arguments");
+    cudaSetDevice(c->device);
+    const int kind = c->grad_kind;
+    c->grad_kind = RZ_GRADIENT_EXACT;  // the slots need the exact-adjoint arrays
+    int chunk = 0;
+    r = ensure_shots(c, nshots);
+    if (!r) r = plan_chunks(c, nshots, &chunk);
+    if (!r) r = set_sources(c, nshots, srcx, srcz);
+    if (r) {
+        c->grad_kind = kind;
+        return r;
+    }
+    const size_t nt = (size_t)nshots * c->ntr;
+    if (nt) CK(cudaMemcpyAsync(c->dTobs, dTmod, nt * 4, have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
+    if ((r = reset_shots(c, nshots))) return r;
+    float *gdst = grad;
+    if (!have_dev(flags)) {
+        if (!c->dGrad) CK(dalloc(&c->dGrad, (size_t)c->g.nx * c->g.ny));
+        gdst = c->dGrad;
+    }
+    if (!c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
+    // the forward fields are recomputed here, chunk by chunk, from the model
+    // and the source positions: nothing of an earlier rz_forward is needed
+    for (int first = 0; first < nshots && !r; first += chunk) {
+        const int m = nshots - first < chunk ? nshots - first : chunk;
+        r = run_batch(c, first, m, true, true, false, true, true);
+        if (!r) r = stack_chunk(c, first, m, gdst);
+    }
+    c->grad_kind = kind;
+    if (r) return r;
+    if (have_dev(flags)) return RZ_OK;
+    CK(cudaMemcpyAsync(grad, gdst, (size_t)c->g.nx * c->g.ny * 4, cudaMemcpyDeviceToHost, c->st));
     return collect_status(c, nshots);
 }
 

@@ -115,6 +115,38 @@ cudaError_t launch_stack(const float *L, size_t fstride, int nshots, const doubl
     return cudaGetLastError();
 }
 
+// Exact-adjoint gradient (not in the reference): dJ/dVp of every cell,
+//   -S^2 * sum over shots of mu * dG/dS,
+// dG/dS from the shot's converged traveltimes (exact_coef), summed in double.
+__global__ void stack_exact_kernel(const float *T, const float *L, size_t fstride, int nshots, const int *src_h,
+                                   const int *src_k, const float *S, int nx, int ny, int nxp, float dh, float *grad,
+                                   double *grad64, bool accumulate) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= (long)nx * ny) return;
+    const int k = (int)(c / nx), h = (int)(c - (long)k * nx);
+    const size_t o = (size_t)k * nxp + h;
+    const float s = S[c];
+    double acc = 0.0;
+    for (int z = 0; z < nshots; ++z) {
+        const ExactCoef cf = exact_coef(T + (size_t)z * fstride, nxp, nx, ny, h, k, s, dh,
+                                        h == src_h[z] && k == src_k[z]);
+        acc += (double)__ldg(L + (size_t)z * fstride + o) * (double)cf.gs;
+    }
+    acc *= -((double)s * (double)s);
+    if (accumulate) acc += grad64[c];
+    grad64[c] = acc;
+    grad[c] = (float)acc;
+}
+
+cudaError_t launch_stack_exact(const float *T, const float *L, size_t fstride, int nshots, const int *src_h,
+                               const int *src_k, const float *S, int nx, int ny, int nxp, float dh, float *grad,
+                               double *grad64, bool accumulate, cudaStream_t st) {
+    const long n = (long)nx * ny;
+    stack_exact_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(T, L, fstride, nshots, src_h, src_k, S, nx, ny,
+                                                                   nxp, dh, grad, grad64, accumulate);
+    return cudaGetLastError();
+}
+
 // cp_grad_frame.c:18-49: top rows, bottom rows, left columns, right columns,
 // each pass completing before the next reads it; applied `times` times.
 template <typename V>

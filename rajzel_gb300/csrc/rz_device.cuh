@@ -352,4 +352,45 @@ RZ_DEV float leung_qian_fast(float tc, float te, float tw, float ts, float tn, f
     return fminf(own, lt);
 }
 
+// ---------------------------------------------------------------------------
+// exact discrete adjoint: linearisation of the Godunov update at the
+// converged traveltimes (not in the reference)
+// ---------------------------------------------------------------------------
+// Cell (h,k) with T its converged traveltime, a / b the smaller x / z
+// neighbour, d = a - b, sh = S*DH.  One-sided (|d| >= sh): T = min(a,b) + sh,
+// dT depends on the smaller neighbour with weight 1 and dT/dS = DH.
+// Two-sided: with r = sqrt(2 sh^2 - d^2), T = (a + b + r)/2, so
+//   dT/da = (r - d)/(2r),  dT/db = (r + d)/(2r),  dT/dS = S DH^2 / r,
+// written without T - a or T - b, which would cancel.  The weights are
+// returned signed: negative points to the lower-index neighbour (west /
+// north), positive to the higher one (east / south), 0 to none.
+struct ExactCoef {
+    float wx, wz, gs;
+};
+
+RZ_DEV ExactCoef exact_coef(const float *T, int nxp, int nx, int ny, int h, int k, float s, float dh, bool source) {
+    ExactCoef c{0.f, 0.f, 0.f};
+    if (source) return c;
+    const float big = 3.0e38f;
+    const float *p = T + (size_t)k * nxp + h;
+    const float tw = h > 0 ? __ldcg(p - 1) : big, te = h < nx - 1 ? __ldcg(p + 1) : big;
+    const float tn = k > 0 ? __ldcg(p - nxp) : big, ts = k < ny - 1 ? __ldcg(p + nxp) : big;
+    const bool west = tw <= te, north = tn <= ts;
+    const float a = west ? tw : te, b = north ? tn : ts;
+    const float sh = s * dh, d = a - b;
+    if (fabsf(d) >= sh) {
+        if (a <= b) c.wx = west ? -1.f : 1.f;
+        else c.wz = north ? -1.f : 1.f;
+        c.gs = dh;
+        return c;
+    }
+    const float r = sqrtf(fmaf(2.0f * sh, sh, -d * d));
+    const float half_rcp = 0.5f / r;
+    const float wa = (r - d) * half_rcp, wb = (r + d) * half_rcp;
+    c.wx = west ? -wa : wa;
+    c.wz = north ? -wb : wb;
+    c.gs = s * dh * dh / r;
+    return c;
+}
+
 }  // namespace rz

@@ -38,7 +38,9 @@ __host__ __device__ inline int skew_lines(int nxb) { return 32 * nxb + 64; }
 constexpr int kEdgePad = 48;
 __host__ __device__ inline int edge_row(int nxp) { return nxp + 2 * kEdgePad; }
 
-enum Mode : int { kModeReference = 0, kModeFast = 1 };
+// kModeExact names the exact discrete adjoint sweeps (FP32); the forward of
+// such a launch runs in the context's reference or fast arithmetic.
+enum Mode : int { kModeReference = 0, kModeFast = 1, kModeExact = 2 };
 
 struct ShotParams {
     // grid
@@ -52,6 +54,8 @@ struct ShotParams {
     int do_residual;        // compute Tres and l2 from Tobs
     int do_adjoint;         // 0: forward (+ residuals) only
     int start_adjoint;      // 1: T and Tres are given; skip forward and residuals
+    int exact;              // adjoint: 0 Leung-Qian (sweep_adj.c), 1 exact discrete adjoint
+    int cotangent;          // exact: Tobs holds dJ/dTmod itself (vector-Jacobian product)
     // model (shared by all shots)
     const float *SA, *SB;   // skewed slowness
     const uint32_t *MA, *MB;  // skewed adjoint skip bits (frame | receiver | outside)
@@ -60,7 +64,11 @@ struct ShotParams {
     float *Told;            // reference-mode snapshot  [nshots][ny][nxp]
     float *L;               // adjoint field lambda [nshots][ny][nxp]
     float *TA, *TB;         // skewed traveltimes [nshots][nstrips][qn][32]
+                            // (exact adjoint: signed x weights, see exact_coef)
     float *EU, *ED;         // rows above / below each strip [nshots][nstrips][edge_row(nxp)]
+                            // (exact adjoint: their signed z weights)
+    float *WZA, *WZB;       // exact adjoint: skewed signed z weights, like TA/TB
+    float *RA, *RB;         // exact adjoint: skewed dJ/dT at receiver cells, like TA/TB
     size_t fstride;         // ny*nxp
     size_t sstride;         // nstrips*qn*32
     size_t estride;         // nstrips*edge_row(nxp)
@@ -73,6 +81,10 @@ struct ShotParams {
     // initialises lambda there ("last receiver wins", init_travel_adj.c:49-54)
     int nrcell;
     const int *rcell_h, *rcell_k, *rcell_rec;
+    // every receiver cell (frame included) with its receivers in index order:
+    // cell i holds receivers xcell_rec[xcell_off[i] .. xcell_off[i+1]-1]
+    int nxcell;
+    const int *xcell_h, *xcell_k, *xcell_off, *xcell_rec;
     const float *Tobs;      // [nshots][ntr]
     float *Tmod, *Tres;     // [nshots][ntr]
     double *l2;             // [nshots]
@@ -99,6 +111,11 @@ cudaError_t launch_skip_masks(const uint8_t *skip, int nx, int ny, int nstrips, 
 cudaError_t launch_stack(const float *L, size_t fstride, int nshots, const double *cube, const float *S, int nx,
                          int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, bool accumulate,
                          cudaStream_t st);
+// exact-adjoint gradient dJ/dVp = -S^2 sum_s mu_s * dG/dS (G the Godunov
+// update at the converged traveltimes T_s); continues grad64 when accumulate
+cudaError_t launch_stack_exact(const float *T, const float *L, size_t fstride, int nshots, const int *src_h,
+                               const int *src_k, const float *S, int nx, int ny, int nxp, float dh, float *grad,
+                               double *grad64, bool accumulate, cudaStream_t st);
 cudaError_t launch_cp_frame(float *A, double *A64, int nx, int ny, int pitch, int times, cudaStream_t st);
 cudaError_t launch_copy_rows(const float *src, int src_pitch, float *dst, int dst_pitch, int nx, int ny,
                              size_t nbatch, size_t src_bstride, size_t dst_bstride, cudaStream_t st);

@@ -105,8 +105,10 @@ constexpr int kRowFloats = kRing * kBlk;          // 96
 constexpr int kRowBytes = kRowFloats * 4;         // 384
 
 template <int DX, int DY, bool ADJ, int MODE>
-__device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mrow, float &acc, int band,
-                                   int W) {
+__device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mrow, float &acc, float &mag,
+                                   int band, int W) {
+    // exact discrete adjoint: mu = R + sum of the weights neighbours put on this cell
+    constexpr bool EX = ADJ && (MODE == kModeExact);
     const int l = w.l, g = w.g;
     // strips are swept in bands of W (one strip per warp); sig is the strip's
     // position in sweep order, s its index from the top of the grid
@@ -159,6 +161,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     uint32_t phase = w.phase;
     int err = 0;
     float acc_l = 0.f;  // fast-mode sum of |change| (the caller's acc lives in local memory)
+    float mag_l = 0.f;  // exact adjoint: sum of |mu|
     auto ring_wait_l = [&](int slot) {
         if (!mbar_wait_a(mbar_s + 8u * slot, (phase >> slot) & 1u, abort_s)) err |= ERR_TMA_TIMEOUT;
         phase ^= 1u << slot;
@@ -189,12 +192,17 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const float *xs;
     const uint32_t *mk = nullptr;
     const float *ep = nullptr;
+    const float *zs = nullptr, *rs = nullptr;  // exact adjoint: z weights (one column ahead), own-cell R
     {
         const int q0 = (DX > 0 ? 0 : ncol + 30) + QS * QOFF + kSkewFront;
         if (!ADJ) {
             xs = (famA ? P.SA : P.SB) + ((size_t)s * P.qn + q0) * 32 + j;
         } else {
             xs = (famA ? P.TA : P.TB) + (size_t)z * P.sstride + ((size_t)s * P.qn + q0) * 32 + j;
+            if (EX) {
+                zs = (famA ? P.WZA : P.WZB) + (size_t)z * P.sstride + ((size_t)s * P.qn + q0) * 32 + j;
+                rs = (famA ? P.RA : P.RB) + (size_t)z * P.sstride + ((size_t)s * P.qn + q0 - QS) * 32 + j;
+            }
             mk = (famA ? P.MA : P.MB) + (size_t)s * P.qn + (q0 - QS * QOFF);
             const float *erow = ((l == 31) == (DY > 0) ? P.ED : P.EU) + (size_t)z * P.estride +
                                 (size_t)s * edge_row(P.nxp) + kEdgePad;
@@ -205,18 +213,26 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     float xq[8];
     uint32_t mq[8];
     float eq[8];
+    float zq[8], rq[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
         if (!ADJ) {
             xq[i] = __ldg(xs + QS * 32 * i);
         } else {
             xq[i] = __ldca(xs + QS * 32 * i);
-            mq[i] = __ldg(mk + QS * i);
+            if (EX) {
+                zq[i] = __ldca(zs + QS * 32 * i);
+                rq[i] = __ldca(rs + QS * 32 * i);
+            } else {
+                mq[i] = __ldg(mk + QS * i);
+            }
             eq[i] = __ldca(ep + QS * i);
         }
     }
-    float c_tt = 0.f, w_tt = 0.f;
+    float c_tt = 0.f, w_tt = 0.f;  // exact adjoint: x weights of this and the previous column
+    float c_wz = 0.f, w_wz = 0.f;  // exact adjoint: z weights of this and the previous column
     if (ADJ) c_tt = __ldca(xs - QS * 32);
+    if (EX) c_wz = __ldca(zs - QS * 32);
 
     issue(0);
     if (nxb > 1) issue(1);
@@ -294,6 +310,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
             const float *xr = xs + QS * 32 * t0;
             const uint32_t *mr = ADJ ? mk + QS * t0 : nullptr;
             const float *er = ADJ ? ep + QS * t0 : nullptr;
+            const float *zr = EX ? zs + QS * 32 * t0 : nullptr;
+            const float *rr = EX ? rs + QS * 32 * t0 : nullptr;
             // ---- 8 wavefront steps, straight-line code ----
 #pragma unroll
             for (int ii = 0; ii < 8; ++ii) {
@@ -330,6 +348,35 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                         (MODE == kModeReference) ? godunov_ref(a, b, xv, dh) : godunov_fast(a, b, xv, dh);
                     r = fminf(own, tt);
                     r = valid ? r : own;
+                } else if (EX) {
+                    xq[ii] = __ldca(xr + QS * 32 * (ii + 8));
+                    const float e_wz = zq[ii];
+                    zq[ii] = __ldca(zr + QS * 32 * (ii + 8));
+                    const float rcell = rq[ii];
+                    rq[ii] = __ldca(rr + QS * 32 * (ii + 8));
+                    const float edge = eq[ii];
+                    eq[ii] = __ldca(er + QS * (ii + 8));
+                    const float e_wx = xv;  // x weight one column downstream
+                    float n_wz = __shfl_up_sync(0xffffffffu, w_wz, 1);
+                    float s_wz = __shfl_down_sync(0xffffffffu, e_wz, 1);
+                    n_wz = (l == 0) ? edge : n_wz;
+                    s_wz = (l == 31) ? edge : s_wz;
+                    // weights of the grid neighbours (signed: < 0 points west / north)
+                    const float wxE = DX > 0 ? e_wx : w_tt, wxW = DX > 0 ? w_tt : e_wx;
+                    const float wzS = DY > 0 ? s_wz : n_wz, wzN = DY > 0 ? n_wz : s_wz;
+                    const float lE = DX > 0 ? ev : res_prev, lW = DX > 0 ? res_prev : ev;
+                    const float lS = DY > 0 ? sv : nv, lN = DY > 0 ? nv : sv;
+                    float m = rcell;
+                    m = wxW > 0.f ? fmaf(wxW, lW, m) : m;
+                    m = wxE < 0.f ? fmaf(-wxE, lE, m) : m;
+                    m = wzN > 0.f ? fmaf(wzN, lN, m) : m;
+                    m = wzS < 0.f ? fmaf(-wzS, lS, m) : m;
+                    r = valid ? m : own;
+                    mag_l += valid ? fabsf(r) : 0.0f;
+                    w_tt = c_tt;
+                    c_tt = e_wx;
+                    w_wz = c_wz;
+                    c_wz = e_wz;
                 } else {
                     xq[ii] = __ldca(xr + QS * 32 * (ii + 8));
                     const uint32_t mword = mq[ii];
@@ -358,6 +405,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 }
                 sts(cur, r);
                 if (MODE == kModeFast) acc_l += valid ? own - r : 0.0f;
+                if (EX) acc_l += valid ? fabsf(own - r) : 0.0f;
                 // lane 31 hands its row down; after the 8th value of a group it signals
                 const int upp = t - 31;
                 sts_if(hb_out + 4u * (uint32_t)(upp & (kHandoff - 1)), r, producer && upp >= 0 && upp < ncol);
@@ -380,6 +428,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     w.phase = phase;
     w.err |= err;
     acc += acc_l;
+    mag += mag_l;
 }
 
 // ---------------------------------------------------------------------------
@@ -522,6 +571,72 @@ __device__ __noinline__ void relayout_strip(const ShotParams &P, Warp &w, const 
     }
 }
 
+// Exact discrete adjoint preparation (not in the reference): signed weights
+// of every cell on its upwind neighbours (exact_coef) in the skewed layout of
+// the sweeps (x weights in TA/TB, z weights in WZA/WZB, those of the rows
+// bordering each strip in EU/ED), dJ/dT at the receiver cells (RA/RB, the
+// residuals of each cell's receivers summed in receiver order), mu = 0.
+RZ_DEV void exact_prepare(const ShotParams &P, int z, const float *T, float *L) {
+    const int tid = threadIdx.x, nthr = blockDim.x;
+    const int l = tid & 31, g = tid >> 5, W = nthr >> 5;
+    const int hs = P.src_h[z], ks = P.src_k[z];
+    const int nx = P.nx, ny = P.ny, nxp = P.nxp, qn = P.qn;
+    const size_t lines = (size_t)P.nstrips * qn;
+    float *wxa = P.TA + (size_t)z * P.sstride, *wxb = P.TB + (size_t)z * P.sstride;
+    float *wza = P.WZA + (size_t)z * P.sstride, *wzb = P.WZB + (size_t)z * P.sstride;
+    float *ra = P.RA + (size_t)z * P.sstride, *rb = P.RB + (size_t)z * P.sstride;
+    for (size_t li = g; li < lines; li += W) {
+        const int s = (int)(li / qn), q = (int)(li - (size_t)s * qn) - kSkewFront;
+        const int row = kStrip * s + l;
+        const int ha = q - l, hb = q + l - 31;
+        const size_t o = li * 32 + l;
+        ExactCoef ca{0.f, 0.f, 0.f}, cb{0.f, 0.f, 0.f};
+        if (row < ny) {
+            if (ha >= 0 && ha < nx) ca = exact_coef(T, nxp, nx, ny, ha, row, __ldg(P.SA + o), P.dh, ha == hs && row == ks);
+            if (hb >= 0 && hb < nx) cb = exact_coef(T, nxp, nx, ny, hb, row, __ldg(P.SB + o), P.dh, hb == hs && row == ks);
+        }
+        wxa[o] = ca.wx;
+        wza[o] = ca.wz;
+        ra[o] = 0.f;
+        wxb[o] = cb.wx;
+        wzb[o] = cb.wz;
+        rb[o] = 0.f;
+    }
+    // z weights of the rows above (EU) and below (ED) each strip
+    const int er = edge_row(nxp);
+    for (int i = tid; i < P.nstrips * nxp; i += nthr) {
+        const int s = i / nxp, col = i - s * nxp;
+        const int ru = kStrip * s - 1, rd = kStrip * s + kStrip;
+        float vu = 0.f, vd = 0.f;
+        if (col < nx) {
+            // slowness of these cells from the skewed copy (family A, q = h + j)
+            if (ru >= 0) {
+                const size_t o = ((size_t)(s - 1) * qn + (col + 31) + kSkewFront) * 32 + 31;
+                vu = exact_coef(T, nxp, nx, ny, col, ru, __ldg(P.SA + o), P.dh, col == hs && ru == ks).wz;
+            }
+            if (rd < ny) {
+                const size_t o = ((size_t)(s + 1) * qn + col + kSkewFront) * 32;
+                vd = exact_coef(T, nxp, nx, ny, col, rd, __ldg(P.SA + o), P.dh, col == hs && rd == ks).wz;
+            }
+        }
+        P.EU[(size_t)z * P.estride + (size_t)s * er + kEdgePad + col] = vu;
+        P.ED[(size_t)z * P.estride + (size_t)s * er + kEdgePad + col] = vd;
+    }
+    for (int c = tid; c < nx * ny; c += nthr) {
+        const int k = c / nx, h = c - k * nx;
+        L[(size_t)k * nxp + h] = 0.f;
+    }
+    __syncthreads();
+    for (int i = tid; i < P.nxcell; i += nthr) {
+        const int h = P.xcell_h[i], k = P.xcell_k[i];
+        float sum = 0.f;
+        for (int r = P.xcell_off[i]; r < P.xcell_off[i + 1]; ++r) sum += P.Tres[(size_t)z * P.ntr + P.xcell_rec[r]];
+        const int s = k >> 5, j = k & 31;
+        ra[((size_t)s * qn + (h + j) + kSkewFront) * 32 + j] = sum;
+        rb[((size_t)s * qn + (h - j + 31) + kSkewFront) * 32 + j] = sum;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // the shot kernel
 // ---------------------------------------------------------------------------
@@ -599,22 +714,22 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
                 fence_proxy_async_global();
                 __syncthreads();
             }
-            float acc = 0.f;
+            float acc = 0.f, mag = 0.f;
             for (int b = 0; b < nbands; ++b) {
-                sweep<+1, +1, false, MODE>(P, w, &mTrow, acc, b, W);
+                sweep<+1, +1, false, MODE>(P, w, &mTrow, acc, mag, b, W);
                 sweep_barrier(sh);
             }
             if (pass == 0) stamp(P, z, 5);
             for (int b = 0; b < nbands; ++b) {
-                sweep<-1, +1, false, MODE>(P, w, &mTrow, acc, b, W);
+                sweep<-1, +1, false, MODE>(P, w, &mTrow, acc, mag, b, W);
                 sweep_barrier(sh);
             }
             for (int b = 0; b < nbands; ++b) {
-                sweep<-1, -1, false, MODE>(P, w, &mTrow, acc, b, W);
+                sweep<-1, -1, false, MODE>(P, w, &mTrow, acc, mag, b, W);
                 sweep_barrier(sh);
             }
             for (int b = 0; b < nbands; ++b) {
-                sweep<+1, -1, false, MODE>(P, w, &mTrow, acc, b, W);
+                sweep<+1, -1, false, MODE>(P, w, &mTrow, acc, mag, b, W);
                 sweep_barrier(sh);
             }
             ++pass;
@@ -645,7 +760,12 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
                     P.Tmod[(size_t)z * P.ntr + r] = tm;
                     const float tob = P.do_residual ? P.Tobs[(size_t)z * P.ntr + r] : -1.0f;
                     float tr = 0.f, q = 0.f;
-                    if (tob >= 0.0f) {
+                    if (P.cotangent) {
+                        tr = tob;  // dJ/dTmod given by the caller
+                    } else if (P.exact && tob >= 0.0f) {
+                        tr = __fsub_rn(tm, tob);  // dJ/dTmod of J = 0.5 sum (Tmod - Tobs)^2
+                        q = __fmul_rn(tr, tr);
+                    } else if (tob >= 0.0f) {
                         tr = __fsub_rn(tm, tob);
                         q = __fmul_rn(tr, tr);
                         float gt;
@@ -693,17 +813,21 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
         if (tid == 0) atomicOr(&P.status[z], cta_err);
         return;
     }
-    for (int s = g; s < P.nstrips; s += W) relayout_strip<0>(P, w, &mTld, s);
-    // lambda: 0 on the frame, 10*TIME inside, residuals at receiver cells
-    const float linit = (float)(10.0 * (double)P.time);
-    for (int c = tid; c < n; c += blockDim.x) {
-        int k = c / P.nx, h = c - k * P.nx;
-        bool in = (h > 0 && h < P.nx - 1 && k > 0 && k < P.ny - 1);
-        L[(size_t)k * P.nxp + h] = in ? linit : 0.0f;
+    if (P.exact) {
+        exact_prepare(P, z, T, L);
+    } else {
+        for (int s = g; s < P.nstrips; s += W) relayout_strip<0>(P, w, &mTld, s);
+        // lambda: 0 on the frame, 10*TIME inside, residuals at receiver cells
+        const float linit = (float)(10.0 * (double)P.time);
+        for (int c = tid; c < n; c += blockDim.x) {
+            int k = c / P.nx, h = c - k * P.nx;
+            bool in = (h > 0 && h < P.nx - 1 && k > 0 && k < P.ny - 1);
+            L[(size_t)k * P.nxp + h] = in ? linit : 0.0f;
+        }
+        __syncthreads();
+        for (int i = tid; i < P.nrcell; i += blockDim.x)
+            L[(size_t)P.rcell_k[i] * P.nxp + P.rcell_h[i]] = P.Tres[(size_t)z * P.ntr + P.rcell_rec[i]];
     }
-    __syncthreads();
-    for (int i = tid; i < P.nrcell; i += blockDim.x)
-        L[(size_t)P.rcell_k[i] * P.nxp + P.rcell_h[i]] = P.Tres[(size_t)z * P.ntr + P.rcell_rec[i]];
     fence_proxy_async_global();
     __syncthreads();
     stamp(P, z, 3);
@@ -716,32 +840,60 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
             cta_err |= ERR_NOCONV_ADJ;
             break;
         }
-        if (MODE == kModeReference) {
+        if (MODE == kModeReference && !P.exact) {
             copy_field(P, L, Told);
             fence_proxy_async_global();
             __syncthreads();
         }
-        float acc = 0.f;
-        for (int b = 0; b < nbands; ++b) {
-                sweep<+1, +1, true, MODE>(P, w, &mLrow, acc, b, W);
+        float acc = 0.f, mag = 0.f;
+        if (P.exact) {
+            // same four orderings as the Leung-Qian sweeps (eikonal_adj.c:43-46)
+            for (int b = 0; b < nbands; ++b) {
+                sweep<+1, +1, true, kModeExact>(P, w, &mLrow, acc, mag, b, W);
                 sweep_barrier(sh);
             }
-        if (pass == 0) stamp(P, z, 6);
-        for (int b = 0; b < nbands; ++b) {
-                sweep<+1, -1, true, MODE>(P, w, &mLrow, acc, b, W);
+            if (pass == 0) stamp(P, z, 6);
+            for (int b = 0; b < nbands; ++b) {
+                sweep<+1, -1, true, kModeExact>(P, w, &mLrow, acc, mag, b, W);
                 sweep_barrier(sh);
             }
-        for (int b = 0; b < nbands; ++b) {
-                sweep<-1, +1, true, MODE>(P, w, &mLrow, acc, b, W);
+            for (int b = 0; b < nbands; ++b) {
+                sweep<-1, +1, true, kModeExact>(P, w, &mLrow, acc, mag, b, W);
                 sweep_barrier(sh);
             }
-        for (int b = 0; b < nbands; ++b) {
-                sweep<-1, -1, true, MODE>(P, w, &mLrow, acc, b, W);
+            for (int b = 0; b < nbands; ++b) {
+                sweep<-1, -1, true, kModeExact>(P, w, &mLrow, acc, mag, b, W);
                 sweep_barrier(sh);
             }
+        } else {
+            for (int b = 0; b < nbands; ++b) {
+                sweep<+1, +1, true, MODE>(P, w, &mLrow, acc, mag, b, W);
+                sweep_barrier(sh);
+            }
+            if (pass == 0) stamp(P, z, 6);
+            for (int b = 0; b < nbands; ++b) {
+                sweep<+1, -1, true, MODE>(P, w, &mLrow, acc, mag, b, W);
+                sweep_barrier(sh);
+            }
+            for (int b = 0; b < nbands; ++b) {
+                sweep<-1, +1, true, MODE>(P, w, &mLrow, acc, mag, b, W);
+                sweep_barrier(sh);
+            }
+            for (int b = 0; b < nbands; ++b) {
+                sweep<-1, -1, true, MODE>(P, w, &mLrow, acc, mag, b, W);
+                sweep_barrier(sh);
+            }
+        }
         ++pass;
         if (*w.abort_word) break;
-        if (MODE == kModeReference) {
+        if (P.exact) {
+            // the adjoint system is triangular in arrival order: Gauss-Seidel
+            // sweeps reach its solution exactly; stop once a pass changes it
+            // by less than 1e-7 of its magnitude
+            double tot = block_sum((double)acc, sh);
+            double m = block_sum((double)mag, sh);
+            go = tot > 1e-7 * m;
+        } else if (MODE == kModeReference) {
             go = ref_continue(P, L, Told, sh);
         } else {
             double tot = block_sum((double)acc, sh);

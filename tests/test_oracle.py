@@ -133,3 +133,37 @@ def test_shot_partition_matches_init_mpishot(oracle_mod):
         assert all(spans[i][1] == spans[i + 1][0] for i in range(np_ - 1))
         sizes = [b - a for a, b in spans]
         assert max(sizes) - min(sizes) <= 1 and sizes == sorted(sizes, reverse=True)
+
+
+def _fd_case(O, seed, nx, ny, nshots, muted=False):
+    w = synth.small_case(seed, nx, ny, nshots=nshots)
+    p = O.Params(w.nx, w.ny, w.dh, w.time, 1e-14, w.eps_adj)
+    vp = w.vp_true.astype(np.float64)
+    Tobs = np.empty((nshots, w.ntr))
+    for i in range(nshots):
+        t, _ = O.eikonal_f64(p, 1.0 / (vp * 1.03), w.srcx[i], w.srcz[i])
+        Tobs[i] = t[w.recz - 1, w.recx - 1]
+    if muted:
+        Tobs[:, ::5] = -1.0
+    return w, p, vp, Tobs
+
+
+@pytest.mark.parametrize("muted", [False, True])
+def test_exact_adjoint_oracle_matches_finite_differences(oracle_mod, muted):
+    """The FP64 exact discrete adjoint (cells visited in order of decreasing
+    traveltime) against central differences of the FP64 misfit along random
+    slowness perturbations."""
+    O = oracle_mod
+    w, p, vp, Tobs = _fd_case(O, 5, 48, 36, 2, muted)
+    S = 1.0 / vp
+    g_vp, L2 = O.grad_exact_f64(p, S, w.srcx, w.srcz, w.recx, w.recz, Tobs)
+    assert L2 == pytest.approx(O.misfit_f64(p, S, w.srcx, w.srcz, w.recx, w.recz, Tobs), rel=1e-15)
+    g_s = -g_vp * vp * vp  # dJ/dS = dJ/dVp * dVp/dS
+    rng = np.random.default_rng(1)
+    for _ in range(4):
+        d = rng.standard_normal(S.shape) * S
+        eps = 1e-6
+        jp = O.misfit_f64(p, S + eps * d, w.srcx, w.srcz, w.recx, w.recz, Tobs)
+        jm = O.misfit_f64(p, S - eps * d, w.srcx, w.srcz, w.recx, w.recz, Tobs)
+        fd = (jp - jm) / (2 * eps)
+        assert abs(fd - (g_s * d).sum()) <= 1e-6 * abs(fd)
