@@ -36,6 +36,8 @@ METRIC = "fwd+adjoint shots/s & point-updates/s, batched vs plain GPU, rel err<=
 WORKLOAD = "grad_1700x350: 100 shots x 850 receivers, 1700x350 grid, dh=10 m, fwd+residual+adjoint+stack"
 ALG_BYTES_FWD = 12  # per forward point-update: slowness read, traveltime read + write
 ALG_BYTES_ADJ = 16  # per adjoint point-update: traveltime, lambda read + write, receiver flag
+CHECK_BYTES_FWD = 8  # per cell of a forward fixpoint check: traveltime, slowness read
+CHECK_BYTES_ADJ = 9  # per interior cell of an adjoint fixpoint check: traveltime, lambda, receiver flag
 
 
 def log(*a):
@@ -213,8 +215,12 @@ def run_gpu_arm(args, rank, world, local_rank):
     torch.cuda.synchronize()
     # passes and point-updates of one step (identical every step: same inputs)
     passes = np.array([ctx.shot_info(i)[:2] for i in range(w.nshots)])
-    pu_fwd = int(passes[:, 0].sum()) * 4 * w.nx * w.ny
-    pu_adj = int(passes[:, 1].sum()) * 4 * (w.nx - 2) * (w.ny - 2)
+    swept = np.array([ctx.shot_work(i) for i in range(w.nshots)])
+    # point-updates actually performed (a pass proven by the fixpoint check to
+    # change nothing is counted by the reference's rule but not swept)
+    pu_fwd = int(swept[:, 0].sum()) * 4 * w.nx * w.ny
+    pu_adj = int(swept[:, 1].sum()) * 4 * (w.nx - 2) * (w.ny - 2)
+    checks = (passes - swept).sum(axis=0)  # successful fixpoint checks (forward, adjoint)
     launches0, _, _ = ctx.kernel_stats()  # also clears the per-launch timing list
 
     clocks = ClockSampler(local_rank)
@@ -243,7 +249,8 @@ def run_gpu_arm(args, rank, world, local_rank):
         ms = float(t.item())
     value = world * w.nshots * args.steps / (ms / 1e3)
     kernel_ms = shot_ms / max(shot_calls, 1)
-    alg_bytes = pu_fwd * ALG_BYTES_FWD + pu_adj * ALG_BYTES_ADJ
+    alg_bytes = (pu_fwd * ALG_BYTES_FWD + pu_adj * ALG_BYTES_ADJ + int(checks[0]) * CHECK_BYTES_FWD * w.nx * w.ny
+                 + int(checks[1]) * CHECK_BYTES_ADJ * (w.nx - 2) * (w.ny - 2))
     hbm_peak, peak_src = 6800.0, "fallback"
     try:
         hbm_peak, peak_src = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))["hbm_gbs"]), "measured"
@@ -303,6 +310,7 @@ def run_gpu_arm(args, rank, world, local_rank):
         "point_updates_per_s": world * (pu_fwd + pu_adj) * args.steps / (ms / 1e3),
         "point_updates_per_step": pu_fwd + pu_adj,
         "passes_fwd_adj": [int(passes[:, 0].sum()), int(passes[:, 1].sum())],
+        "passes_swept_fwd_adj": [int(swept[:, 0].sum()), int(swept[:, 1].sum())],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": peak_src,
                      "traffic": traffic,

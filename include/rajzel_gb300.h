@@ -149,6 +149,11 @@ int rz_backward(rz_context *ctx, int nshots, const float *srcx, const float *src
    may be NULL): outer passes of forward/adjoint, device status bits. */
 int rz_shot_info(rz_context *ctx, int shot, int *fwd_passes, int *adj_passes, int *status);
 
+/* Passes of shot `shot` in the last batch that were actually swept.  A pass
+   that a parallel fixpoint check proves to change no cell is counted in
+   rz_shot_info's pass counts (the reference runs it) but not swept. */
+int rz_shot_work(rz_context *ctx, int shot, int *fwd_swept, int *adj_swept);
+
 /* Fields of shot `shot` from the last rz_grad_obj: TT, lambda [ny][nx],
    Tres [ntr] (scaled residuals as passed to eikonal_adj).  TT and lambda
    are kept only for the shots of the last chunk (all shots when the batch

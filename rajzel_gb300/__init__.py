@@ -78,9 +78,10 @@ def load_library(path: str = LIB_PATH):
     lib.rz_kernel_stats.argtypes = [vp, vp, vp, vp]
     lib.rz_eikonal_adj.argtypes = [vp, vp, vp, vp, vp, C.c_int]
     lib.rz_set_memory_cap.argtypes = [vp, C.c_size_t]
+    lib.rz_shot_work.argtypes = [vp, C.c_int, vp, vp]
     lib.rz_set_gradient.argtypes = [vp, C.c_int]
     lib.rz_backward.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
-    for name in ("rz_set_memory_cap", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
+    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
                  "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
                  "rz_eikonal_adj", "rz_shot_timeline", "rz_kernel_stats"):
         getattr(lib, name).restype = C.c_int
@@ -241,6 +242,12 @@ class Context:
         a, b, s = C.c_int(0), C.c_int(0), C.c_int(0)
         self._check(self.lib.rz_shot_info(self.h, int(shot), C.byref(a), C.byref(b), C.byref(s)), "rz_shot_info")
         return a.value, b.value, s.value
+
+    def shot_work(self, shot):
+        """(forward, adjoint) passes actually swept for one shot of the last batch."""
+        a, b = C.c_int(0), C.c_int(0)
+        self._check(self.lib.rz_shot_work(self.h, int(shot), C.byref(a), C.byref(b)), "rz_shot_work")
+        return a.value, b.value
 
     def kernel_stats(self):
         """(kernels launched so far, summed shot-kernel ms since the last call, shot-kernel calls)."""

@@ -70,6 +70,7 @@ struct rz_context {
     float *dTobs = nullptr, *dTmod = nullptr, *dTres = nullptr;
     double *dl2 = nullptr, *dL2 = nullptr;
     int *dPf = nullptr, *dPa = nullptr, *dStat = nullptr, *dSrcH = nullptr, *dSrcK = nullptr;
+    int *dSwept = nullptr;  // [n][2] passes actually swept
     unsigned long long *dTl = nullptr;
     float *dGrad = nullptr;
     double *dGrad64 = nullptr;
@@ -163,7 +164,7 @@ static void free_fields(rz_context *c) {
 
 static void free_shots(rz_context *c) {
     dfree(c->dTobs), dfree(c->dTmod), dfree(c->dTres), dfree(c->dl2), dfree(c->dPf), dfree(c->dPa);
-    dfree(c->dStat), dfree(c->dSrcH), dfree(c->dSrcK), dfree(c->dTl);
+    dfree(c->dStat), dfree(c->dSrcH), dfree(c->dSrcK), dfree(c->dTl), dfree(c->dSwept);
     c->cap_s = 0;
 }
 
@@ -226,6 +227,7 @@ static int ensure_shots(rz_context *c, int n) {
     CK(dalloc(&c->dSrcH, (size_t)n));
     CK(dalloc(&c->dSrcK, (size_t)n));
     CK(dalloc(&c->dTl, (size_t)n * kTimelineSlots));
+    CK(dalloc(&c->dSwept, (size_t)n * 2));
     c->cap_s = n;
     return RZ_OK;
 }
@@ -306,6 +308,8 @@ static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     P.div_fast = c->div_fast;
     P.max_passes = c->g.max_passes > 0 ? c->g.max_passes : 10000;
     P.nshots = n;
+    P.S = c->dS;
+    P.skip = c->dSkip;
     P.SA = c->dSA;
     P.SB = c->dSB;
     P.MA = c->dMA;
@@ -346,6 +350,7 @@ static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     P.passes_adj = c->dPa + first;
     P.status = c->dStat + first;
     P.timeline = c->dTl + (size_t)first * kTimelineSlots;
+    P.swept = c->dSwept + (size_t)first * 2;
 }
 
 static int status_to_code(int bits) {
@@ -421,6 +426,7 @@ static int reset_shots(rz_context *c, int n) {
     CK(cudaMemsetAsync(c->dTl, 0, (size_t)n * kTimelineSlots * sizeof(unsigned long long), c->st));
     CK(cudaMemsetAsync(c->dPf, 0, n * sizeof(int), c->st));
     CK(cudaMemsetAsync(c->dPa, 0, n * sizeof(int), c->st));
+    CK(cudaMemsetAsync(c->dSwept, 0, 2 * n * sizeof(int), c->st));
     c->last_n = n;
     return RZ_OK;
 }
@@ -818,6 +824,18 @@ int rz_shot_info(rz_context *c, int shot, int *fwd_passes, int *adj_passes, int 
     if (fwd_passes) *fwd_passes = v[0];
     if (adj_passes) *adj_passes = v[1];
     if (status) *status = v[2];
+    return RZ_OK;
+}
+
+int rz_shot_work(rz_context *c, int shot, int *fwd_swept, int *adj_swept) {
+    if (!c) return RZ_EINVAL;
+    if (shot < 0 || shot >= c->last_n) return fail(c, RZ_EINVAL, "shot %d not in the last batch", shot);
+    cudaSetDevice(c->device);
+    int v[2] = {0, 0};
+    CK(cudaMemcpyAsync(v, c->dSwept + 2 * (size_t)shot, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    if (fwd_swept) *fwd_swept = v[0];
+    if (adj_swept) *adj_swept = v[1];
     return RZ_OK;
 }
 

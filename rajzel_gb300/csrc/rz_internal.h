@@ -57,6 +57,8 @@ struct ShotParams {
     int exact;              // adjoint: 0 Leung-Qian (sweep_adj.c), 1 exact discrete adjoint
     int cotangent;          // exact: Tobs holds dJ/dTmod itself (vector-Jacobian product)
     // model (shared by all shots)
+    const float *S;         // slowness [ny][nx]
+    const uint8_t *skip;    // receiver cell flags [ny][nx] (adjoint fixpoint check), or null
     const float *SA, *SB;   // skewed slowness
     const uint32_t *MA, *MB;  // skewed adjoint skip bits (frame | receiver | outside)
     // per-shot fields; shot z at offset z*fstride (floats)
@@ -89,6 +91,9 @@ struct ShotParams {
     float *Tmod, *Tres;     // [nshots][ntr]
     double *l2;             // [nshots]
     int *passes_fwd, *passes_adj, *status;  // [nshots]
+    // passes actually swept [nshots][2] (forward, adjoint): a pass proven to
+    // change nothing is counted in passes_* but not swept
+    int *swept;
     unsigned long long *timeline;           // [nshots][kTimelineSlots] ns stamps, or null
 };
 

@@ -130,6 +130,7 @@ extern "C" int rz_eikonal_noalloc(const rz_grid *grid, const float *S, float src
     P.dh_rcp = (float)(1.0 / (double)g.dh);
     P.max_passes = g.max_passes > 0 ? g.max_passes : 10000;
     P.nshots = 1;
+    P.S = S;
     P.SA = SA;
     P.SB = SB;
     P.T = T;

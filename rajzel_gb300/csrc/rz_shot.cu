@@ -23,6 +23,8 @@
 // converged traveltimes, adjoint skip bits) are stored pre-skewed so that the
 // 32 values one wavefront step needs are one 128-byte line: fully coalesced
 // and prefetched eight steps ahead into registers.
+#include <type_traits>
+
 #include "rz_device.cuh"
 #include "rz_internal.h"
 
@@ -136,7 +138,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
         prev_row = (ADJ ? P.L : P.T) + (size_t)z * P.fstride + (size_t)rup * P.nxp;
     }
     const bool producer = (l == 31) && is_producer_warp;
-    const bool consumer = (l == 0) && is_consumer_warp;
     const int ngrp = ncol >> 3;  // hand-off groups per sweep
     float *ring = &w.ws->ring[0][0];
     const uint32_t ring_s = smem_u32(ring);
@@ -150,7 +151,9 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const bool div_fast = P.div_fast != 0;
     // valid sweep-local columns [lo, hi) of this lane's row
     const int lo = DX > 0 ? 0 : ncol - nx;
-    const int hi = rowok ? (DX > 0 ? nx : ncol) : lo;
+    const int hi_row = DX > 0 ? nx : ncol;
+    const int hi = rowok ? hi_row : lo;
+    const bool full_strip = kStrip * s + kStrip - 1 < P.ny;  // all 32 rows inside the grid
     // everything the step loop touches lives in registers: shared-window
     // addresses of the barriers, the phase bits, the error bits
     const uint32_t abort_s = smem_u32((const void *)w.abort_word);
@@ -201,7 +204,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
             xs = (famA ? P.TA : P.TB) + (size_t)z * P.sstride + ((size_t)s * P.qn + q0) * 32 + j;
             if (EX) {
                 zs = (famA ? P.WZA : P.WZB) + (size_t)z * P.sstride + ((size_t)s * P.qn + q0) * 32 + j;
-                rs = (famA ? P.RA : P.RB) + (size_t)z * P.sstride + ((size_t)s * P.qn + q0 - QS) * 32 + j;
+                rs = (famA ? P.RA : P.RB) + (size_t)z * P.sstride + ((size_t)s * P.qn + (q0 - QS)) * 32 + j;
             }
             mk = (famA ? P.MA : P.MB) + (size_t)s * P.qn + (q0 - QS * QOFF);
             const float *erow = ((l == 31) == (DY > 0) ? P.ED : P.EU) + (size_t)z * P.estride +
@@ -313,6 +316,11 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
             const float *zr = EX ? zs + QS * 32 * t0 : nullptr;
             const float *rr = EX ? rs + QS * 32 * t0 : nullptr;
             // ---- 8 wavefront steps, straight-line code ----
+            // IN: every lane's 8 cells lie inside the grid, away from its
+            // west/east border, and lane 31's hand-off range covers them all
+            // (most groups): the per-step border and range tests drop out
+            auto steps8 = [&](auto interior_tag) {
+            constexpr bool IN = decltype(interior_tag)::value;
 #pragma unroll
             for (int ii = 0; ii < 8; ++ii) {
                 const int t = t0 + ii;
@@ -333,12 +341,12 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 nv = (l == 0) ? hbq[ii] : nv;
                 sv = (l == 31) ? halo : sv;
                 const float xv = xq[ii];
-                const bool valid = (unsigned)(up - lo) < (unsigned)(hi - lo);
+                const bool valid = IN || (unsigned)(up - lo) < (unsigned)(hi - lo);
                 float r;
                 if (!ADJ) {
                     xq[ii] = __ldg(xr + QS * 32 * (ii + 8));
-                    const bool hasW = up > lo;
-                    const bool hasE = up < hi - 1;
+                    const bool hasW = IN || up > lo;
+                    const bool hasE = IN || up < hi - 1;
                     const float tw = hasW ? res_prev : own;
                     const float te = hasE ? ev : own;
                     const float tn = hasUp ? nv : own;
@@ -398,7 +406,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     } else {
                         r = leung_qian_fast(c_tt, tE, tW, tS, tN, lE, lW, lS, lN, own, dh_rcp, eps_adj);
                     }
-                    const bool keep = !valid || ((mword >> j) & 1u);
+                    const bool keep = (!IN && !valid) || ((mword >> j) & 1u);
                     r = keep ? own : r;
                     w_tt = c_tt;
                     c_tt = e_tt;
@@ -408,11 +416,14 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 if (EX) acc_l += valid ? fabsf(own - r) : 0.0f;
                 // lane 31 hands its row down; after the 8th value of a group it signals
                 const int upp = t - 31;
-                sts_if(hb_out + 4u * (uint32_t)(upp & (kHandoff - 1)), r, producer && upp >= 0 && upp < ncol);
+                sts_if(hb_out + 4u * (uint32_t)(upp & (kHandoff - 1)), r, IN ? producer : (producer && upp >= 0 && upp < ncol));
                 if (ii == 6) mbar_arrive_if(full_out + 8u * (((t - 38) >> 3) & (kGroups - 1)),
-                                            producer && t >= 38 && ((t - 38) >> 3) < ngrp);
+                                            IN ? producer : (producer && t >= 38 && ((t - 38) >> 3) < ngrp));
                 res_prev = r;
             }
+            };
+            if (full_strip && t0 >= lo + 32 && t0 + 9 <= hi_row) steps8(std::true_type{});
+            else steps8(std::false_type{});
         }
         // block k-1 is complete: write it back (each lane its own row)
         if (k >= 1) {
@@ -511,6 +522,52 @@ RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold,
     int d = sh.ctl[0];
     __syncthreads();
     return d != 0;
+}
+
+// Fixpoint checks.  Every point update of a sweep is F_c = min(own, G_c)
+// of the current field; if no cell of the field would change under F (each
+// evaluated on the same field, in the sweep's arithmetic), then a
+// Gauss-Seidel pass changes nothing: its first update leaves the field as it
+// is, hence so does the second, and so on through all four sweeps.  Such a
+// pass has zero change, so the stopping rule ends the loop after it; the
+// caller counts it without sweeping it, and every result stays the same.
+template <int MODE>
+RZ_DEV bool forward_is_fixpoint(const ShotParams &P, const float *T) {
+    const int nx = P.nx, ny = P.ny, nxp = P.nxp, n = nx * ny;
+    bool change = false;
+    for (int c = threadIdx.x; c < n && !change; c += blockDim.x) {
+        const int k = c / nx, h = c - k * nx;
+        const float *p = T + (size_t)k * nxp + h;
+        const float own = __ldcg(p);
+        const float tw = h > 0 ? __ldcg(p - 1) : own, te = h < nx - 1 ? __ldcg(p + 1) : own;
+        const float tn = k > 0 ? __ldcg(p - nxp) : own, ts = k < ny - 1 ? __ldcg(p + nxp) : own;
+        const float a = fminf(tw, te), b = fminf(tn, ts), sv = __ldg(P.S + c);
+        const float tt = (MODE == kModeReference) ? godunov_ref(a, b, sv, P.dh) : godunov_fast(a, b, sv, P.dh);
+        change = tt < own;
+    }
+    return !__syncthreads_or(change);
+}
+
+// the Leung-Qian update of interior, non-receiver cells (sweep_adj.c:26-30)
+template <int MODE>
+RZ_DEV bool adjoint_is_fixpoint(const ShotParams &P, const float *T, const float *L) {
+    const int nx = P.nx, ny = P.ny, nxp = P.nxp, ni = nx - 2, n = ni * (ny - 2);
+    DivDH div{P.dh, P.dh_rcp, P.div_fast != 0};
+    bool change = false;
+    for (int c = threadIdx.x; c < n && !change; c += blockDim.x) {
+        const int k = 1 + c / ni, h = 1 + c - (k - 1) * ni;
+        if (P.skip[(size_t)k * nx + h]) continue;
+        const size_t o = (size_t)k * nxp + h;
+        const float own = __ldcg(L + o);
+        const float tc = __ldcg(T + o), te = __ldcg(T + o + 1), tw = __ldcg(T + o - 1);
+        const float ts = __ldcg(T + o + nxp), tn = __ldcg(T + o - nxp);
+        const float le = __ldcg(L + o + 1), lw = __ldcg(L + o - 1), ls = __ldcg(L + o + nxp), ln = __ldcg(L + o - nxp);
+        const float r = (MODE == kModeReference)
+                            ? leung_qian_ref(tc, te, tw, ts, tn, le, lw, ls, ln, own, div, P.eps_adj)
+                            : leung_qian_fast(tc, te, tw, ts, tn, le, lw, ls, ln, own, P.dh_rcp, P.eps_adj);
+        change = r != own;
+    }
+    return !__syncthreads_or(change);
 }
 
 RZ_DEV void copy_field(const ShotParams &P, const float *src, float *dst) {
@@ -702,7 +759,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
         fence_proxy_async_global();
         __syncthreads();
 
-        int pass = 0;
+        int pass = 0, swept = 0;
         bool go = true;
         while (go) {
             if (pass >= P.max_passes) {
@@ -733,6 +790,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
                 sweep_barrier(sh);
             }
             ++pass;
+            ++swept;
             if (*w.abort_word) break;
             if (MODE == kModeReference) {
                 go = ref_continue(P, T, Told, sh);
@@ -740,8 +798,13 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
                 double tot = block_sum((double)acc, sh);
                 go = (tot / (double)n) >= (double)P.ttnorm;
             }
+            if (go && pass < P.max_passes && forward_is_fixpoint<MODE>(P, T)) {
+                ++pass;  // the next pass would change nothing
+                go = false;
+            }
         }
         if (tid == 0) P.passes_fwd[z] = pass;
+        if (tid == 0 && P.swept) P.swept[2 * z] = swept;
         stamp(P, z, 1);
 
         // ---------------- receivers: picks, residuals, misfit ----------------
@@ -833,7 +896,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
     stamp(P, z, 3);
 
     // ---------------- adjoint ----------------
-    int pass = 0;
+    int pass = 0, swept = 0;
     bool go = true;
     while (go) {
         if (pass >= P.max_passes) {
@@ -885,6 +948,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
             }
         }
         ++pass;
+        ++swept;
         if (*w.abort_word) break;
         if (P.exact) {
             // the adjoint system is triangular in arrival order: Gauss-Seidel
@@ -899,8 +963,13 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
             double tot = block_sum((double)acc, sh);
             go = (tot / (double)n) >= (double)P.ttnorm;
         }
+        if (go && !P.exact && P.skip && pass < P.max_passes && adjoint_is_fixpoint<MODE>(P, T, L)) {
+            ++pass;  // the next pass would change nothing
+            go = false;
+        }
     }
     if (tid == 0) P.passes_adj[z] = pass;
+    if (tid == 0 && P.swept) P.swept[2 * z + 1] = swept;
     stamp(P, z, 4);
     __syncthreads();
     if (l == 0) atomicOr(&P.status[z], w.err);
