@@ -23,8 +23,6 @@
 // converged traveltimes, adjoint skip bits) are stored pre-skewed so that the
 // 32 values one wavefront step needs are one 128-byte line: fully coalesced
 // and prefetched eight steps ahead into registers.
-#include <type_traits>
-
 #include "rz_device.cuh"
 #include "rz_internal.h"
 
@@ -151,9 +149,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const bool div_fast = P.div_fast != 0;
     // valid sweep-local columns [lo, hi) of this lane's row
     const int lo = DX > 0 ? 0 : ncol - nx;
-    const int hi_row = DX > 0 ? nx : ncol;
-    const int hi = rowok ? hi_row : lo;
-    const bool full_strip = kStrip * s + kStrip - 1 < P.ny;  // all 32 rows inside the grid
+    const int hi = rowok ? (DX > 0 ? nx : ncol) : lo;
     // everything the step loop touches lives in registers: shared-window
     // addresses of the barriers, the phase bits, the error bits
     const uint32_t abort_s = smem_u32((const void *)w.abort_word);
@@ -316,11 +312,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
             const float *zr = EX ? zs + QS * 32 * t0 : nullptr;
             const float *rr = EX ? rs + QS * 32 * t0 : nullptr;
             // ---- 8 wavefront steps, straight-line code ----
-            // IN: every lane's 8 cells lie inside the grid, away from its
-            // west/east border, and lane 31's hand-off range covers them all
-            // (most groups): the per-step border and range tests drop out
-            auto steps8 = [&](auto interior_tag) {
-            constexpr bool IN = decltype(interior_tag)::value;
 #pragma unroll
             for (int ii = 0; ii < 8; ++ii) {
                 const int t = t0 + ii;
@@ -341,12 +332,12 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 nv = (l == 0) ? hbq[ii] : nv;
                 sv = (l == 31) ? halo : sv;
                 const float xv = xq[ii];
-                const bool valid = IN || (unsigned)(up - lo) < (unsigned)(hi - lo);
+                const bool valid = (unsigned)(up - lo) < (unsigned)(hi - lo);
                 float r;
                 if (!ADJ) {
                     xq[ii] = __ldg(xr + QS * 32 * (ii + 8));
-                    const bool hasW = IN || up > lo;
-                    const bool hasE = IN || up < hi - 1;
+                    const bool hasW = up > lo;
+                    const bool hasE = up < hi - 1;
                     const float tw = hasW ? res_prev : own;
                     const float te = hasE ? ev : own;
                     const float tn = hasUp ? nv : own;
@@ -406,7 +397,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     } else {
                         r = leung_qian_fast(c_tt, tE, tW, tS, tN, lE, lW, lS, lN, own, dh_rcp, eps_adj);
                     }
-                    const bool keep = (!IN && !valid) || ((mword >> j) & 1u);
+                    const bool keep = !valid || ((mword >> j) & 1u);
                     r = keep ? own : r;
                     w_tt = c_tt;
                     c_tt = e_tt;
@@ -416,14 +407,11 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 if (EX) acc_l += valid ? fabsf(own - r) : 0.0f;
                 // lane 31 hands its row down; after the 8th value of a group it signals
                 const int upp = t - 31;
-                sts_if(hb_out + 4u * (uint32_t)(upp & (kHandoff - 1)), r, IN ? producer : (producer && upp >= 0 && upp < ncol));
+                sts_if(hb_out + 4u * (uint32_t)(upp & (kHandoff - 1)), r, producer && upp >= 0 && upp < ncol);
                 if (ii == 6) mbar_arrive_if(full_out + 8u * (((t - 38) >> 3) & (kGroups - 1)),
-                                            IN ? producer : (producer && t >= 38 && ((t - 38) >> 3) < ngrp));
+                                            producer && t >= 38 && ((t - 38) >> 3) < ngrp);
                 res_prev = r;
             }
-            };
-            if (full_strip && t0 >= lo + 32 && t0 + 9 <= hi_row) steps8(std::true_type{});
-            else steps8(std::false_type{});
         }
         // block k-1 is complete: write it back (each lane its own row)
         if (k >= 1) {
@@ -531,41 +519,95 @@ RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold,
 // is, hence so does the second, and so on through all four sweeps.  Such a
 // pass has zero change, so the stopping rule ends the loop after it; the
 // caller counts it without sweeping it, and every result stays the same.
+// Four consecutive cells of a row per lane (a warp covers 128 columns per
+// step) with their west and east neighbours: 16-byte loads, the neighbours
+// from the adjacent lanes.  Columns at or past the padded row end read as
+// `fill`; columns h0+i >= nx are the caller's to ignore.
+struct Row4 {
+    float w, v[4], e;
+};
+
+RZ_DEV Row4 row4(const float *row, int h0, int nxp, int l, float fill) {
+    Row4 r;
+    float4 c = make_float4(fill, fill, fill, fill);
+    if (h0 < nxp) c = __ldcg(reinterpret_cast<const float4 *>(row + h0));
+    r.v[0] = c.x, r.v[1] = c.y, r.v[2] = c.z, r.v[3] = c.w;
+    r.w = __shfl_up_sync(0xffffffffu, c.w, 1);
+    r.e = __shfl_down_sync(0xffffffffu, c.x, 1);
+    if (l == 0) r.w = h0 > 0 ? __ldcg(row + h0 - 1) : fill;
+    if (l == 31) r.e = h0 + 4 < nxp ? __ldcg(row + h0 + 4) : fill;
+    return r;
+}
+
 template <int MODE>
-RZ_DEV bool forward_is_fixpoint(const ShotParams &P, const float *T) {
-    const int nx = P.nx, ny = P.ny, nxp = P.nxp, n = nx * ny;
+__device__ __noinline__ bool forward_is_fixpoint(const ShotParams &P, const float *T, int *found) {
+    const int nx = P.nx, ny = P.ny, nxp = P.nxp;
+    const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
+    if (threadIdx.x == 0) *found = 0;
+    __syncthreads();
     bool change = false;
-    for (int c = threadIdx.x; c < n && !change; c += blockDim.x) {
-        const int k = c / nx, h = c - k * nx;
-        const float *p = T + (size_t)k * nxp + h;
-        const float own = __ldcg(p);
-        const float tw = h > 0 ? __ldcg(p - 1) : own, te = h < nx - 1 ? __ldcg(p + 1) : own;
-        const float tn = k > 0 ? __ldcg(p - nxp) : own, ts = k < ny - 1 ? __ldcg(p + nxp) : own;
-        const float a = fminf(tw, te), b = fminf(tn, ts), sv = __ldg(P.S + c);
-        const float tt = (MODE == kModeReference) ? godunov_ref(a, b, sv, P.dh) : godunov_fast(a, b, sv, P.dh);
-        change = tt < own;
+    for (int k = g; k < ny && !change; k += W) {
+        if (__shfl_sync(0xffffffffu, *(volatile int *)found, 0)) break;  // warp-uniform
+        const float *row = T + (size_t)k * nxp;
+        for (int base = 0; base < nx && !change; base += 128) {
+            const int h0 = base + 4 * l;
+            const Row4 c = row4(row, h0, nxp, l, 0.f);
+            const Row4 u = row4(k > 0 ? row - nxp : row, h0, nxp, l, 0.f);
+            const Row4 d = row4(k < ny - 1 ? row + nxp : row, h0, nxp, l, 0.f);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int h = h0 + i;
+                if (h >= nx) break;
+                const float own = c.v[i];
+                const float tw = h > 0 ? (i == 0 ? c.w : c.v[i - 1]) : own;
+                const float te = h < nx - 1 ? (i == 3 ? c.e : c.v[i + 1]) : own;
+                const float tn = k > 0 ? u.v[i] : own, ts = k < ny - 1 ? d.v[i] : own;
+                const float a = fminf(tw, te), b = fminf(tn, ts), sv = __ldg(P.S + (size_t)k * nx + h);
+                const float tt = (MODE == kModeReference) ? godunov_ref(a, b, sv, P.dh) : godunov_fast(a, b, sv, P.dh);
+                change |= tt < own;
+            }
+            change = __any_sync(0xffffffffu, change);
+        }
+        if (change && l == 0) *(volatile int *)found = 1;
     }
     return !__syncthreads_or(change);
 }
 
 // the Leung-Qian update of interior, non-receiver cells (sweep_adj.c:26-30)
 template <int MODE>
-RZ_DEV bool adjoint_is_fixpoint(const ShotParams &P, const float *T, const float *L) {
-    const int nx = P.nx, ny = P.ny, nxp = P.nxp, ni = nx - 2, n = ni * (ny - 2);
-    DivDH div{P.dh, P.dh_rcp, P.div_fast != 0};
+__device__ __noinline__ bool adjoint_is_fixpoint(const ShotParams &P, const float *T, const float *L, int *found) {
+    const int nx = P.nx, ny = P.ny, nxp = P.nxp;
+    const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
+    const DivDH div{P.dh, P.dh_rcp, P.div_fast != 0};
+    if (threadIdx.x == 0) *found = 0;
+    __syncthreads();
     bool change = false;
-    for (int c = threadIdx.x; c < n && !change; c += blockDim.x) {
-        const int k = 1 + c / ni, h = 1 + c - (k - 1) * ni;
-        if (P.skip[(size_t)k * nx + h]) continue;
-        const size_t o = (size_t)k * nxp + h;
-        const float own = __ldcg(L + o);
-        const float tc = __ldcg(T + o), te = __ldcg(T + o + 1), tw = __ldcg(T + o - 1);
-        const float ts = __ldcg(T + o + nxp), tn = __ldcg(T + o - nxp);
-        const float le = __ldcg(L + o + 1), lw = __ldcg(L + o - 1), ls = __ldcg(L + o + nxp), ln = __ldcg(L + o - nxp);
-        const float r = (MODE == kModeReference)
-                            ? leung_qian_ref(tc, te, tw, ts, tn, le, lw, ls, ln, own, div, P.eps_adj)
-                            : leung_qian_fast(tc, te, tw, ts, tn, le, lw, ls, ln, own, P.dh_rcp, P.eps_adj);
-        change = r != own;
+    for (int k = 1 + g; k < ny - 1 && !change; k += W) {
+        if (__shfl_sync(0xffffffffu, *(volatile int *)found, 0)) break;  // warp-uniform
+        const float *trow = T + (size_t)k * nxp, *lrow = L + (size_t)k * nxp;
+        for (int base = 0; base < nx && !change; base += 128) {
+            const int h0 = base + 4 * l;
+            const Row4 tc = row4(trow, h0, nxp, l, 0.f), lc = row4(lrow, h0, nxp, l, 0.f);
+            const Row4 tu = row4(trow - nxp, h0, nxp, l, 0.f), lu = row4(lrow - nxp, h0, nxp, l, 0.f);
+            const Row4 td = row4(trow + nxp, h0, nxp, l, 0.f), ld = row4(lrow + nxp, h0, nxp, l, 0.f);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) {
+                const int h = h0 + i;
+                if (h < 1 || h >= nx - 1) continue;
+                if (P.skip[(size_t)k * nx + h]) continue;
+                const float te = i == 3 ? tc.e : tc.v[i + 1], tw = i == 0 ? tc.w : tc.v[i - 1];
+                const float le = i == 3 ? lc.e : lc.v[i + 1], lw = i == 0 ? lc.w : lc.v[i - 1];
+                const float own = lc.v[i];
+                const float r = (MODE == kModeReference)
+                                    ? leung_qian_ref(tc.v[i], te, tw, td.v[i], tu.v[i], le, lw, ld.v[i], lu.v[i], own,
+                                                     div, P.eps_adj)
+                                    : leung_qian_fast(tc.v[i], te, tw, td.v[i], tu.v[i], le, lw, ld.v[i], lu.v[i], own,
+                                                      P.dh_rcp, P.eps_adj);
+                change |= r != own;
+            }
+            change = __any_sync(0xffffffffu, change);
+        }
+        if (change && l == 0) *(volatile int *)found = 1;
     }
     return !__syncthreads_or(change);
 }
@@ -633,7 +675,7 @@ __device__ __noinline__ void relayout_strip(const ShotParams &P, Warp &w, const 
 // the sweeps (x weights in TA/TB, z weights in WZA/WZB, those of the rows
 // bordering each strip in EU/ED), dJ/dT at the receiver cells (RA/RB, the
 // residuals of each cell's receivers summed in receiver order), mu = 0.
-RZ_DEV void exact_prepare(const ShotParams &P, int z, const float *T, float *L) {
+__device__ __noinline__ void exact_prepare(const ShotParams &P, int z, const float *T, float *L) {
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int l = tid & 31, g = tid >> 5, W = nthr >> 5;
     const int hs = P.src_h[z], ks = P.src_k[z];
@@ -798,7 +840,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
                 double tot = block_sum((double)acc, sh);
                 go = (tot / (double)n) >= (double)P.ttnorm;
             }
-            if (go && pass < P.max_passes && forward_is_fixpoint<MODE>(P, T)) {
+            if (go && pass < P.max_passes && forward_is_fixpoint<MODE>(P, T, &sh.ctl[2])) {
                 ++pass;  // the next pass would change nothing
                 go = false;
             }
@@ -963,7 +1005,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
             double tot = block_sum((double)acc, sh);
             go = (tot / (double)n) >= (double)P.ttnorm;
         }
-        if (go && !P.exact && P.skip && pass < P.max_passes && adjoint_is_fixpoint<MODE>(P, T, L)) {
+        if (go && !P.exact && P.skip && pass < P.max_passes && adjoint_is_fixpoint<MODE>(P, T, L, &sh.ctl[2])) {
             ++pass;  // the next pass would change nothing
             go = false;
         }
