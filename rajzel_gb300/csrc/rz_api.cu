@@ -54,6 +54,7 @@ struct rz_context {
     int *dRecH = nullptr, *dRecK = nullptr, *dRcH = nullptr, *dRcK = nullptr, *dRcRec = nullptr;
     int *dXcH = nullptr, *dXcK = nullptr, *dXcOff = nullptr, *dXcRec = nullptr;  // all receiver cells
     uint8_t *dSkip = nullptr;
+    uint8_t *dSkipP = nullptr;  // [ny][nxp]: frame, receiver and padding cells (adjoint fixpoint check)
     uint32_t *dMA = nullptr, *dMB = nullptr;
 
     // per-shot field slots (a batch larger than cap_f runs in chunks of cap_f shots)
@@ -309,7 +310,7 @@ static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     P.max_passes = c->g.max_passes > 0 ? c->g.max_passes : 10000;
     P.nshots = n;
     P.S = c->dS;
-    P.skip = c->dSkip;
+    P.skip = c->dSkipP;
     P.SA = c->dSA;
     P.SB = c->dSB;
     P.MA = c->dMA;
@@ -501,6 +502,7 @@ void rz_destroy(rz_context *c) {
     for (auto &pr : c->shot_events) cudaEventDestroy(pr.first), cudaEventDestroy(pr.second);
     dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dVp), dfree(c->dCube), dfree(c->dGrad), dfree(c->dL2);
     dfree(c->dRecH), dfree(c->dRecK), dfree(c->dRcH), dfree(c->dRcK), dfree(c->dRcRec), dfree(c->dSkip);
+    dfree(c->dSkipP);
     dfree(c->dMA), dfree(c->dMB), dfree(c->dGrad64);
     dfree(c->dXcH), dfree(c->dXcK), dfree(c->dXcOff), dfree(c->dXcRec);
     if (c->own) cudaStreamDestroy(c->own);
@@ -672,6 +674,14 @@ int rz_set_receivers(rz_context *c, int ntr, const int *recx, const int *recz) {
     }
     CK(cudaMemcpyAsync(c->dXcOff, xoff.data(), xoff.size() * sizeof(int), cudaMemcpyHostToDevice, c->st));
     CK(cudaMemcpyAsync(c->dSkip, skip.data(), skip.size(), cudaMemcpyHostToDevice, c->st));
+    {
+        std::vector<uint8_t> sp((size_t)ny * c->nxp, 1);
+        for (int k = 1; k < ny - 1; ++k)
+            for (int h = 1; h < nx - 1; ++h) sp[(size_t)k * c->nxp + h] = skip[(size_t)k * nx + h];
+        CK(dalloc(&c->dSkipP, sp.size()));
+        CK(cudaMemcpyAsync(c->dSkipP, sp.data(), sp.size(), cudaMemcpyHostToDevice, c->st));
+        CK(cudaStreamSynchronize(c->st));
+    }
     const size_t lines = (size_t)c->nstrips * c->qn;
     CK(dalloc(&c->dMA, lines));
     CK(dalloc(&c->dMB, lines));

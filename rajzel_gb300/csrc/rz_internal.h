@@ -58,7 +58,7 @@ struct ShotParams {
     int cotangent;          // exact: Tobs holds dJ/dTmod itself (vector-Jacobian product)
     // model (shared by all shots)
     const float *S;         // slowness [ny][nx]
-    const uint8_t *skip;    // receiver cell flags [ny][nx] (adjoint fixpoint check), or null
+    const uint8_t *skip;    // cells the adjoint leaves unchanged [ny][nxp] (frame, receivers, padding), or null
     const float *SA, *SB;   // skewed slowness
     const uint32_t *MA, *MB;  // skewed adjoint skip bits (frame | receiver | outside)
     // per-shot fields; shot z at offset z*fstride (floats)

@@ -519,94 +519,173 @@ RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold,
 // is, hence so does the second, and so on through all four sweeps.  Such a
 // pass has zero change, so the stopping rule ends the loop after it; the
 // caller counts it without sweeping it, and every result stays the same.
-// Four consecutive cells of a row per lane (a warp covers 128 columns per
-// step) with their west and east neighbours: 16-byte loads, the neighbours
-// from the adjacent lanes.  Columns at or past the padded row end read as
-// `fill`; columns h0+i >= nx are the caller's to ignore.
+// The checks split the grid into tasks of 128 columns x kCheckRows rows.  A
+// warp walks a task top to bottom, four cells per lane; the rows stream
+// through the warp's shared-memory ring by per-thread asynchronous copies
+// (cp.async, one group per row), several rows ahead of use.  Each lane
+// copies and reads back only its own 16 bytes per row (plus a one-column
+// halo for lanes 0 and 31); neighbours across lanes come by shuffle.
+constexpr int kCheckRows = 64;
+
+RZ_DEV void cp_async16(uint32_t dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+RZ_DEV void cp_async4(uint32_t dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+RZ_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+RZ_DEV void cp_async_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+RZ_DEV float4 lds4(uint32_t a) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+    return v;
+}
+RZ_DEV uint32_t lds_u32(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
+    return v;
+}
+
+// four cells of a row with their west and east neighbours
 struct Row4 {
     float w, v[4], e;
 };
 
-RZ_DEV Row4 row4(const float *row, int h0, int nxp, int l, float fill) {
+// own 16 bytes at slot + 16*l, halo of lanes 0 / 31 at hw / he
+RZ_DEV Row4 ring_row4(uint32_t slot, uint32_t hw, uint32_t he, int l) {
     Row4 r;
-    float4 c = make_float4(fill, fill, fill, fill);
-    if (h0 < nxp) c = __ldcg(reinterpret_cast<const float4 *>(row + h0));
+    const float4 c = lds4(slot + 16u * l);
     r.v[0] = c.x, r.v[1] = c.y, r.v[2] = c.z, r.v[3] = c.w;
     r.w = __shfl_up_sync(0xffffffffu, c.w, 1);
     r.e = __shfl_down_sync(0xffffffffu, c.x, 1);
-    if (l == 0) r.w = h0 > 0 ? __ldcg(row + h0 - 1) : fill;
-    if (l == 31) r.e = h0 + 4 < nxp ? __ldcg(row + h0 + 4) : fill;
+    if (l == 0) r.w = lds(hw);
+    if (l == 31) r.e = lds(he);
     return r;
 }
 
 template <int MODE>
-__device__ __noinline__ bool forward_is_fixpoint(const ShotParams &P, const float *T, int *found) {
+__device__ __noinline__ bool forward_is_fixpoint(const ShotParams &P, const float *T, uint32_t ring_s, int *found) {
+    // slot: T [0,512), S [512,1024), T halo west/east [1024,1032)
+    constexpr int RS = 12, SLOT = 1040;
+    static_assert(RS * SLOT <= (int)sizeof(float) * kRing * kSlotFloats, "check ring exceeds the warp's ring");
     const int nx = P.nx, ny = P.ny, nxp = P.nxp;
     const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
+    const int nch = (nx + 127) >> 7, nrb = (ny + kCheckRows - 1) / kCheckRows;
     if (threadIdx.x == 0) *found = 0;
     __syncthreads();
     bool change = false;
-    for (int k = g; k < ny && !change; k += W) {
+    for (int task = g; task < nch * nrb && !change; task += W) {
         if (__shfl_sync(0xffffffffu, *(volatile int *)found, 0)) break;  // warp-uniform
-        const float *row = T + (size_t)k * nxp;
-        for (int base = 0; base < nx && !change; base += 128) {
-            const int h0 = base + 4 * l;
-            const Row4 c = row4(row, h0, nxp, l, 0.f);
-            const Row4 u = row4(k > 0 ? row - nxp : row, h0, nxp, l, 0.f);
-            const Row4 d = row4(k < ny - 1 ? row + nxp : row, h0, nxp, l, 0.f);
+        const int h0 = ((task % nch) << 7) + 4 * l;
+        const int k0 = (task / nch) * kCheckRows, k1 = min(ny, k0 + kCheckRows);
+        auto slot = [&](int k) { return ring_s + (uint32_t)(((k - k0 + 1) % RS) * SLOT); };
+        auto issue = [&](int k) {  // rows k0-1 .. k1 are read; later ones commit empty groups
+            if (k <= k1) {
+                const int kk = min(max(k, 0), ny - 1);
+                const uint32_t sl = slot(k);
+                const float *tr = T + (size_t)kk * nxp;
+                if (h0 < nxp) cp_async16(sl + 16u * l, tr + h0);
+#pragma unroll
+                for (int i = 0; i < 4; ++i)
+                    if (h0 + i < nx) cp_async4(sl + 512u + 16u * l + 4u * i, P.S + (size_t)kk * nx + h0 + i);
+                if (l == 0 && h0 > 0) cp_async4(sl + 1024u, tr + h0 - 1);
+                if (l == 31 && h0 + 4 < nxp) cp_async4(sl + 1028u, tr + h0 + 4);
+            }
+            cp_async_commit();
+        };
+        for (int i = 0; i < RS; ++i) issue(k0 - 1 + i);
+        for (int k = k0; k < k1; ++k) {
+            cp_async_wait<RS - 3>();  // rows up to k+1 have landed
+            const uint32_t sc = slot(k);
+            const Row4 c = ring_row4(sc, sc + 1024u, sc + 1028u, l);
+            const float4 u = lds4(slot(k - 1) + 16u * l), d = lds4(slot(k + 1) + 16u * l);
+            const float4 sv4 = lds4(sc + 512u + 16u * l);
+            const float uv[4] = {u.x, u.y, u.z, u.w}, dv[4] = {d.x, d.y, d.z, d.w};
+            const float sv[4] = {sv4.x, sv4.y, sv4.z, sv4.w};
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
                 const int h = h0 + i;
-                if (h >= nx) break;
                 const float own = c.v[i];
                 const float tw = h > 0 ? (i == 0 ? c.w : c.v[i - 1]) : own;
                 const float te = h < nx - 1 ? (i == 3 ? c.e : c.v[i + 1]) : own;
-                const float tn = k > 0 ? u.v[i] : own, ts = k < ny - 1 ? d.v[i] : own;
-                const float a = fminf(tw, te), b = fminf(tn, ts), sv = __ldg(P.S + (size_t)k * nx + h);
-                const float tt = (MODE == kModeReference) ? godunov_ref(a, b, sv, P.dh) : godunov_fast(a, b, sv, P.dh);
-                change |= tt < own;
+                const float tn = k > 0 ? uv[i] : own, ts = k < ny - 1 ? dv[i] : own;
+                const float a = fminf(tw, te), b = fminf(tn, ts);
+                const float tt = (MODE == kModeReference) ? godunov_ref(a, b, sv[i], P.dh) : godunov_fast(a, b, sv[i], P.dh);
+                change |= (h < nx) && (tt < own);
             }
-            change = __any_sync(0xffffffffu, change);
+            issue(k - 1 + RS);  // into the slot of row k-1, no longer read
         }
+        cp_async_wait<0>();
+        change = __any_sync(0xffffffffu, change);
         if (change && l == 0) *(volatile int *)found = 1;
     }
     return !__syncthreads_or(change);
 }
 
-// the Leung-Qian update of interior, non-receiver cells (sweep_adj.c:26-30)
+// the Leung-Qian update of interior, non-receiver cells (sweep_adj.c:26-30);
+// skip is the [ny][nxp] byte map of cells the adjoint sweeps leave unchanged
 template <int MODE>
-__device__ __noinline__ bool adjoint_is_fixpoint(const ShotParams &P, const float *T, const float *L, int *found) {
+__device__ __noinline__ bool adjoint_is_fixpoint(const ShotParams &P, const float *T, const float *L, uint32_t ring_s,
+                                                 int *found) {
+    // slot: T [0,512), lambda [512,1024), skip [1024,1152), T halo [1152,1160), lambda halo [1160,1168)
+    constexpr int RS = 10, SLOT = 1168;
+    static_assert(RS * SLOT <= (int)sizeof(float) * kRing * kSlotFloats, "check ring exceeds the warp's ring");
     const int nx = P.nx, ny = P.ny, nxp = P.nxp;
     const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
+    const int nch = (nx + 127) >> 7, nrb = (ny - 2 + kCheckRows - 1) / kCheckRows;
     const DivDH div{P.dh, P.dh_rcp, P.div_fast != 0};
     if (threadIdx.x == 0) *found = 0;
     __syncthreads();
     bool change = false;
-    for (int k = 1 + g; k < ny - 1 && !change; k += W) {
+    for (int task = g; task < nch * nrb && !change; task += W) {
         if (__shfl_sync(0xffffffffu, *(volatile int *)found, 0)) break;  // warp-uniform
-        const float *trow = T + (size_t)k * nxp, *lrow = L + (size_t)k * nxp;
-        for (int base = 0; base < nx && !change; base += 128) {
-            const int h0 = base + 4 * l;
-            const Row4 tc = row4(trow, h0, nxp, l, 0.f), lc = row4(lrow, h0, nxp, l, 0.f);
-            const Row4 tu = row4(trow - nxp, h0, nxp, l, 0.f), lu = row4(lrow - nxp, h0, nxp, l, 0.f);
-            const Row4 td = row4(trow + nxp, h0, nxp, l, 0.f), ld = row4(lrow + nxp, h0, nxp, l, 0.f);
+        const int h0 = ((task % nch) << 7) + 4 * l;
+        const int k0 = 1 + (task / nch) * kCheckRows, k1 = min(ny - 1, k0 + kCheckRows);
+        auto slot = [&](int k) { return ring_s + (uint32_t)(((k - k0 + 1) % RS) * SLOT); };
+        auto issue = [&](int k) {
+            if (k <= k1) {
+                const uint32_t sl = slot(k);
+                const size_t o = (size_t)k * nxp;
+                if (h0 < nxp) {
+                    cp_async16(sl + 16u * l, T + o + h0);
+                    cp_async16(sl + 512u + 16u * l, L + o + h0);
+                    cp_async4(sl + 1024u + 4u * l, P.skip + o + h0);
+                }
+                if (l == 0 && h0 > 0) cp_async4(sl + 1152u, T + o + h0 - 1), cp_async4(sl + 1160u, L + o + h0 - 1);
+                if (l == 31 && h0 + 4 < nxp) cp_async4(sl + 1156u, T + o + h0 + 4), cp_async4(sl + 1164u, L + o + h0 + 4);
+            }
+            cp_async_commit();
+        };
+        for (int i = 0; i < RS; ++i) issue(k0 - 1 + i);
+        for (int k = k0; k < k1; ++k) {
+            cp_async_wait<RS - 3>();
+            const uint32_t sc = slot(k), su = slot(k - 1), sd = slot(k + 1);
+            const Row4 tc = ring_row4(sc, sc + 1152u, sc + 1156u, l);
+            const Row4 lc = ring_row4(sc + 512u, sc + 1160u, sc + 1164u, l);
+            const float4 tu = lds4(su + 16u * l), td = lds4(sd + 16u * l);
+            const float4 lu = lds4(su + 512u + 16u * l), ld = lds4(sd + 512u + 16u * l);
+            const uint32_t sk = h0 < nxp ? lds_u32(sc + 1024u + 4u * l) : 0x01010101u;
+            const float tuv[4] = {tu.x, tu.y, tu.z, tu.w}, tdv[4] = {td.x, td.y, td.z, td.w};
+            const float luv[4] = {lu.x, lu.y, lu.z, lu.w}, ldv[4] = {ld.x, ld.y, ld.z, ld.w};
 #pragma unroll
             for (int i = 0; i < 4; ++i) {
-                const int h = h0 + i;
-                if (h < 1 || h >= nx - 1) continue;
-                if (P.skip[(size_t)k * nx + h]) continue;
                 const float te = i == 3 ? tc.e : tc.v[i + 1], tw = i == 0 ? tc.w : tc.v[i - 1];
                 const float le = i == 3 ? lc.e : lc.v[i + 1], lw = i == 0 ? lc.w : lc.v[i - 1];
                 const float own = lc.v[i];
                 const float r = (MODE == kModeReference)
-                                    ? leung_qian_ref(tc.v[i], te, tw, td.v[i], tu.v[i], le, lw, ld.v[i], lu.v[i], own,
-                                                     div, P.eps_adj)
-                                    : leung_qian_fast(tc.v[i], te, tw, td.v[i], tu.v[i], le, lw, ld.v[i], lu.v[i], own,
+                                    ? leung_qian_ref(tc.v[i], te, tw, tdv[i], tuv[i], le, lw, ldv[i], luv[i], own, div,
+                                                     P.eps_adj)
+                                    : leung_qian_fast(tc.v[i], te, tw, tdv[i], tuv[i], le, lw, ldv[i], luv[i], own,
                                                       P.dh_rcp, P.eps_adj);
-                change |= r != own;
+                change |= (((sk >> (8 * i)) & 0xffu) == 0) && (r != own);
             }
-            change = __any_sync(0xffffffffu, change);
+            issue(k - 1 + RS);
         }
+        cp_async_wait<0>();
+        change = __any_sync(0xffffffffu, change);
         if (change && l == 0) *(volatile int *)found = 1;
     }
     return !__syncthreads_or(change);
@@ -840,7 +919,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
                 double tot = block_sum((double)acc, sh);
                 go = (tot / (double)n) >= (double)P.ttnorm;
             }
-            if (go && pass < P.max_passes && forward_is_fixpoint<MODE>(P, T, &sh.ctl[2])) {
+            if (go && pass < P.max_passes && forward_is_fixpoint<MODE>(P, T, smem_u32(&sh.w[g].ring[0][0]), &sh.ctl[2])) {
                 ++pass;  // the next pass would change nothing
                 go = false;
             }
@@ -1005,7 +1084,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
             double tot = block_sum((double)acc, sh);
             go = (tot / (double)n) >= (double)P.ttnorm;
         }
-        if (go && !P.exact && P.skip && pass < P.max_passes && adjoint_is_fixpoint<MODE>(P, T, L, &sh.ctl[2])) {
+        if (go && !P.exact && P.skip && pass < P.max_passes && adjoint_is_fixpoint<MODE>(P, T, L, smem_u32(&sh.w[g].ring[0][0]), &sh.ctl[2])) {
             ++pass;  // the next pass would change nothing
             go = false;
         }
