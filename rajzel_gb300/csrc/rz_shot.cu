@@ -41,6 +41,7 @@ struct CtaShared {
     uint64_t *mbar;  // [W][kRing]
     double *red;     // [W] reduction scratch
     int *ctl;        // [8] broadcast words
+    int *done;       // [W] sweeps each warp has completed (pipelined sweeps)
 };
 
 __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -49,7 +50,7 @@ size_t shot_kernel_smem(int W) {
     size_t o = sizeof(WarpShared) * W;
     o = align_up(o, 8) + sizeof(uint64_t) * kRing * W;
     o = align_up(o, 8) + sizeof(double) * W;
-    o += sizeof(int) * 8;
+    o += sizeof(int) * 8 + sizeof(int) * W;
     return align_up(o, 128);
 }
 
@@ -58,8 +59,28 @@ struct Warp {
     uint32_t phase;  // expected parity per ring slot
     int err;
     WarpShared *ws, *ws_down;
+    WarpShared *ws_all;  // every warp's shared block (pipelined sweeps)
+    int *done;           // every warp's completed-sweep counter (pipelined sweeps)
     uint64_t *mbar;
     volatile int *abort_word;  // CTA-wide: a bounded wait gave up
+};
+
+// Sweep sequencing.  Banded (default): warp g takes the g-th strip of the
+// band in sweep order and the CTA synchronises after every sweep.
+// Pipelined (one band): warp g keeps strip g in every sweep, so for dy < 0
+// its upstream neighbour is warp g+1; a warp starts its next sweep as soon as
+// the strip it reads its halo row from has finished the current one, and
+// hand-off groups are numbered across sweeps (no barrier re-arming), so the
+// wavefront never drains between the four sweeps of a pass.
+struct SweepSeq {
+    int pipelined;
+    int n;           // sweeps this warp has run in this launch
+    int npos, nneg;  // of which with dy > 0 / dy < 0
+    RZ_DEV void advance(int dy) {
+        ++n;
+        if (dy > 0) ++npos;
+        else ++nneg;
+    }
 };
 
 RZ_DEV int mod3(int v) { return v - 3 * (v / 3); }
@@ -106,13 +127,14 @@ constexpr int kRowBytes = kRowFloats * 4;         // 384
 
 template <int DX, int DY, bool ADJ, int MODE>
 __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mrow, float &acc, float &mag,
-                                   int band, int W) {
+                                   int band, int W, const SweepSeq &seq) {
     // exact discrete adjoint: mu = R + sum of the weights neighbours put on this cell
     constexpr bool EX = ADJ && (MODE == kModeExact);
     const int l = w.l, g = w.g;
+    const bool pipe = seq.pipelined != 0;
     // strips are swept in bands of W (one strip per warp); sig is the strip's
     // position in sweep order, s its index from the top of the grid
-    const int sig = band * W + g;
+    const int sig = pipe ? (DY > 0 ? g : P.nstrips - 1 - g) : band * W + g;
     if (sig >= P.nstrips) return;
     const int z = w.z;
     const int s = DY > 0 ? sig : P.nstrips - 1 - sig;
@@ -125,8 +147,25 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const bool hasUp = DY > 0 ? (row > 0) : (row < P.ny - 1);
     const bool hasDn = DY > 0 ? (row < P.ny - 1) : (row > 0);
     const int nxb = P.nxb, ncol = kBlk * nxb, nx = P.nx;
-    const bool is_producer_warp = (g + 1 < W) && (sig + 1 < P.nstrips);
-    const bool is_consumer_warp = (g > 0);
+    const bool is_producer_warp = pipe ? (sig + 1 < P.nstrips) : (g + 1 < W) && (sig + 1 < P.nstrips);
+    const bool is_consumer_warp = pipe ? (sig > 0) : (g > 0);
+    // the warp whose strip follows in sweep order, and the hand-off groups
+    // already delivered into its ring and into ours (pipelined numbering)
+    WarpShared *const down = !is_producer_warp ? w.ws : pipe ? w.ws_all + (DY > 0 ? g + 1 : g - 1) : w.ws_down;
+    auto delivered = [&](int strip) {  // ring of a strip receives in dy>0 sweeps unless first, dy<0 unless last
+        return (strip > 0 ? seq.npos : 0) + (strip < P.nstrips - 1 ? seq.nneg : 0);
+    };
+    const int ngrp0 = (kBlk * P.nxb) >> 3;
+    const int cons_base = pipe ? ngrp0 * delivered(s) : 0;
+    const int prod_base = pipe && is_producer_warp ? ngrp0 * delivered(DY > 0 ? s + 1 : s - 1) : 0;
+    const int cb8 = 8 * cons_base, pb8 = 8 * prod_base;
+    if (pipe && is_producer_warp) {
+        // the halo row belongs to the next strip in sweep order: it must hold
+        // that strip's values after the previous sweep
+        if (l == 0 && !wait_flag_ge(w.done + (DY > 0 ? g + 1 : g - 1), seq.n, w.abort_word)) w.err |= ERR_FLAG_TIMEOUT;
+        __syncwarp();
+        fence_proxy_async_global();
+    }
     // the first warp of a later band reads its upstream row (final for this
     // sweep: the previous band is complete) from global memory
     const bool reads_prev_band = (g == 0) && (band > 0);
@@ -143,7 +182,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const uint32_t row_end = row_s + kRowBytes;
     const int hoff = (halorow - boxrow) * kRowBytes;
     const uint32_t hb_in = smem_u32(w.ws->hb);
-    const uint32_t hb_out = smem_u32(is_producer_warp ? w.ws_down->hb : w.ws->hb);
+    const uint32_t hb_out = smem_u32(down->hb);
     const float dh = P.dh;
     const float dh_rcp = P.dh_rcp, eps_adj = P.eps_adj;
     const bool div_fast = P.div_fast != 0;
@@ -155,8 +194,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const uint32_t abort_s = smem_u32((const void *)w.abort_word);
     const uint32_t mbar_s = smem_u32(w.mbar);
     const uint32_t full_in = smem_u32(w.ws->full), empty_in = smem_u32(w.ws->empty);
-    const uint32_t full_out = smem_u32(is_producer_warp ? w.ws_down->full : w.ws->full);
-    const uint32_t empty_out = smem_u32(is_producer_warp ? w.ws_down->empty : w.ws->empty);
+    const uint32_t full_out = smem_u32(down->full);
+    const uint32_t empty_out = smem_u32(down->empty);
     uint32_t phase = w.phase;
     int err = 0;
     float acc_l = 0.f;  // fast-mode sum of |change| (the caller's acc lives in local memory)
@@ -276,12 +315,13 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
             if (is_consumer_warp) {
                 const int G = t0 >> 3;
                 if (G < ngrp) {
-                    if (!mbar_wait_a(full_in + 8u * (G & (kGroups - 1)), (G >> 4) & 1, abort_s)) err |= ERR_FLAG_TIMEOUT;
-                    const uint32_t hb_g = hb_in + 4u * (uint32_t)(t0 & (kHandoff - 1));
+                    const int Gg = G + cons_base;  // group number in this ring's lifetime
+                    if (!mbar_wait_a(full_in + 8u * (Gg & (kGroups - 1)), (Gg >> 4) & 1, abort_s)) err |= ERR_FLAG_TIMEOUT;
+                    const uint32_t hb_g = hb_in + 4u * (uint32_t)((t0 + cb8) & (kHandoff - 1));
 #pragma unroll
-                    for (int q = 0; q < 8; ++q) hbq[q] = lds(hb_g + 4u * q);
+                    for (int i = 0; i < 8; ++i) hbq[i] = lds(hb_g + 4u * i);
                     // the values are in registers: release the slot at once
-                    mbar_arrive_if(empty_in + 8u * (G & (kGroups - 1)), l == 0);
+                    mbar_arrive_if(empty_in + 8u * (Gg & (kGroups - 1)), l == 0);
                 } else {
 #pragma unroll
                     for (int q = 0; q < 8; ++q) hbq[q] = 0.f;
@@ -300,9 +340,9 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
             }
             if (is_producer_warp) {
                 // lane 31 starts hand-off group Gp at step t0+7 (column t0-24)
-                const int Gp = (t0 - 24) >> 3;
-                if (t0 >= 24 && Gp >= kGroups && Gp < ngrp &&
-                    !mbar_wait_a(empty_out + 8u * (Gp & (kGroups - 1)), ((Gp >> 4) - 1) & 1, abort_s))
+                const int Gp = (t0 - 24) >> 3, Gpg = Gp + prod_base;
+                if (t0 >= 24 && Gpg >= kGroups && Gp < ngrp &&
+                    !mbar_wait_a(empty_out + 8u * (Gpg & (kGroups - 1)), ((Gpg >> 4) - 1) & 1, abort_s))
                     err |= ERR_FLAG_TIMEOUT;
             }
             const int u0 = t0 - l;
@@ -407,8 +447,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 if (EX) acc_l += valid ? fabsf(own - r) : 0.0f;
                 // lane 31 hands its row down; after the 8th value of a group it signals
                 const int upp = t - 31;
-                sts_if(hb_out + 4u * (uint32_t)(upp & (kHandoff - 1)), r, producer && upp >= 0 && upp < ncol);
-                if (ii == 6) mbar_arrive_if(full_out + 8u * (((t - 38) >> 3) & (kGroups - 1)),
+                sts_if(hb_out + 4u * (uint32_t)((upp + pb8) & (kHandoff - 1)), r, producer && upp >= 0 && upp < ncol);
+                if (ii == 6) mbar_arrive_if(full_out + 8u * (((t - 38 + pb8) >> 3) & (kGroups - 1)),
                                             producer && t >= 38 && ((t - 38) >> 3) < ngrp);
                 res_prev = r;
             }
@@ -424,6 +464,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     tma_store_wait_all<0>();
     fence_proxy_async_global();
     __syncwarp();
+    if (pipe && l == 0) st_release_smem(w.done + g, seq.n + 1);
     w.phase = phase;
     w.err |= err;
     acc += acc_l;
@@ -840,12 +881,14 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
         sh.red = reinterpret_cast<double *>(smem_raw + o);
         o += sizeof(double) * W;
         sh.ctl = reinterpret_cast<int *>(smem_raw + o);
+        sh.done = sh.ctl + 8;
     }
     if (l == 0) {
         for (int i = 0; i < kRing; ++i) mbar_init(&sh.mbar[g * kRing + i], 1);
     }
     handoff_init(&sh.w[g], false);
     if (tid < 8) sh.ctl[tid] = 0;
+    if (tid < W) sh.done[tid] = 0;
     if (tid == 0) tma_prefetch_desc(&mTld), tma_prefetch_desc(&mTrow), tma_prefetch_desc(&mLrow);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     __syncthreads();
@@ -858,6 +901,8 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
     w.err = 0;
     w.ws = &sh.w[g];
     w.ws_down = (g + 1 < W) ? &sh.w[g + 1] : nullptr;
+    w.ws_all = sh.w;
+    w.done = sh.done;
     w.mbar = &sh.mbar[g * kRing];
     w.abort_word = &sh.ctl[1];
 
@@ -868,6 +913,17 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
     const int n = P.nx * P.ny;
     const int nbands = (P.nstrips + W - 1) / W;
     int cta_err = 0;
+    SweepSeq seq{nbands == 1 ? 1 : 0, 0, 0, 0};
+    // one directional sweep of every band; banded sweeps synchronise the CTA
+    // after each band, pipelined ones only at the end of a pass
+#define RZ_SWEEP(DX_, DY_, ADJ_, MODE_, MAP_)                                   \
+    do {                                                                       \
+        for (int b = 0; b < nbands; ++b) {                                     \
+            sweep<DX_, DY_, ADJ_, MODE_>(P, w, MAP_, acc, mag, b, W, seq);     \
+            if (!seq.pipelined) sweep_barrier(sh);                             \
+        }                                                                      \
+        seq.advance(DY_);                                                      \
+    } while (0)
 
     if (!P.start_adjoint) {
         // ---------------- forward ----------------
@@ -893,23 +949,12 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
                 __syncthreads();
             }
             float acc = 0.f, mag = 0.f;
-            for (int b = 0; b < nbands; ++b) {
-                sweep<+1, +1, false, MODE>(P, w, &mTrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
+            RZ_SWEEP(+1, +1, false, MODE, &mTrow);
             if (pass == 0) stamp(P, z, 5);
-            for (int b = 0; b < nbands; ++b) {
-                sweep<-1, +1, false, MODE>(P, w, &mTrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
-            for (int b = 0; b < nbands; ++b) {
-                sweep<-1, -1, false, MODE>(P, w, &mTrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
-            for (int b = 0; b < nbands; ++b) {
-                sweep<+1, -1, false, MODE>(P, w, &mTrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
+            RZ_SWEEP(-1, +1, false, MODE, &mTrow);
+            RZ_SWEEP(-1, -1, false, MODE, &mTrow);
+            RZ_SWEEP(+1, -1, false, MODE, &mTrow);
+            if (seq.pipelined) __syncthreads();
             ++pass;
             ++swept;
             if (*w.abort_word) break;
@@ -1032,42 +1077,19 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
         float acc = 0.f, mag = 0.f;
         if (P.exact) {
             // same four orderings as the Leung-Qian sweeps (eikonal_adj.c:43-46)
-            for (int b = 0; b < nbands; ++b) {
-                sweep<+1, +1, true, kModeExact>(P, w, &mLrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
+            RZ_SWEEP(+1, +1, true, kModeExact, &mLrow);
             if (pass == 0) stamp(P, z, 6);
-            for (int b = 0; b < nbands; ++b) {
-                sweep<+1, -1, true, kModeExact>(P, w, &mLrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
-            for (int b = 0; b < nbands; ++b) {
-                sweep<-1, +1, true, kModeExact>(P, w, &mLrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
-            for (int b = 0; b < nbands; ++b) {
-                sweep<-1, -1, true, kModeExact>(P, w, &mLrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
+            RZ_SWEEP(+1, -1, true, kModeExact, &mLrow);
+            RZ_SWEEP(-1, +1, true, kModeExact, &mLrow);
+            RZ_SWEEP(-1, -1, true, kModeExact, &mLrow);
         } else {
-            for (int b = 0; b < nbands; ++b) {
-                sweep<+1, +1, true, MODE>(P, w, &mLrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
+            RZ_SWEEP(+1, +1, true, MODE, &mLrow);
             if (pass == 0) stamp(P, z, 6);
-            for (int b = 0; b < nbands; ++b) {
-                sweep<+1, -1, true, MODE>(P, w, &mLrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
-            for (int b = 0; b < nbands; ++b) {
-                sweep<-1, +1, true, MODE>(P, w, &mLrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
-            for (int b = 0; b < nbands; ++b) {
-                sweep<-1, -1, true, MODE>(P, w, &mLrow, acc, mag, b, W);
-                sweep_barrier(sh);
-            }
+            RZ_SWEEP(+1, -1, true, MODE, &mLrow);
+            RZ_SWEEP(-1, +1, true, MODE, &mLrow);
+            RZ_SWEEP(-1, -1, true, MODE, &mLrow);
         }
+        if (seq.pipelined) __syncthreads();
         ++pass;
         ++swept;
         if (*w.abort_word) break;
@@ -1090,6 +1112,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
         }
     }
     if (tid == 0) P.passes_adj[z] = pass;
+#undef RZ_SWEEP
     if (tid == 0 && P.swept) P.swept[2 * z + 1] = swept;
     stamp(P, z, 4);
     __syncthreads();
