@@ -47,13 +47,26 @@ def log(*a):
 # ---------------------------------------------------------------------------
 # host CPU: the reference algorithm on all host cores
 # ---------------------------------------------------------------------------
+def _workload(name, nshots):
+    from rajzel_gb300 import synth
+    if name == "grad_1700x350":
+        return synth.grad_1700x350(nshots=nshots)
+    if name == "fatt":
+        return synth.fatt_2000x500(nshots=nshots)
+    if name == "stress":
+        return synth.stress_8192x2048(nshots=nshots)
+    if name.startswith("uneven"):
+        return synth.uneven_grid(int(name[-1]))
+    raise KeyError(name)
+
+
 def _cpu_worker(args):
     """One worker process = one MPI rank of the reference: grad_obj over its shots."""
-    kind, shots, nshots_total, seed = args
+    kind, shots, nshots_total, wname = args
     import numpy as np
     import oracle as O
     from rajzel_gb300 import synth
-    w = synth.grad_1700x350(nshots=nshots_total)
+    w = _workload(wname, nshots_total)
     p = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
     Sobs = synth.slowness(w.vp_true)
     S = synth.slowness(w.vp_start)
@@ -74,14 +87,14 @@ def _cpu_worker(args):
     return time.perf_counter() - t0
 
 
-def cpu_run(nshots_sample, cores, kind):
+def cpu_run(nshots_sample, cores, kind, wname="grad_1700x350", nshots_total=100):
     """Time grad_obj over `nshots_sample` shots split across `cores` processes
     exactly as init_MPIshot splits shots over ranks; returns wall seconds."""
     import multiprocessing as mp
     import oracle as O
     O.build(ref=(kind == "reference"))
     spans = [O.shot_partition(nshots_sample, cores, r) for r in range(cores)]
-    jobs = [(kind, list(range(a - 1, b - 1)), 100, 0) for a, b in spans]
+    jobs = [(kind, list(range(a - 1, b - 1)), nshots_total, wname) for a, b in spans]
     ctx = mp.get_context("spawn")
     with ctx.Pool(cores) as pool:
         times = pool.map(_cpu_worker, jobs)
@@ -362,7 +375,8 @@ def torch_device_index():
 def run_workload(args, local_rank):
     """fwd_500x174: one forward solve (latency); uneven: 256 shots over three
     grids, forward + adjoint gradient; stress: 1024 shots on 8192 x 2048
-    under a 120 GB cap on the field slots."""
+    under a 120 GB cap on the field slots; fatt: 30 l-BFGS iterations, 200
+    shots x 1000 receivers on 2000 x 500."""
     import numpy as np
     import torch
     import rajzel_gb300 as R
@@ -405,10 +419,8 @@ def run_workload(args, local_rank):
         for w in grids:
             st = torch.cuda.Stream()
             ctx = _context(R, w, args.mode, st, w.vp_true)
-            Tobs = np.empty((w.nshots, w.ntr), np.float32)
-            ctx.set_velocity(w.vp_true * np.float32(1.03))
             _, Tobs, _ = ctx.forward(w.srcx, w.srcz, want_tt=False)
-            ctx.set_velocity(w.vp_true)
+            ctx.set_velocity(w.vp_start)
             bufs.append((torch.from_numpy(np.ascontiguousarray(Tobs)).cuda(),
                          torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda"),
                          torch.empty(1, dtype=torch.float64, device="cuda")))
@@ -434,12 +446,19 @@ def run_workload(args, local_rank):
         per_grid = []
         for i, w in enumerate(grids):
             ms_i = _events_ms(lambda: launch(i), streams[i], max(1, args.steps // 2))
-            pf = sum(ctxs[i].shot_info(s)[0] for s in range(w.nshots))
-            pa = sum(ctxs[i].shot_info(s)[1] for s in range(w.nshots))
+            sw = np.array([ctxs[i].shot_work(s) for s in range(w.nshots)]).sum(axis=0)
             per_grid.append({"grid": [w.nx, w.ny], "shots": w.nshots, "ms": ms_i,
-                             "point_updates": 4 * (pf * w.nx * w.ny + pa * (w.nx - 2) * (w.ny - 2))})
+                             "passes_swept_fwd_adj": [int(sw[0]), int(sw[1])],
+                             "point_updates": 4 * (int(sw[0]) * w.nx * w.ny + int(sw[1]) * (w.nx - 2) * (w.ny - 2))})
         nsh = sum(w.nshots for w in grids)
         pu = sum(g["point_updates"] for g in per_grid)
+        cores = os.cpu_count() or 1
+        kind = cpu_kind()
+        cpu_s = 0.0
+        for i, w in enumerate(grids):  # one shot per core of each grid, scaled to the grid's shots
+            cpu_s += cpu_run(cores, cores, kind, f"uneven{i}", w.nshots) * w.nshots / cores
+        out["cpu_baseline"] = {"value": nsh / cpu_s, "unit": "shots/s", "cores": cores, "kind": kind,
+                               "sample": "grad_obj of one shot per core on each grid, scaled to 86/85/85 shots"}
         out.update({"metric": "fwd+adjoint shots/s", "value": nsh / (conc_ms / 1e3), "unit": "shots/s",
                     "higher_is_better": True, "ms_per_step": conc_ms, "shots": nsh,
                     "point_updates_per_s": pu / (conc_ms / 1e3), "per_grid": per_grid,
@@ -453,20 +472,60 @@ def run_workload(args, local_rank):
         ctx.forward_device(w.srcx, w.srcz, 0, to.data_ptr())
         torch.cuda.synchronize()
         fwd_s = time.perf_counter() - t0
-        vstart = np.where(w.vp_true == 4500.0, np.float32(3500.0), w.vp_true).astype(np.float32)
-        ctx.set_velocity(vstart)
+        ctx.set_velocity(w.vp_start)
         g = torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda")
         l2 = torch.empty(1, dtype=torch.float64, device="cuda")
         step = lambda: ctx.grad_obj_device(w.srcx, w.srcz, to.data_ptr(), g.data_ptr(), l2.data_ptr())  # noqa
         ms = _events_ms(step, stream, max(1, args.steps))
         pf = sum(ctx.shot_info(s)[0] for s in range(w.nshots))
         pa = sum(ctx.shot_info(s)[1] for s in range(w.nshots))
-        pu = 4 * (pf * w.nx * w.ny + pa * (w.nx - 2) * (w.ny - 2))
+        sw = np.array([ctx.shot_work(s) for s in range(w.nshots)]).sum(axis=0)
+        pu = 4 * (int(sw[0]) * w.nx * w.ny + int(sw[1]) * (w.nx - 2) * (w.ny - 2))  # swept passes only
+        cores = os.cpu_count() or 1
+        kind = cpu_kind()
+        cpu_s = cpu_run(cores, cores, kind, "stress", w.nshots)
+        out["cpu_baseline"] = {"value": cores / cpu_s, "unit": "shots/s", "cores": cores, "kind": kind,
+                               "sample": "grad_obj of one shot per core (the first shots of the 1024)"}
         out.update({"metric": "fwd+adjoint shots/s", "value": w.nshots / (ms / 1e3), "unit": "shots/s",
                     "higher_is_better": True, "ms_per_step": ms, "shots": w.nshots,
-                    "forward_only_s": fwd_s, "passes_fwd_adj": [pf, pa],
+                    "forward_only_s": fwd_s, "passes_fwd_adj": [pf, pa], "passes_swept_fwd_adj": [int(sw[0]), int(sw[1])],
                     "point_updates_per_s": pu / (ms / 1e3), "memory_cap_bytes": 120 << 30,
                     "peak_allocated_note": "field slots sized to the cap, chunks of a multiple of the SM count"})
+    elif args.workload == "fatt":
+        w = synth.fatt_2000x500(nshots=args.shots if args.shots != 100 else 200)
+        ctx = _context(R, w, args.mode, stream, w.vp_true)
+        _, Tobs, _ = ctx.forward(w.srcx, w.srcz, want_tt=False)  # observed picks from the true model
+        # the reference's example workflow: Gaussian-filtered gradients (SPATFILTER 4,
+        # 80 x 40 points) and the horizontal taper of its parameter file
+        opts = dict(itermax=30, nlbfgs=5, stepmax=10, vp_lo=1000.0, vp_hi=6000.0, recursion=1, spatfilter=4,
+                    filt_size_grad=80, filt_size_grad1=40, taper_hor=1, gradt1=22, gradt2=25,
+                    exp_taper_grad_hor=0.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        vp, mis, it, ev = ctx.fatt(w.srcx, w.srcz, Tobs, w.vp_start, **opts)
+        secs = time.perf_counter() - t0
+        err0 = float(np.linalg.norm(w.vp_start - w.vp_true) / np.linalg.norm(w.vp_true))
+        err1 = float(np.linalg.norm(vp - w.vp_true) / np.linalg.norm(w.vp_true))
+        # the same inversion in the reference's own float arithmetic, for the model difference
+        ref = None
+        if args.mode == "fast" and not args.no_ref_run:
+            ctx_r = _context(R, w, "reference", stream, w.vp_true)
+            t1 = time.perf_counter()
+            vp_r, mis_r, it_r, ev_r = ctx_r.fatt(w.srcx, w.srcz, Tobs, w.vp_start, **opts)
+            ref = {"seconds": time.perf_counter() - t1, "iterations": it_r, "evaluations": ev_r,
+                   "final_misfit": float(mis_r[-1]) if len(mis_r) else None,
+                   "model_rel_diff_fast_vs_reference": float(np.linalg.norm(vp - vp_r) / np.linalg.norm(vp_r))}
+        out.update({"metric": "FATT stage wall time", "value": secs, "unit": "s", "higher_is_better": False,
+                    "iterations": it, "gradient_evaluations": ev, "shots": w.nshots, "receivers": w.ntr,
+                    "ms_per_gradient": 1e3 * secs / max(ev, 1), "shots_per_s": w.nshots * ev / secs,
+                    "misfit_first_last": [float(mis[0]), float(mis[-1])] if len(mis) else None,
+                    "model_rel_error_start_final": [err0, err1], "options": opts, "reference_mode_run": ref})
+        cores = os.cpu_count() or 1
+        kind = cpu_kind()
+        cpu_s = cpu_run(cores, cores, kind, "fatt", w.nshots)
+        per_eval = cpu_s * w.nshots / cores
+        out["cpu_baseline"] = {"value": per_eval * ev, "unit": "s", "cores": cores, "kind": kind,
+                               "sample": f"grad_obj of one shot per core, scaled to {w.nshots} shots x {ev} evaluations"}
     t_wall1 = time.time()
     time.sleep(0.15)
     clocks.stop()
@@ -482,8 +541,9 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mode", choices=["fast", "reference"], default="fast")
     ap.add_argument("--shots", type=int, default=100, help="shots per step (the workload has 100)")
-    ap.add_argument("--workload", choices=["grad_1700x350", "fwd_500x174", "uneven", "stress"],
+    ap.add_argument("--workload", choices=["grad_1700x350", "fwd_500x174", "uneven", "stress", "fatt"],
                     default="grad_1700x350", help="the benchmark workload (default) or another named one")
+    ap.add_argument("--no-ref-run", action="store_true", help="fatt: skip the reference-arithmetic comparison run")
     ap.add_argument("--profile-only", action="store_true",
                     help="only the device-timed loop (for profiler runs); no baselines, no JSON contract line")
     args = ap.parse_args()

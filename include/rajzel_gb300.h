@@ -145,6 +145,50 @@ int rz_grad_obj(rz_context *ctx, int nshots, const float *srcx, const float *src
 int rz_backward(rz_context *ctx, int nshots, const float *srcx, const float *srcz, const float *dTmod, float *grad,
                 int flags);
 
+/* ----------------------------------------------------------------------
+ * FATT inversion (fatt.c:108-258): l-BFGS with a weak-Wolfe line search over
+ * rz_grad_obj, on the GPU; one workflow stage.  Parameter names are the
+ * reference's (RAJZEL .inp and workflow files).
+ * ---------------------------------------------------------------------- */
+#define RZ_LBFGS_SLOT_ORDER 0    /* history visited in slot order, as LBFGS.c:113-150 */
+#define RZ_LBFGS_CHRONOLOGICAL 1 /* newest to oldest and back (Nocedal & Wright 7.4) */
+
+typedef struct {
+    int itermax;              /* ITERMAX: iterations of the stage */
+    int nlbfgs;               /* NLBFGS: stored (s, y) pairs */
+    int stepmax;              /* STEPMAX: gradient evaluations per line search */
+    float eps_scale;          /* EPS_SCALE: first trial step = EPS_SCALE*max(Vp)/max(Hgrad) */
+    float c1, c2;             /* C1, C2: Wolfe constants */
+    float scalefac;           /* SCALEFAC: step growth / bisection factor */
+    float vp_lo, vp_hi;       /* VPLOWERLIM, VPUPPERLIM: hard model limits */
+    float pro;                /* PRO: stop once |L2(i-2)-L2(i)|/L2(i-2) <= PRO */
+    int spatfilter;           /* SPATFILTER: 0 none, 4 Gaussian filter (gauss_filt.c) */
+    int filt_size_grad;       /* FILT_SIZE_GRAD: filter length in x (grid points) */
+    int filt_size_grad1;      /* FILT_SIZE_GRAD1: filter length in depth */
+    int taper_hor;            /* SWS_TAPER_GRAD_HOR: horizontal gradient taper */
+    int gradt1, gradt2;       /* GRADT1, GRADT2: taper rows (1-based) */
+    float exp_taper_grad_hor; /* EXP_TAPER_GRAD_HOR: depth scaling exponent below GRADT2 */
+    int recursion;            /* RZ_LBFGS_SLOT_ORDER or RZ_LBFGS_CHRONOLOGICAL */
+} rz_fatt_opts;
+
+/* The reference's example settings (par/RAJZEL_marm_OBC.inp) with NLBFGS 5,
+   ITERMAX 30, no filter or taper, slot-order recursion. */
+int rz_fatt_defaults(rz_fatt_opts *opts);
+
+/* precond() (precond.c:12-58) for SPATFILTER 4 and the horizontal taper:
+   grad [ny][nx] is filtered (gauss_filt.c) and tapered (taper_grad.c, sws 2)
+   in place, as opts selects.  The context must hold the grid. */
+int rz_precond(rz_context *ctx, const rz_fatt_opts *opts, float *grad, int flags);
+
+/* Invert for Vp.  The context must hold the grid and receivers (the model is
+   set by this call).  vp [ny][nx] is the start model on entry and the final
+   model on return (host pointers); Tobs [nshots][ntr] the observed picks;
+   misfit[itermax] receives L2 per iteration (or NULL); iterations and
+   evaluations (or NULL) the iterations done and rz_grad_obj calls made.
+   Misfit, dot products and the l-BFGS scalars are FP64; vectors FP32. */
+int rz_fatt(rz_context *ctx, const rz_fatt_opts *opts, int nshots, const float *srcx, const float *srcz,
+            const float *Tobs, float *vp, double *misfit, int *iterations, int *evaluations);
+
 /* Per-shot results of the last rz_forward/rz_grad_obj (host pointers, any
    may be NULL): outer passes of forward/adjoint, device status bits. */
 int rz_shot_info(rz_context *ctx, int shot, int *fwd_passes, int *adj_passes, int *status);

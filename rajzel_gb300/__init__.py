@@ -79,14 +79,37 @@ def load_library(path: str = LIB_PATH):
     lib.rz_eikonal_adj.argtypes = [vp, vp, vp, vp, vp, C.c_int]
     lib.rz_set_memory_cap.argtypes = [vp, C.c_size_t]
     lib.rz_shot_work.argtypes = [vp, C.c_int, vp, vp]
+    lib.rz_fatt_defaults.argtypes = [vp]
+    lib.rz_fatt.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp]
+    lib.rz_precond.argtypes = [vp, vp, vp, C.c_int]
     lib.rz_set_gradient.argtypes = [vp, C.c_int]
     lib.rz_backward.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
-    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
+    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
                  "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
                  "rz_eikonal_adj", "rz_shot_timeline", "rz_kernel_stats"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
+
+
+class FattOpts(C.Structure):
+    """rz_fatt_opts: the reference's FATT parameters (RAJZEL .inp / workflow names)."""
+    _fields_ = [("itermax", C.c_int), ("nlbfgs", C.c_int), ("stepmax", C.c_int), ("eps_scale", C.c_float),
+                ("c1", C.c_float), ("c2", C.c_float), ("scalefac", C.c_float), ("vp_lo", C.c_float),
+                ("vp_hi", C.c_float), ("pro", C.c_float), ("spatfilter", C.c_int), ("filt_size_grad", C.c_int),
+                ("filt_size_grad1", C.c_int), ("taper_hor", C.c_int), ("gradt1", C.c_int), ("gradt2", C.c_int),
+                ("exp_taper_grad_hor", C.c_float), ("recursion", C.c_int)]
+
+
+def fatt_opts(**kw):
+    """rz_fatt_defaults() with keyword overrides (field names of rz_fatt_opts)."""
+    o = FattOpts()
+    load_library().rz_fatt_defaults(C.byref(o))
+    for k, v in kw.items():
+        if not hasattr(o, k):
+            raise KeyError(k)
+        setattr(o, k, v)
+    return o
 
 
 def _ptr(a):
@@ -181,6 +204,26 @@ class Context:
         self._check(self.lib.rz_backward(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(dTmod), _ptr(grad), 0),
                     "rz_backward")
         return grad
+
+    def fatt(self, srcx, srcz, Tobs, vp, opts=None, **kw):
+        """FATT stage (rz_fatt): returns (final vp, misfit per iteration, iterations, gradient evaluations)."""
+        o = opts if opts is not None else fatt_opts(**kw)
+        srcx, srcz = _f32(srcx), _f32(srcz)
+        n = len(srcx)
+        Tobs = _f32(Tobs).reshape(n, self.ntr) if self.ntr else np.zeros((n, 1), np.float32)
+        model = _f32(vp).reshape(self.ny, self.nx).copy()
+        mis = np.zeros(max(o.itermax, 1), np.float64)
+        it, ev = C.c_int(0), C.c_int(0)
+        self._check(self.lib.rz_fatt(self.h, C.byref(o), n, _ptr(srcx), _ptr(srcz), _ptr(Tobs), _ptr(model),
+                                     _ptr(mis), C.byref(it), C.byref(ev)), "rz_fatt")
+        return model, mis[: it.value], it.value, ev.value
+
+    def precond(self, grad, opts=None, **kw):
+        """precond() on one gradient (rz_precond): Gaussian filter and horizontal taper."""
+        o = opts if opts is not None else fatt_opts(**kw)
+        g = _f32(grad).reshape(self.ny, self.nx).copy()
+        self._check(self.lib.rz_precond(self.h, C.byref(o), _ptr(g), 0), "rz_precond")
+        return g
 
     def set_memory_cap(self, nbytes: int):
         """Bytes of device memory the per-shot field slots may use (0 = automatic)."""

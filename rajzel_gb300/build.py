@@ -25,7 +25,7 @@ SELFTEST = os.path.join(PKG, "librz_selftest.so")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
-CU_SOURCES = ["rz_shot.cu", "rz_aux.cu", "rz_api.cu", "rz_noalloc.cu"]
+CU_SOURCES = ["rz_shot.cu", "rz_aux.cu", "rz_api.cu", "rz_noalloc.cu", "rz_fatt.cu"]
 HEADERS = ["rz_device.cuh", "rz_internal.h"]
 
 

@@ -457,6 +457,22 @@ static int stack_chunk(rz_context *c, int first, int m, float *gdst) {
     return RZ_OK;
 }
 
+int rz_context_query(rz_context *c, int *nx, int *ny, float *dh, int *ntr, cudaStream_t *stream) {
+    if (!c) return RZ_EINVAL;
+    if (!c->grid_set) return fail(c, RZ_ESTATE, "rz_set_grid has not been called");
+    cudaSetDevice(c->device);
+    *nx = c->g.nx;
+    *ny = c->g.ny;
+    *dh = c->g.dh;
+    *ntr = c->rec_set ? c->ntr : 0;
+    *stream = c->st;
+    return RZ_OK;
+}
+
+void rz_context_set_error(rz_context *c, const char *msg) {
+    if (c) c->err = msg;
+}
+
 // ---------------------------------------------------------------------------
 // C ABI
 // ---------------------------------------------------------------------------

@@ -131,3 +131,8 @@ cudaError_t launch_calc_s(const float *vp, float *S, long n, cudaStream_t st);
 cudaError_t launch_sum_l2(const double *l2, int n, double *out, cudaStream_t st);
 
 }  // namespace rz
+
+// context accessors for code layered on the C ABI (rz_fatt.cu)
+struct rz_context;
+int rz_context_query(rz_context *c, int *nx, int *ny, float *dh, int *ntr, cudaStream_t *stream);
+void rz_context_set_error(rz_context *c, const char *msg);

@@ -135,7 +135,9 @@ def uneven_grid(idx, seed=77, nshots=None, ntr=None):
     nr = nx // 2 if ntr is None else ntr
     recx = grid_index(dh * (1.0 + np.linspace(1, nx - 2, nr)), dh)
     recz = np.full(nr, 2, np.int32)
-    return Workload(f"uneven_{nx}x{ny}", nx, ny, dh, 40.0, 1e-6, 1e-9, vp, vp, srcx, srcz, recx.astype(np.int32), recz)
+    # picks from this model; gradients taken at a start model 3% slower
+    return Workload(f"uneven_{nx}x{ny}", nx, ny, dh, 40.0, 1e-6, 1e-9, vp, (vp * np.float32(0.97)).astype(np.float32),
+                    srcx, srcz, recx.astype(np.int32), recz)
 
 
 def fatt_2000x500(seed=99, nshots=200, ntr=1000):
@@ -154,6 +156,21 @@ def fatt_2000x500(seed=99, nshots=200, ntr=1000):
     recz = np.full(ntr, 2, np.int32)
     return Workload("fatt_2000x500", nx, ny, dh, 30.0, 1e-6, 1e-9, true.astype(np.float32),
                     start.astype(np.float32), srcx, srcz, recx.astype(np.int32), recz)
+
+
+def fatt_small(sub=8, nshots=8, ntr=100, seed=99):
+    """The FATT model sampled every `sub` cells (2000x500 / sub, dh*sub): a
+    small case of the same structure for tests."""
+    w = fatt_2000x500(seed=seed, nshots=1, ntr=10)
+    vt = np.ascontiguousarray(w.vp_true[::sub, ::sub])
+    vs = np.ascontiguousarray(w.vp_start[::sub, ::sub])
+    ny, nx = vt.shape
+    dh = w.dh * sub
+    srcx = (dh * (2.0 + (nx - 4) * (np.arange(nshots) + 0.5) / nshots)).astype(np.float32)
+    srcz = np.full(nshots, 2 * dh, np.float32)
+    recx = grid_index(dh * (1.0 + np.linspace(1, nx - 2, ntr)), dh).astype(np.int32)
+    recz = np.full(ntr, 2, np.int32)
+    return Workload(f"fatt_{nx}x{ny}", nx, ny, dh, w.time, w.ttnorm, w.eps_adj, vt, vs, srcx, srcz, recx, recz)
 
 
 def _polygon_mask(rng, nx, ny, dh, cx, cz, r_mean, nvert=9):
@@ -189,7 +206,9 @@ def stress_8192x2048(seed=4096, nshots=1024, ntr=4096):
     srcz = np.full(nshots, 2 * dh, np.float32)
     recx = grid_index(dh * (1.0 + np.linspace(1, nx - 2, ntr)), dh)
     recz = np.full(ntr, 2, np.int32)
-    return Workload("stress_8192x2048", nx, ny, dh, 30.0, 1e-6, 1e-9, vp, vp, srcx, srcz, recx.astype(np.int32),
+    # start model: the block at 3500 m/s
+    start = np.where(mask, np.float32(3500.0), vp).astype(np.float32)
+    return Workload("stress_8192x2048", nx, ny, dh, 30.0, 1e-6, 1e-9, vp, start, srcx, srcz, recx.astype(np.int32),
                     recz)
 
 
