@@ -502,7 +502,7 @@ def run_workload(args, local_rank):
                     exp_taper_grad_hor=0.0)
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        vp, mis, it, ev = ctx.fatt(w.srcx, w.srcz, Tobs, w.vp_start, **opts)
+        vp, mis, it, ev, _ = ctx.fatt(w.srcx, w.srcz, Tobs, w.vp_start, **opts)
         secs = time.perf_counter() - t0
         err0 = float(np.linalg.norm(w.vp_start - w.vp_true) / np.linalg.norm(w.vp_true))
         err1 = float(np.linalg.norm(vp - w.vp_true) / np.linalg.norm(w.vp_true))
@@ -511,7 +511,7 @@ def run_workload(args, local_rank):
         if args.mode == "fast" and not args.no_ref_run:
             ctx_r = _context(R, w, "reference", stream, w.vp_true)
             t1 = time.perf_counter()
-            vp_r, mis_r, it_r, ev_r = ctx_r.fatt(w.srcx, w.srcz, Tobs, w.vp_start, **opts)
+            vp_r, mis_r, it_r, ev_r, _ = ctx_r.fatt(w.srcx, w.srcz, Tobs, w.vp_start, **opts)
             ref = {"seconds": time.perf_counter() - t1, "iterations": it_r, "evaluations": ev_r,
                    "final_misfit": float(mis_r[-1]) if len(mis_r) else None,
                    "model_rel_diff_fast_vs_reference": float(np.linalg.norm(vp - vp_r) / np.linalg.norm(vp_r))}

@@ -183,11 +183,19 @@ int rz_precond(rz_context *ctx, const rz_fatt_opts *opts, float *grad, int flags
 /* Invert for Vp.  The context must hold the grid and receivers (the model is
    set by this call).  vp [ny][nx] is the start model on entry and the final
    model on return (host pointers); Tobs [nshots][ntr] the observed picks;
-   misfit[itermax] receives L2 per iteration (or NULL); iterations and
-   evaluations (or NULL) the iterations done and rz_grad_obj calls made.
-   Misfit, dot products and the l-BFGS scalars are FP64; vectors FP32. */
+   misfit[itermax] and steps[itermax] receive L2 and the accepted step length
+   per iteration (the columns of the reference's misfit log, fatt.c:202), or
+   NULL; iterations and evaluations (or NULL) the iterations done and
+   rz_grad_obj calls made.  Misfit, dot products and the l-BFGS scalars are
+   FP64; vectors FP32. */
 int rz_fatt(rz_context *ctx, const rz_fatt_opts *opts, int nshots, const float *srcx, const float *srcz,
-            const float *Tobs, float *vp, double *misfit, int *iterations, int *evaluations);
+            const float *Tobs, float *vp, double *misfit, float *steps, int *iterations, int *evaluations);
+
+/* Misfit only: forward solves and residuals of nshots sources, L2 =
+   0.5*sum (Tmod - Tobs)^2 over unmuted picks (the objective of
+   grid_search.c:62-80, calc_FA_res.c:34-47); no adjoint, no gradient. */
+int rz_misfit(rz_context *ctx, int nshots, const float *srcx, const float *srcz, const float *Tobs, double *L2,
+              int flags);
 
 /* Per-shot results of the last rz_forward/rz_grad_obj (host pointers, any
    may be NULL): outer passes of forward/adjoint, device status bits. */

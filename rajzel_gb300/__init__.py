@@ -19,6 +19,7 @@ device present, or the calls raise.
 """
 from __future__ import annotations
 
+import collections
 import ctypes as C
 import os
 
@@ -80,11 +81,12 @@ def load_library(path: str = LIB_PATH):
     lib.rz_set_memory_cap.argtypes = [vp, C.c_size_t]
     lib.rz_shot_work.argtypes = [vp, C.c_int, vp, vp]
     lib.rz_fatt_defaults.argtypes = [vp]
-    lib.rz_fatt.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp]
+    lib.rz_fatt.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
+    lib.rz_misfit.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
     lib.rz_precond.argtypes = [vp, vp, vp, C.c_int]
     lib.rz_set_gradient.argtypes = [vp, C.c_int]
     lib.rz_backward.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
-    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
+    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_misfit", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
                  "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
                  "rz_eikonal_adj", "rz_shot_timeline", "rz_kernel_stats"):
         getattr(lib, name).restype = C.c_int
@@ -99,6 +101,9 @@ class FattOpts(C.Structure):
                 ("vp_hi", C.c_float), ("pro", C.c_float), ("spatfilter", C.c_int), ("filt_size_grad", C.c_int),
                 ("filt_size_grad1", C.c_int), ("taper_hor", C.c_int), ("gradt1", C.c_int), ("gradt2", C.c_int),
                 ("exp_taper_grad_hor", C.c_float), ("recursion", C.c_int)]
+
+
+FattResult = collections.namedtuple("FattResult", "vp misfit iterations evaluations steps")
 
 
 def fatt_opts(**kw):
@@ -206,17 +211,27 @@ class Context:
         return grad
 
     def fatt(self, srcx, srcz, Tobs, vp, opts=None, **kw):
-        """FATT stage (rz_fatt): returns (final vp, misfit per iteration, iterations, gradient evaluations)."""
+        """FATT stage (rz_fatt): returns FattResult(vp, misfit, iterations, evaluations, steps)."""
         o = opts if opts is not None else fatt_opts(**kw)
         srcx, srcz = _f32(srcx), _f32(srcz)
         n = len(srcx)
         Tobs = _f32(Tobs).reshape(n, self.ntr) if self.ntr else np.zeros((n, 1), np.float32)
         model = _f32(vp).reshape(self.ny, self.nx).copy()
         mis = np.zeros(max(o.itermax, 1), np.float64)
+        steps = np.zeros(max(o.itermax, 1), np.float32)
         it, ev = C.c_int(0), C.c_int(0)
         self._check(self.lib.rz_fatt(self.h, C.byref(o), n, _ptr(srcx), _ptr(srcz), _ptr(Tobs), _ptr(model),
-                                     _ptr(mis), C.byref(it), C.byref(ev)), "rz_fatt")
-        return model, mis[: it.value], it.value, ev.value
+                                     _ptr(mis), _ptr(steps), C.byref(it), C.byref(ev)), "rz_fatt")
+        return FattResult(model, mis[: it.value], it.value, ev.value, steps[: it.value])
+
+    def misfit(self, srcx, srcz, Tobs):
+        """0.5 * sum (Tmod - Tobs)^2 over unmuted picks (rz_misfit: forward solves only)."""
+        srcx, srcz = _f32(srcx), _f32(srcz)
+        n = len(srcx)
+        Tobs = _f32(Tobs).reshape(n, self.ntr) if self.ntr else np.zeros((n, 1), np.float32)
+        L2 = C.c_double(0.0)
+        self._check(self.lib.rz_misfit(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(Tobs), C.byref(L2), 0), "rz_misfit")
+        return L2.value
 
     def precond(self, grad, opts=None, **kw):
         """precond() on one gradient (rz_precond): Gaussian filter and horizontal taper."""

@@ -6,6 +6,7 @@ Products (all git-ignored, rebuilt on each machine):
     rajzel_gb300/librajzel_gb300.so     CUDA kernels + the C ABI of include/rajzel_gb300.h
     rajzel_gb300/librajzel_compat.so    reference-signature shim (eikonal(), grad_obj(), ...)
     rajzel_gb300/librz_selftest.so      device self-tests of the arithmetic kernels (tests only)
+    rajzel_gb300/rajzel_gpu             driver: runs a RAJZEL parameter directory (INVMAT 0/1/2)
 """
 from __future__ import annotations
 
@@ -22,6 +23,8 @@ BUILD = os.path.join(ROOT, "_build")
 LIB = os.path.join(PKG, "librajzel_gb300.so")
 COMPAT = os.path.join(PKG, "librajzel_compat.so")
 SELFTEST = os.path.join(PKG, "librz_selftest.so")
+DRIVER = os.path.join(PKG, "rajzel_gpu")
+C_SOURCES = ["rz_io.c"]  # host C compiled into the library
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
@@ -63,6 +66,13 @@ def build(verbose: bool = False) -> str:
     selftest_obj = os.path.join(BUILD, "rz_selftest.o")
     if os.path.exists(selftest_src) and _stale(selftest_obj, [selftest_src] + hdrs):
         jobs.append([nvcc(), *NVFLAGS, "-c", selftest_src, "-o", selftest_obj])
+    inc = os.path.join(ROOT, "include")
+    for src in C_SOURCES:
+        s = os.path.join(CSRC, src)
+        o = os.path.join(BUILD, src.replace(".c", ".o"))
+        objs.append(o)
+        if _stale(o, [s, os.path.join(inc, "rajzel_io.h")]):
+            jobs.append(["gcc", "-O2", "-std=gnu99", "-fPIC", "-Wall", "-ffp-contract=off", "-I", inc, "-c", s, "-o", o])
     if jobs:
         with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             list(ex.map(_run, jobs))
@@ -74,6 +84,10 @@ def build(verbose: bool = False) -> str:
     if os.path.exists(compat_src) and _stale(COMPAT, [compat_src, LIB, os.path.join(ROOT, "include", "rajzel_compat.h")]):
         _run(["gcc", "-O2", "-std=gnu99", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"), "-o", COMPAT,
               compat_src, "-L", PKG, "-lrajzel_gb300", "-Wl,-rpath,$ORIGIN", "-lm"])
+    driver_src = os.path.join(CSRC, "rz_main.c")
+    if os.path.exists(driver_src) and _stale(DRIVER, [driver_src, LIB]):
+        _run(["gcc", "-O2", "-std=gnu99", "-Wall", "-ffp-contract=off", "-I", inc, "-o", DRIVER, driver_src, "-L",
+              PKG, "-lrajzel_gb300", "-Wl,-rpath,$ORIGIN", "-lm"])
     if verbose:
         print(f"built {LIB}")
     return LIB

@@ -791,6 +791,34 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
     return collect_status(c, nshots);
 }
 
+int rz_misfit(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *Tobs, double *L2,
+              int flags) {
+    int r;
+    if ((r = ready(c, true))) return r;
+    if (nshots < 1 || !Tobs || !L2) return fail(c, RZ_EINVAL, "bad arguments");
+    cudaSetDevice(c->device);
+    int chunk = 0;
+    if ((r = ensure_shots(c, nshots))) return r;
+    if ((r = plan_chunks(c, nshots, &chunk))) return r;
+    if ((r = set_sources(c, nshots, srcx, srcz))) return r;
+    const size_t nt = (size_t)nshots * c->ntr;
+    if (nt) CK(cudaMemcpyAsync(c->dTobs, Tobs, nt * 4, have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
+    if ((r = reset_shots(c, nshots))) return r;
+    for (int first = 0; first < nshots; first += chunk) {
+        const int m = nshots - first < chunk ? nshots - first : chunk;
+        if ((r = run_batch(c, first, m, false, true, false))) return r;
+    }
+    if (!c->dL2) CK(dalloc(&c->dL2, 1));
+    CK(launch_sum_l2(c->dl2, nshots, c->dL2, c->st));
+    c->launches += 1;
+    if (have_dev(flags)) {
+        CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+        return RZ_OK;
+    }
+    CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    return collect_status(c, nshots);
+}
+
 int rz_set_gradient(rz_context *c, int kind) {
     if (!c) return RZ_EINVAL;
     if (kind != RZ_GRADIENT_REFERENCE && kind != RZ_GRADIENT_EXACT)

@@ -415,7 +415,7 @@ int rz_precond(rz_context *ctx, const rz_fatt_opts *opts, float *grad, int flags
 }
 
 int rz_fatt(rz_context *ctx, const rz_fatt_opts *opts, int nshots, const float *srcx, const float *srcz,
-            const float *Tobs, float *vp_io, double *misfit, int *iterations, int *evaluations) {
+            const float *Tobs, float *vp_io, double *misfit, float *steps, int *iterations, int *evaluations) {
     if (!ctx || !opts || !srcx || !srcz || !Tobs || !vp_io || nshots < 1) return RZ_EINVAL;
     struct {
         int nx, ny;
@@ -467,6 +467,7 @@ int rz_fatt(rz_context *ctx, const rz_fatt_opts *opts, int nshots, const float *
         if (F.err) break;
         hist.push_back(L2);
         if (misfit) misfit[iter - 1] = L2;
+        if (steps) steps[iter - 1] = step;
         model_step_kernel<<<grid_for(F.n), kThreads, 0, st>>>(F.n, F.vp, F.hgrad, step, opts->vp_lo, opts->vp_hi, F.vnp1);
         F.ck(cudaGetLastError(), "model update");
         F.copy(F.vp, F.vnp1);

@@ -59,7 +59,7 @@ def test_fatt_matches_oracle_loop(R, recursion):
     w, p, Tobs, start = fatt_case()
     opts = dict(itermax=5, nlbfgs=3, recursion=recursion, vp_lo=1000.0, vp_hi=6000.0)
     ctx = make(R, w, "reference")
-    vp_g, mis_g, it_g, ev_g = ctx.fatt(w.srcx, w.srcz, Tobs, start, **opts)
+    vp_g, mis_g, it_g, ev_g, _ = ctx.fatt(w.srcx, w.srcz, Tobs, start, **opts)
     full = R.fatt_opts(**opts)
     o = {f: getattr(full, f) for f, _ in R.FattOpts._fields_}
     vp_o, mis_o, it_o, ev_o = OF.fatt(p, start, w.srcx, w.srcz, w.recx, w.recz, Tobs, o)
@@ -71,7 +71,7 @@ def test_fatt_matches_oracle_loop(R, recursion):
 def test_fatt_fast_mode_reduces_misfit_and_model_error(R):
     w, p, Tobs, start = fatt_case(sub=4, nshots=12)
     ctx = make(R, w, "fast")
-    vp, mis, it, ev = ctx.fatt(w.srcx, w.srcz, Tobs, start, itermax=8, nlbfgs=5, vp_lo=1000.0, vp_hi=6000.0,
+    vp, mis, it, ev, _ = ctx.fatt(w.srcx, w.srcz, Tobs, start, itermax=8, nlbfgs=5, vp_lo=1000.0, vp_hi=6000.0,
                                recursion=1)
     assert it >= 3 and ev >= it
     assert mis[-1] < 0.5 * mis[0]
