@@ -191,6 +191,17 @@ int rz_precond(rz_context *ctx, const rz_fatt_opts *opts, float *grad, int flags
 int rz_fatt(rz_context *ctx, const rz_fatt_opts *opts, int nshots, const float *srcx, const float *srcz,
             const float *Tobs, float *vp, double *misfit, float *steps, int *iterations, int *evaluations);
 
+/* Several grids in one launch (no counterpart in the reference): each
+   context holds one grid, its model and receivers; shot i of grid g is a job
+   of one persistent kernel whose CTAs take jobs largest grid first, so small
+   grids fill the SMs while the large ones run.  Per grid the results equal
+   rz_grad_obj on that context.  All contexts must use the same device and
+   mode and the reference gradient; the work runs on ctxs[0]'s stream.
+     nshots[g], srcx[g], srcz[g], Tobs[g], grad[g]: as rz_grad_obj, per grid
+     L2[ngrids]: misfit per grid */
+int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, const float *const *srcx,
+                      const float *const *srcz, const float *const *Tobs, float *const *grad, double *L2, int flags);
+
 /* Misfit only: forward solves and residuals of nshots sources, L2 =
    0.5*sum (Tmod - Tobs)^2 over unmuted picks (the objective of
    grid_search.c:62-80, calc_FA_res.c:34-47); no adjoint, no gradient. */

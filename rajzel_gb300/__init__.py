@@ -80,18 +80,39 @@ def load_library(path: str = LIB_PATH):
     lib.rz_eikonal_adj.argtypes = [vp, vp, vp, vp, vp, C.c_int]
     lib.rz_set_memory_cap.argtypes = [vp, C.c_size_t]
     lib.rz_shot_work.argtypes = [vp, C.c_int, vp, vp]
+    lib.rz_grad_obj_multi.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_int]
     lib.rz_fatt_defaults.argtypes = [vp]
     lib.rz_fatt.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
     lib.rz_misfit.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
     lib.rz_precond.argtypes = [vp, vp, vp, C.c_int]
     lib.rz_set_gradient.argtypes = [vp, C.c_int]
     lib.rz_backward.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
-    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_misfit", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
+    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_grad_obj_multi", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_misfit", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
                  "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
                  "rz_eikonal_adj", "rz_shot_timeline", "rz_kernel_stats"):
         getattr(lib, name).restype = C.c_int
     _lib = lib
     return lib
+
+
+def grad_obj_multi(ctxs, srcx, srcz, Tobs):
+    """rz_grad_obj_multi: one persistent launch over the shots of several
+    contexts (one grid each); returns [(grad, L2)] per context."""
+    n = len(ctxs)
+    lib = ctxs[0].lib
+    sx = [_f32(a) for a in srcx]
+    sz = [_f32(a) for a in srcz]
+    tob = [_f32(t).reshape(len(sx[i]), ctxs[i].ntr) if ctxs[i].ntr else np.zeros((len(sx[i]), 1), np.float32)
+           for i, t in enumerate(Tobs)]
+    grads = [np.empty((c.ny, c.nx), np.float32) for c in ctxs]
+    P = C.c_void_p * n
+    handles = P(*[c.h.value for c in ctxs])
+    ns = (C.c_int * n)(*[len(a) for a in sx])
+    L2 = (C.c_double * n)()
+    st = lib.rz_grad_obj_multi(n, handles, ns, P(*[a.ctypes.data for a in sx]), P(*[a.ctypes.data for a in sz]),
+                               P(*[a.ctypes.data for a in tob]), P(*[g.ctypes.data for g in grads]), L2, 0)
+    ctxs[0]._check(st, "rz_grad_obj_multi")
+    return [(grads[i], L2[i]) for i in range(n)]
 
 
 class FattOpts(C.Structure):

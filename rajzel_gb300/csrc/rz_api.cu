@@ -10,6 +10,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -79,6 +80,11 @@ struct rz_context {
     int last_n = 0;           // shots of the last batch
     int last_first = 0;       // first shot whose fields are still in the slots
     bool last_adj = false;
+
+    // persistent multi-grid launches driven by this context
+    int2 *dJobs = nullptr;
+    int njobs_cap = 0;
+    int *dCounter = nullptr;
 
     // accounting: kernels launched, and CUDA-event timing of every shot-kernel launch
     long long launches = 0;
@@ -521,6 +527,7 @@ void rz_destroy(rz_context *c) {
     dfree(c->dSkipP);
     dfree(c->dMA), dfree(c->dMB), dfree(c->dGrad64);
     dfree(c->dXcH), dfree(c->dXcK), dfree(c->dXcOff), dfree(c->dXcRec);
+    dfree(c->dJobs), dfree(c->dCounter);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
 }
@@ -817,6 +824,126 @@ int rz_misfit(rz_context *c, int nshots, const float *srcx, const float *srcz, c
     }
     CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToHost, c->st));
     return collect_status(c, nshots);
+}
+
+int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, const float *const *srcx,
+                      const float *const *srcz, const float *const *Tobs, float *const *grad, double *L2, int flags) {
+    if (ngrids < 1 || ngrids > kMaxGrids || !ctxs || !nshots || !srcx || !srcz || !Tobs || !grad || !L2)
+        return RZ_EINVAL;
+    rz_context *c0 = ctxs[0];
+    if (!c0) return RZ_EINVAL;
+    rz_context *c = c0;  // error reports of the CK() checks below
+    for (int i = 0; i < ngrids; ++i) {
+        rz_context *c = ctxs[i];
+        int r;
+        if (!c) return fail(c0, RZ_EINVAL, "context %d is NULL", i);
+        if ((r = ready(c, true))) return fail(c0, r, "grid %d: %s", i, c->err.c_str());
+        if (c->device != c0->device || c->mode != c0->mode)
+            return fail(c0, RZ_EINVAL, "grid %d: every context must use the same device and mode", i);
+        if (c->grad_kind != RZ_GRADIENT_REFERENCE)
+            return fail(c0, RZ_EUNSUPPORTED, "grid %d: the exact gradient is not available in multi-grid launches", i);
+        if (nshots[i] < 1 || !Tobs[i] || !grad[i]) return fail(c0, RZ_EINVAL, "grid %d: bad arguments", i);
+        for (int k = 0; k < i; ++k)
+            if (ctxs[k] == c) return fail(c0, RZ_EINVAL, "context %d appears twice", i);
+    }
+    cudaSetDevice(c0->device);
+    cudaStream_t st = c0->st;
+    // every grid's work goes on the first context's stream for this call
+    std::vector<cudaStream_t> saved(ngrids);
+    for (int i = 0; i < ngrids; ++i) {
+        saved[i] = ctxs[i]->st;
+        if (ctxs[i]->st != st) CK(cudaStreamSynchronize(ctxs[i]->st));
+        ctxs[i]->st = st;
+    }
+    struct Restore {
+        rz_context *const *c;
+        std::vector<cudaStream_t> &s;
+        ~Restore() {
+            for (size_t i = 0; i < s.size(); ++i) c[i]->st = s[i];
+        }
+    } restore{ctxs, saved};
+
+    MultiParams M;
+    memset(&M, 0, sizeof M);
+    M.ngrids = ngrids;
+    int Wb = 1, r;
+    std::vector<std::pair<long, int2>> jobs;
+    for (int i = 0; i < ngrids; ++i) {
+        rz_context *c = ctxs[i];
+        const int n = nshots[i];
+        int chunk = 0;
+        if ((r = ensure_shots(c, n)) || (r = plan_chunks(c, n, &chunk))) return fail(c0, r, "%s", c->err.c_str());
+        if (chunk < n)
+            return fail(c0, RZ_EUNSUPPORTED, "grid %d: %d shots do not fit the memory cap in one launch", i, n);
+        if ((r = set_sources(c, n, srcx[i], srcz[i]))) return fail(c0, r, "%s", c->err.c_str());
+        if (c->mode == RZ_MODE_REFERENCE && (r = ensure_cube(c))) return fail(c0, r, "%s", c->err.c_str());
+        if ((r = ensure_div(c))) return fail(c0, r, "%s", c->err.c_str());
+        const size_t nt = (size_t)n * c->ntr;
+        if (nt)
+            CK(cudaMemcpyAsync(c->dTobs, Tobs[i], nt * 4, have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                               st));
+        if ((r = reset_shots(c, n))) return r;
+        MultiGrid &G = M.grid[i];
+        fill_params(c, G.P, 0, n);
+        G.P.do_residual = 1;
+        G.P.do_adjoint = 1;
+        G.tld = c->mTld;
+        G.trow = c->mTrow;
+        G.lrow = c->mLrow;
+        G.W = shot_kernel_warps(c->nstrips);
+        Wb = std::max(Wb, G.W);
+        const long cost = (long)c->g.ny * c->nxp;  // cells per shot: the larger grids go first
+        for (int z = 0; z < n; ++z) jobs.push_back({cost, make_int2(i, z)});
+        c->last_first = 0;
+        c->last_adj = true;
+    }
+    std::stable_sort(jobs.begin(), jobs.end(), [](const std::pair<long, int2> &a, const std::pair<long, int2> &b) {
+        return a.first > b.first;
+    });
+    const int nj = (int)jobs.size();
+    if (nj > c0->njobs_cap) {
+        CK(dalloc(&c0->dJobs, (size_t)nj));
+        c0->njobs_cap = nj;
+    }
+    if (!c0->dCounter) CK(dalloc(&c0->dCounter, 1));
+    std::vector<int2> hj(nj);
+    for (int k = 0; k < nj; ++k) hj[k] = jobs[k].second;
+    CK(cudaMemcpyAsync(c0->dJobs, hj.data(), sizeof(int2) * nj, cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(c0->dCounter, 0, sizeof(int), st));
+    M.njobs = nj;
+    M.counter = c0->dCounter;
+    M.jobs = c0->dJobs;
+    cudaEvent_t e0, e1;
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    CK(cudaEventRecord(e0, st));
+    CK(launch_multi_shot_kernel(M, c0->mode, Wb, nullptr, st));
+    CK(cudaEventRecord(e1, st));
+    c0->shot_events.emplace_back(e0, e1);
+    c0->launches += 1;
+    // per grid: stack, frame copy, misfit
+    for (int i = 0; i < ngrids; ++i) {
+        rz_context *c = ctxs[i];
+        float *gdst = grad[i];
+        if (!have_dev(flags)) {
+            if (!c->dGrad) CK(dalloc(&c->dGrad, (size_t)c->g.nx * c->g.ny));
+            gdst = c->dGrad;
+        }
+        if (c->mode == RZ_MODE_FAST && !c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
+        if ((r = stack_chunk(c, 0, nshots[i], gdst))) return fail(c0, r, "%s", c->err.c_str());
+        CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, st));
+        if (!c->dL2) CK(dalloc(&c->dL2, 1));
+        CK(launch_sum_l2(c->dl2, nshots[i], c->dL2, st));
+        c->launches += 2;
+        CK(cudaMemcpyAsync(L2 + i, c->dL2, sizeof(double),
+                           have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
+        if (!have_dev(flags))
+            CK(cudaMemcpyAsync(grad[i], gdst, (size_t)c->g.nx * c->g.ny * 4, cudaMemcpyDeviceToHost, st));
+    }
+    if (have_dev(flags)) return RZ_OK;
+    for (int i = 0; i < ngrids; ++i)
+        if ((r = collect_status(ctxs[i], nshots[i]))) return fail(c0, r, "grid %d: %s", i, ctxs[i]->err.c_str());
+    return RZ_OK;
 }
 
 int rz_set_gradient(rz_context *c, int kind) {

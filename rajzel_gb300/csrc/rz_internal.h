@@ -97,8 +97,25 @@ struct ShotParams {
     unsigned long long *timeline;           // [nshots][kTimelineSlots] ns stamps, or null
 };
 
+// several grids in one persistent launch
+constexpr int kMaxGrids = 8;
+struct MultiGrid {
+    CUtensorMap tld, trow, lrow;  // as for launch_shot_kernel
+    ShotParams P;
+    int W;                        // warps of the CTA that sweep this grid's strips
+};
+struct MultiParams {
+    MultiGrid grid[kMaxGrids];
+    int ngrids, njobs;
+    int *counter;       // zeroed before the launch
+    const int2 *jobs;   // [njobs] (grid, shot), largest grids first
+};
+
 // launchers (rz_shot.cu)
 size_t shot_kernel_smem(int nwarps);
+int shot_kernel_warps(int nstrips);  // warps per CTA for a grid of nstrips strips
+// persistent CTAs of Wb warps (Wb >= every grid's W); nctas receives the grid size
+cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int Wb, int *nctas, cudaStream_t st);
 // mapT_tile: [shots][ny][nx] traveltimes, 32x33 box (adjoint preparation);
 // mapT_row / mapL_row: traveltime / lambda, 32x1 box (the sweeps)
 cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const CUtensorMap &mapT_tile, const CUtensorMap &mapT_row,

@@ -23,6 +23,8 @@
 // converged traveltimes, adjoint skip bits) are stored pre-skewed so that the
 // 32 values one wavefront step needs are one 128-byte line: fully coalesced
 // and prefetched eight steps ahead into registers.
+#include <algorithm>
+
 #include "rz_device.cuh"
 #include "rz_internal.h"
 
@@ -131,6 +133,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     // exact discrete adjoint: mu = R + sum of the weights neighbours put on this cell
     constexpr bool EX = ADJ && (MODE == kModeExact);
     const int l = w.l, g = w.g;
+    if (g >= W) return;  // warps beyond this grid's W only join the CTA's barriers
     const bool pipe = seq.pipelined != 0;
     // strips are swept in bands of W (one strip per warp); sig is the strip's
     // position in sweep order, s its index from the top of the grid
@@ -859,39 +862,49 @@ __device__ __noinline__ void exact_prepare(const ShotParams &P, int z, const flo
 // ---------------------------------------------------------------------------
 // the shot kernel
 // ---------------------------------------------------------------------------
-template <int MODE>
-__global__ void __launch_bounds__(kMaxWarps * 32, 1)
-    shot_kernel(const __grid_constant__ ShotParams P, const __grid_constant__ CUtensorMap mTld,
-                const __grid_constant__ CUtensorMap mTrow, const __grid_constant__ CUtensorMap mLrow) {
-    extern __shared__ __align__(128) unsigned char smem_raw[];
-    const int W = blockDim.x >> 5;
-    const int tid = threadIdx.x, g = tid >> 5, l = tid & 31;
-    const int z = blockIdx.x;
-    if (z >= P.nshots) return;
-
+// Shared-memory layout of a CTA of Wb warps, and its (re)initialisation: ring
+// and hand-off barriers armed at phase 0, control words and completed-sweep
+// counters cleared.  reinit invalidates the barriers of the previous job.
+RZ_DEV CtaShared carve_smem(unsigned char *smem_raw, int Wb) {
     CtaShared sh;
-    {
-        size_t o = 0;
-        sh.w = reinterpret_cast<WarpShared *>(smem_raw);
-        o = sizeof(WarpShared) * W;
-        o = align_up(o, 8);
-        sh.mbar = reinterpret_cast<uint64_t *>(smem_raw + o);
-        o += sizeof(uint64_t) * kRing * W;
-        o = align_up(o, 8);
-        sh.red = reinterpret_cast<double *>(smem_raw + o);
-        o += sizeof(double) * W;
-        sh.ctl = reinterpret_cast<int *>(smem_raw + o);
-        sh.done = sh.ctl + 8;
-    }
+    size_t o = 0;
+    sh.w = reinterpret_cast<WarpShared *>(smem_raw);
+    o = sizeof(WarpShared) * Wb;
+    o = align_up(o, 8);
+    sh.mbar = reinterpret_cast<uint64_t *>(smem_raw + o);
+    o += sizeof(uint64_t) * kRing * Wb;
+    o = align_up(o, 8);
+    sh.red = reinterpret_cast<double *>(smem_raw + o);
+    o += sizeof(double) * Wb;
+    sh.ctl = reinterpret_cast<int *>(smem_raw + o);
+    sh.done = sh.ctl + 8;
+    return sh;
+}
+
+RZ_DEV void init_cta(const CtaShared &sh, int Wb, bool reinit) {
+    const int tid = threadIdx.x, g = tid >> 5, l = tid & 31;
     if (l == 0) {
-        for (int i = 0; i < kRing; ++i) mbar_init(&sh.mbar[g * kRing + i], 1);
+        for (int i = 0; i < kRing; ++i) {
+            if (reinit) mbar_inval(&sh.mbar[g * kRing + i]);
+            mbar_init(&sh.mbar[g * kRing + i], 1);
+        }
     }
-    handoff_init(&sh.w[g], false);
-    if (tid < 8) sh.ctl[tid] = 0;
-    if (tid < W) sh.done[tid] = 0;
-    if (tid == 0) tma_prefetch_desc(&mTld), tma_prefetch_desc(&mTrow), tma_prefetch_desc(&mLrow);
+    handoff_init(&sh.w[g], reinit);
+    if (tid < 7) sh.ctl[tid] = 0;  // ctl[7] carries the job number of a persistent CTA
+    if (tid < Wb) sh.done[tid] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     __syncthreads();
+}
+
+// One shot (forward, residuals, adjoint) by a CTA whose warps 0..Wg-1 take
+// the strips (further warps of the CTA only join its barriers and the
+// cell-parallel loops).
+template <int MODE>
+__device__ __noinline__ void run_shot(const ShotParams &P, const CUtensorMap *pTld, const CUtensorMap *pTrow,
+                                      const CUtensorMap *pLrow, int z, const CtaShared &sh, int Wg) {
+    const int W = Wg;
+    const int tid = threadIdx.x, g = tid >> 5, l = tid & 31;
+    if (tid == 0) tma_prefetch_desc(pTld), tma_prefetch_desc(pTrow), tma_prefetch_desc(pLrow);
 
     Warp w;
     w.g = g;
@@ -949,11 +962,11 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
                 __syncthreads();
             }
             float acc = 0.f, mag = 0.f;
-            RZ_SWEEP(+1, +1, false, MODE, &mTrow);
+            RZ_SWEEP(+1, +1, false, MODE, pTrow);
             if (pass == 0) stamp(P, z, 5);
-            RZ_SWEEP(-1, +1, false, MODE, &mTrow);
-            RZ_SWEEP(-1, -1, false, MODE, &mTrow);
-            RZ_SWEEP(+1, -1, false, MODE, &mTrow);
+            RZ_SWEEP(-1, +1, false, MODE, pTrow);
+            RZ_SWEEP(-1, -1, false, MODE, pTrow);
+            RZ_SWEEP(+1, -1, false, MODE, pTrow);
             if (seq.pipelined) __syncthreads();
             ++pass;
             ++swept;
@@ -1045,7 +1058,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
     if (P.exact) {
         exact_prepare(P, z, T, L);
     } else {
-        for (int s = g; s < P.nstrips; s += W) relayout_strip<0>(P, w, &mTld, s);
+        for (int s = g; s < P.nstrips && g < W; s += W) relayout_strip<0>(P, w, pTld, s);
         // lambda: 0 on the frame, 10*TIME inside, residuals at receiver cells
         const float linit = (float)(10.0 * (double)P.time);
         for (int c = tid; c < n; c += blockDim.x) {
@@ -1077,17 +1090,17 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
         float acc = 0.f, mag = 0.f;
         if (P.exact) {
             // same four orderings as the Leung-Qian sweeps (eikonal_adj.c:43-46)
-            RZ_SWEEP(+1, +1, true, kModeExact, &mLrow);
+            RZ_SWEEP(+1, +1, true, kModeExact, pLrow);
             if (pass == 0) stamp(P, z, 6);
-            RZ_SWEEP(+1, -1, true, kModeExact, &mLrow);
-            RZ_SWEEP(-1, +1, true, kModeExact, &mLrow);
-            RZ_SWEEP(-1, -1, true, kModeExact, &mLrow);
+            RZ_SWEEP(+1, -1, true, kModeExact, pLrow);
+            RZ_SWEEP(-1, +1, true, kModeExact, pLrow);
+            RZ_SWEEP(-1, -1, true, kModeExact, pLrow);
         } else {
-            RZ_SWEEP(+1, +1, true, MODE, &mLrow);
+            RZ_SWEEP(+1, +1, true, MODE, pLrow);
             if (pass == 0) stamp(P, z, 6);
-            RZ_SWEEP(+1, -1, true, MODE, &mLrow);
-            RZ_SWEEP(-1, +1, true, MODE, &mLrow);
-            RZ_SWEEP(-1, -1, true, MODE, &mLrow);
+            RZ_SWEEP(+1, -1, true, MODE, pLrow);
+            RZ_SWEEP(-1, +1, true, MODE, pLrow);
+            RZ_SWEEP(-1, -1, true, MODE, pLrow);
         }
         if (seq.pipelined) __syncthreads();
         ++pass;
@@ -1120,11 +1133,66 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1)
     if (tid == 0) atomicOr(&P.status[z], cta_err);
 }
 
+// one CTA per shot
+template <int MODE>
+__global__ void __launch_bounds__(kMaxWarps * 32, 1)
+    shot_kernel(const __grid_constant__ ShotParams P, const __grid_constant__ CUtensorMap mTld,
+                const __grid_constant__ CUtensorMap mTrow, const __grid_constant__ CUtensorMap mLrow) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int Wb = blockDim.x >> 5;
+    if ((int)blockIdx.x >= P.nshots) return;
+    const CtaShared sh = carve_smem(smem_raw, Wb);
+    init_cta(sh, Wb, false);
+    run_shot<MODE>(P, &mTld, &mTrow, &mLrow, blockIdx.x, sh, Wb);
+}
+
+// Persistent CTAs over the shots of several grids: each CTA takes the next
+// job (grid, shot) from a counter, in the host's largest-first order, until
+// none is left.
+template <int MODE>
+__global__ void __launch_bounds__(kMaxWarps * 32, 1) multi_shot_kernel(const __grid_constant__ MultiParams M) {
+    extern __shared__ __align__(128) unsigned char smem_raw[];
+    const int Wb = blockDim.x >> 5;
+    const CtaShared sh = carve_smem(smem_raw, Wb);
+    bool first = true;
+    for (;;) {
+        if (threadIdx.x == 0) sh.ctl[7] = atomicAdd(M.counter, 1);
+        __syncthreads();
+        const int job = sh.ctl[7];
+        if (job >= M.njobs) break;
+        const int2 jb = M.jobs[job];
+        init_cta(sh, Wb, !first);
+        first = false;
+        const MultiGrid &G = M.grid[jb.x];
+        run_shot<MODE>(G.P, &G.tld, &G.trow, &G.lrow, jb.y, sh, G.W);
+        __syncthreads();
+    }
+}
+
+int shot_kernel_warps(int nstrips) {
+    const int nb = (nstrips + kMaxWarps - 1) / kMaxWarps;  // bands per sweep
+    return (nstrips + nb - 1) / nb;                         // warps per CTA, bands balanced
+}
+
+cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int Wb, int *nctas, cudaStream_t st) {
+    const size_t smem = shot_kernel_smem(Wb);
+    int dev = 0, sms = 0, per_sm = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess) return e;
+    auto kern = mode == kModeReference ? multi_shot_kernel<kModeReference> : multi_shot_kernel<kModeFast>;
+    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * Wb, smem))) return e;
+    const int n = std::max(1, std::min(M.njobs, sms * std::max(per_sm, 1)));
+    kern<<<n, 32 * Wb, smem, st>>>(M);
+    if (nctas) *nctas = n;
+    return cudaGetLastError();
+}
+
 cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const CUtensorMap &mTld, const CUtensorMap &mTrow,
                                const CUtensorMap &mLrow, cudaStream_t st) {
     if (P.nstrips < 1) return cudaErrorInvalidValue;
-    const int nb = (P.nstrips + kMaxWarps - 1) / kMaxWarps;  // bands per sweep
-    const int W = (P.nstrips + nb - 1) / nb;                  // warps per CTA, bands balanced
+    const int W = shot_kernel_warps(P.nstrips);
     const size_t smem = shot_kernel_smem(W);
     dim3 grid(P.nshots), block(32 * W);
     cudaError_t e;

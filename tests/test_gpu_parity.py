@@ -300,3 +300,25 @@ def test_full_size_gradient_properties(R):
     S = synth.slowness(w.vp_start)
     to, _ = O.eikonal(p, S, w.srcx[0], w.srcz[0])
     assert np.array_equal(TT, to)
+
+
+@pytest.mark.parametrize("mode", ["reference", "fast"])
+def test_multi_grid_launch_equals_per_grid_calls(R, mode):
+    """One persistent launch over three grids (one of them banded, one leaving
+    warps of the CTA idle) gives every grid exactly its rz_grad_obj result."""
+    shapes = [(120, 90, 5), (60, 600, 3), (200, 40, 7)]
+    ctxs, ws, tobs, want = [], [], [], []
+    for k, (nx, ny, ns) in enumerate(shapes):
+        w = synth.small_case(300 + k, nx, ny, nshots=ns)
+        p = params(w)
+        S = synth.slowness(w.vp_true)
+        Tobs = _noisy_picks(p, w, S, ns, 40 + k)
+        ctx = make_ctx(R, w, mode=mode)
+        want.append(ctx.grad_obj(w.srcx, w.srcz, Tobs) + ([ctx.shot_info(i)[:2] for i in range(ns)],))
+        ctxs.append(ctx)
+        ws.append(w)
+        tobs.append(Tobs)
+    got = R.grad_obj_multi(ctxs, [w.srcx for w in ws], [w.srcz for w in ws], tobs)
+    for (g, l2), (gw, lw, passes), ctx, w in zip(got, want, ctxs, ws):
+        assert np.array_equal(g, gw) and l2 == lw
+        assert [ctx.shot_info(i)[:2] for i in range(w.nshots)] == passes
