@@ -108,6 +108,13 @@ int rz_set_velocity(rz_context *ctx, const float *vp, int flags);
    indices (recpos[1..2][1..ntr] of receiver.c).  Host pointers. */
 int rz_set_receivers(rz_context *ctx, int ntr, const int *recx, const int *recz);
 
+/* CUDA graphs (default on): rz_grad_obj captures its device sequence
+   (per-shot resets, shot-kernel launches, stacks, frame copy, misfit sum)
+   once and replays it while the buffers, shapes and settings it baked in are
+   unchanged; inputs are uploaded before each replay.  Results are the same
+   either way.  0 disables capture and frees the graph. */
+int rz_set_graphs(rz_context *ctx, int enable);
+
 /* Device memory the per-shot field slots (traveltimes, lambda, pass
    snapshot, skewed copies: about 28 bytes per padded cell) may occupy.
    A batch whose slots exceed it runs in chunks of as many shots as fit, in

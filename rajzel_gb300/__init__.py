@@ -80,6 +80,7 @@ def load_library(path: str = LIB_PATH):
     lib.rz_eikonal_adj.argtypes = [vp, vp, vp, vp, vp, C.c_int]
     lib.rz_set_memory_cap.argtypes = [vp, C.c_size_t]
     lib.rz_shot_work.argtypes = [vp, C.c_int, vp, vp]
+    lib.rz_set_graphs.argtypes = [vp, C.c_int]
     lib.rz_grad_obj_multi.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_int]
     lib.rz_fatt_defaults.argtypes = [vp]
     lib.rz_fatt.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
@@ -87,7 +88,7 @@ def load_library(path: str = LIB_PATH):
     lib.rz_precond.argtypes = [vp, vp, vp, C.c_int]
     lib.rz_set_gradient.argtypes = [vp, C.c_int]
     lib.rz_backward.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
-    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_grad_obj_multi", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_misfit", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
+    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_set_graphs", "rz_grad_obj_multi", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_misfit", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
                  "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
                  "rz_eikonal_adj", "rz_shot_timeline", "rz_kernel_stats"):
         getattr(lib, name).restype = C.c_int
@@ -260,6 +261,10 @@ class Context:
         g = _f32(grad).reshape(self.ny, self.nx).copy()
         self._check(self.lib.rz_precond(self.h, C.byref(o), _ptr(g), 0), "rz_precond")
         return g
+
+    def set_graphs(self, enable: bool):
+        """Capture rz_grad_obj's device sequence as a CUDA graph and replay it (default on)."""
+        self._check(self.lib.rz_set_graphs(self.h, int(bool(enable))), "rz_set_graphs")
 
     def set_memory_cap(self, nbytes: int):
         """Bytes of device memory the per-shot field slots may use (0 = automatic)."""

@@ -81,6 +81,22 @@ struct rz_context {
     int last_first = 0;       // first shot whose fields are still in the slots
     bool last_adj = false;
 
+    // CUDA graph of the rz_grad_obj sequence, replayed while its key is unchanged
+    bool use_graphs = true;
+    bool capturing = false;
+    struct GraphKey {
+        ShotParams P0;  // parameters of the first chunk (pointers, constants)
+        int nshots, chunk, mode, kind, cap_f, flags_dev;
+        const void *gdst, *grad64, *cube, *S, *L2;
+    } gkey;
+    cudaGraph_t graph = nullptr;          // kept: its nodes name the exec's event records
+    cudaGraphExec_t gexec = nullptr;
+    std::vector<cudaGraphNode_t> gevents;  // event-record nodes around each shot-kernel launch
+    std::vector<cudaEvent_t> gcap_events;  // the events recorded at capture time
+    std::vector<cudaEvent_t> ginstalled;   // events the exec's nodes hold now
+    std::vector<cudaEvent_t> gretired;     // read by rz_kernel_stats, still installed
+    long long glaunches = 0;               // kernels per replay
+
     // persistent multi-grid launches driven by this context
     int2 *dJobs = nullptr;
     int njobs_cap = 0;
@@ -106,12 +122,16 @@ static int fail(rz_context *c, int code, const char *fmt, ...) {
     return code;
 }
 
+// a failed call's error is reported and cleared, so that it does not
+// resurface in the next call's launch check
 #define CK(call)                                                                                         \
     do {                                                                                                 \
         cudaError_t e_ = (call);                                                                         \
-        if (e_ != cudaSuccess)                                                                           \
+        if (e_ != cudaSuccess) {                                                                         \
+            (void)cudaGetLastError();                                                                    \
             return fail(c, e_ == cudaErrorMemoryAllocation ? RZ_ENOMEM : RZ_ECUDA, "%s: %s (%s:%d)", #call, \
                         cudaGetErrorString(e_), __FILE__, __LINE__);                                     \
+        }                                                                                                \
     } while (0)
 
 template <typename T>
@@ -289,7 +309,7 @@ static int ensure_cube(rz_context *c) {
     const size_t n = (size_t)c->g.nx * c->g.ny;
     std::vector<double> cube(n);
     for (size_t i = 0; i < n; ++i) cube[i] = std::pow((double)c->hS[i], 3.0);
-    CK(dalloc(&c->dCube, n));
+    if (!c->dCube) CK(dalloc(&c->dCube, n));  // kept across models (graphs hold the pointer)
     CK(cudaMemcpyAsync(c->dCube, cube.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));
     c->cube_valid = true;
@@ -417,9 +437,10 @@ static int run_batch(rz_context *c, int first, int n, bool adjoint, bool residua
     cudaEvent_t e0, e1;
     CK(cudaEventCreate(&e0));
     CK(cudaEventCreate(&e1));
-    CK(cudaEventRecord(e0, c->st));
+    const unsigned evf = c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
+    CK(cudaEventRecordWithFlags(e0, c->st, evf));
     CK(launch_shot_kernel(P, c->mode, c->mTld, c->mTrow, c->mLrow, c->st));
-    CK(cudaEventRecord(e1, c->st));
+    CK(cudaEventRecordWithFlags(e1, c->st, evf));
     c->shot_events.emplace_back(e0, e1);
     c->launches += 1;
     c->last_first = first;
@@ -447,6 +468,23 @@ static int collect_status(rz_context *c, int n) {
     int code = status_to_code(worst);
     if (code != RZ_OK) return fail(c, code, "device status bits 0x%x", worst);
     return RZ_OK;
+}
+
+static void drop_graph(rz_context *c) {
+    if (c->gexec) cudaGraphExecDestroy(c->gexec);
+    if (c->graph) cudaGraphDestroy(c->graph);
+    c->gexec = nullptr;
+    c->graph = nullptr;
+    c->gevents.clear();
+    for (auto e : c->gcap_events) cudaEventDestroy(e);
+    c->gcap_events.clear();
+    for (auto e : c->gretired) cudaEventDestroy(e);
+    c->gretired.clear();
+    c->ginstalled.clear();  // still listed for rz_kernel_stats, which frees them
+}
+
+static bool contains(const std::vector<cudaEvent_t> &v, cudaEvent_t e) {
+    return std::find(v.begin(), v.end(), e) != v.end();
 }
 
 // gradient contribution of the shots first..first+m-1 (fields in slots 0..m-1)
@@ -528,6 +566,7 @@ void rz_destroy(rz_context *c) {
     dfree(c->dMA), dfree(c->dMB), dfree(c->dGrad64);
     dfree(c->dXcH), dfree(c->dXcK), dfree(c->dXcOff), dfree(c->dXcRec);
     dfree(c->dJobs), dfree(c->dCounter);
+    drop_graph(c);
     if (c->own) cudaStreamDestroy(c->own);
     delete c;
 }
@@ -565,6 +604,7 @@ int rz_set_grid(rz_context *c, const rz_grid *g) {
         c->nstrips = nstrips;
         c->qn = skew_lines(c->nxb);
         free_batch(c);
+        dfree(c->dCube);
         c->model_set = false;
         c->rec_set = false;
         c->cube_valid = false;
@@ -767,7 +807,6 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
     if (c->mode == RZ_MODE_REFERENCE && (r = ensure_cube(c))) return r;
     const size_t nt = (size_t)nshots * c->ntr;
     if (nt) CK(cudaMemcpyAsync(c->dTobs, Tobs, nt * 4, have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
-    if ((r = reset_shots(c, nshots))) return r;
     float *gdst = grad;
     if (!have_dev(flags)) {
         if (!c->dGrad) CK(dalloc(&c->dGrad, (size_t)c->g.nx * c->g.ny));
@@ -775,20 +814,110 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
     }
     const bool exact = c->grad_kind == RZ_GRADIENT_EXACT;
     if ((c->mode == RZ_MODE_FAST || exact) && !c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
-    // chunks run in shot order; each stack continues the previous chunk's sums,
-    // so the result does not depend on the chunk size
-    for (int first = 0; first < nshots; first += chunk) {
-        const int m = nshots - first < chunk ? nshots - first : chunk;
-        if ((r = run_batch(c, first, m, true, true, false, exact))) return r;
-        if ((r = stack_chunk(c, first, m, gdst))) return r;
-    }
-    if (!exact) {
-        CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, c->st));
-        c->launches += 1;
-    }
     if (!c->dL2) CK(dalloc(&c->dL2, 1));
-    CK(launch_sum_l2(c->dl2, nshots, c->dL2, c->st));
-    c->launches += 1;
+    if ((r = ensure_div(c))) return r;
+    // the device sequence: chunks in shot order, each stack continuing the
+    // previous chunk's sums (the result does not depend on the chunk size)
+    auto sequence = [&]() -> int {
+        int q;
+        if ((q = reset_shots(c, nshots))) return q;
+        for (int first = 0; first < nshots; first += chunk) {
+            const int m = nshots - first < chunk ? nshots - first : chunk;
+            if ((q = run_batch(c, first, m, true, true, false, exact))) return q;
+            if ((q = stack_chunk(c, first, m, gdst))) return q;
+        }
+        if (!exact) {
+            CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, c->st));
+            c->launches += 1;
+        }
+        CK(launch_sum_l2(c->dl2, nshots, c->dL2, c->st));
+        c->launches += 1;
+        return RZ_OK;
+    };
+    if (!c->use_graphs) {
+        if ((r = sequence())) return r;
+    } else {
+        rz_context::GraphKey key;
+        memset(&key, 0, sizeof key);
+        fill_params(c, key.P0, 0, nshots < chunk ? nshots : chunk);
+        key.nshots = nshots, key.chunk = chunk, key.mode = c->mode, key.kind = c->grad_kind, key.cap_f = c->cap_f;
+        key.flags_dev = have_dev(flags), key.gdst = gdst, key.grad64 = c->dGrad64, key.cube = c->dCube;
+        key.S = c->dS, key.L2 = c->dL2;
+        if (!c->gexec || memcmp(&key, &c->gkey, sizeof key) != 0) {
+            drop_graph(c);
+            const size_t ev0 = c->shot_events.size();
+            const long long l0 = c->launches;
+            CK(cudaStreamBeginCapture(c->st, cudaStreamCaptureModeThreadLocal));
+            c->capturing = true;
+            r = sequence();
+            c->capturing = false;
+            cudaGraph_t graph = nullptr;
+            const cudaError_t ce = cudaStreamEndCapture(c->st, &graph);
+            // the capture's events are nodes of the graph, not recorded work
+            std::vector<cudaEvent_t> cap_ev;
+            for (size_t i = ev0; i < c->shot_events.size(); ++i)
+                cap_ev.push_back(c->shot_events[i].first), cap_ev.push_back(c->shot_events[i].second);
+            c->shot_events.resize(ev0);
+            c->glaunches = c->launches - l0;
+            c->launches = l0;
+            if (r || ce != cudaSuccess) {
+                (void)cudaGetLastError();
+                if (graph) cudaGraphDestroy(graph);
+                for (auto e : cap_ev) cudaEventDestroy(e);
+                if (r) return r;
+                return fail(c, RZ_ECUDA, "stream capture failed: %s", cudaGetErrorString(ce));
+            }
+            c->graph = graph;  // owned from here on (drop_graph frees it)
+            c->gcap_events = cap_ev;
+            size_t nn = 0;
+            CK(cudaGraphGetNodes(graph, nullptr, &nn));
+            std::vector<cudaGraphNode_t> nodes(nn);
+            CK(cudaGraphGetNodes(graph, nodes.data(), &nn));
+            c->gevents.assign(cap_ev.size(), nullptr);
+            for (auto nd : nodes) {
+                cudaGraphNodeType t;
+                CK(cudaGraphNodeGetType(nd, &t));
+                if (t != cudaGraphNodeTypeEventRecord) continue;
+                cudaEvent_t e;
+                CK(cudaGraphEventRecordNodeGetEvent(nd, &e));
+                for (size_t i = 0; i < cap_ev.size(); ++i)
+                    if (cap_ev[i] == e) c->gevents[i] = nd;
+            }
+            const cudaError_t ie = cudaGraphInstantiate(&c->gexec, graph, 0);
+            if (ie != cudaSuccess) {
+                c->gexec = nullptr;
+                (void)cudaGetLastError();
+                drop_graph(c);
+                return fail(c, RZ_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(ie));
+            }
+            c->gkey = key;
+        }
+        // fresh events for this replay's shot-kernel timings; the ones they
+        // replace are freed once rz_kernel_stats has read them
+        std::vector<cudaEvent_t> now;
+        for (size_t i = 0; i + 1 < c->gevents.size(); i += 2) {
+            cudaEvent_t e0, e1;
+            CK(cudaEventCreate(&e0));
+            CK(cudaEventCreate(&e1));
+            if (c->gevents[i]) CK(cudaGraphExecEventRecordNodeSetEvent(c->gexec, c->gevents[i], e0));
+            if (c->gevents[i + 1]) CK(cudaGraphExecEventRecordNodeSetEvent(c->gexec, c->gevents[i + 1], e1));
+            c->shot_events.emplace_back(e0, e1);
+            now.push_back(e0), now.push_back(e1);
+        }
+        for (auto e : c->gcap_events) cudaEventDestroy(e);
+        c->gcap_events.clear();
+        for (auto e : c->ginstalled)
+            if (contains(c->gretired, e)) {
+                cudaEventDestroy(e);
+                c->gretired.erase(std::find(c->gretired.begin(), c->gretired.end(), e));
+            }
+        c->ginstalled = now;
+        CK(cudaGraphLaunch(c->gexec, c->st));
+        c->launches += c->glaunches;
+        c->last_n = nshots;
+        c->last_first = nshots - ((nshots - 1) % chunk + 1);
+        c->last_adj = true;
+    }
     if (have_dev(flags)) {
         if (L2) CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
         return RZ_OK;
@@ -946,6 +1075,16 @@ int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, co
     return RZ_OK;
 }
 
+int rz_set_graphs(rz_context *c, int enable) {
+    if (!c) return RZ_EINVAL;
+    c->use_graphs = enable != 0;
+    if (!c->use_graphs) {
+        cudaSetDevice(c->device);
+        drop_graph(c);
+    }
+    return RZ_OK;
+}
+
 int rz_set_gradient(rz_context *c, int kind) {
     if (!c) return RZ_EINVAL;
     if (kind != RZ_GRADIENT_REFERENCE && kind != RZ_GRADIENT_EXACT)
@@ -1050,8 +1189,10 @@ int rz_kernel_stats(rz_context *c, long long *launches, double *shot_kernel_ms, 
         CK(cudaEventElapsedTime(&ms, pr.first, pr.second));
         tot += ms;
         ++n;
-        cudaEventDestroy(pr.first);
-        cudaEventDestroy(pr.second);
+        for (cudaEvent_t e : {pr.first, pr.second}) {
+            if (contains(c->ginstalled, e)) c->gretired.push_back(e);  // a graph node still holds it
+            else cudaEventDestroy(e);
+        }
     }
     c->shot_events.clear();
     if (launches) *launches = c->launches;

@@ -900,7 +900,7 @@ RZ_DEV void init_cta(const CtaShared &sh, int Wb, bool reinit) {
 // the strips (further warps of the CTA only join its barriers and the
 // cell-parallel loops).
 template <int MODE>
-__device__ __noinline__ void run_shot(const ShotParams &P, const CUtensorMap *pTld, const CUtensorMap *pTrow,
+__device__ __forceinline__ void run_shot(const ShotParams &P, const CUtensorMap *pTld, const CUtensorMap *pTrow,
                                       const CUtensorMap *pLrow, int z, const CtaShared &sh, int Wg) {
     const int W = Wg;
     const int tid = threadIdx.x, g = tid >> 5, l = tid & 31;

@@ -24,9 +24,12 @@ def harness(gpu_lib):
     O.build(ref=False)
     out = os.path.join(tempfile.mkdtemp(prefix="rzh"), "libharness.so")
     pkg = os.path.join(ROOT, "rajzel_gb300")
+    # the shim is compiled into the harness and bound to it (-Bsymbolic): its err(),
+    # writemod(), ... calls then reach the harness, as they reach the RAJZEL program
+    # that links it, and not the C library's err() of the loading process
     subprocess.run(["gcc", "-O2", "-fPIC", "-shared", "-I", os.path.join(ROOT, "include"), "-o", out,
-                    os.path.join(HERE, "compat", "harness.c"), "-L", pkg, "-lrajzel_compat", "-lrajzel_gb300",
-                    f"-Wl,-rpath,{pkg}", "-lm"], check=True)
+                    os.path.join(HERE, "compat", "harness.c"), os.path.join(pkg, "csrc", "rz_compat.c"),
+                    "-Wl,-Bsymbolic", "-L", pkg, "-lrajzel_gb300", f"-Wl,-rpath,{pkg}", "-lm"], check=True)
     lib = C.CDLL(out, mode=C.RTLD_GLOBAL)
     f32 = np.ctypeslib.ndpointer(np.float32, flags="C_CONTIGUOUS")
     i32 = np.ctypeslib.ndpointer(np.int32, flags="C_CONTIGUOUS")

@@ -322,3 +322,32 @@ def test_multi_grid_launch_equals_per_grid_calls(R, mode):
     for (g, l2), (gw, lw, passes), ctx, w in zip(got, want, ctxs, ws):
         assert np.array_equal(g, gw) and l2 == lw
         assert [ctx.shot_info(i)[:2] for i in range(w.nshots)] == passes
+
+
+@pytest.mark.parametrize("mode", ["reference", "fast"])
+def test_graph_replay_equals_direct_launches(R, mode):
+    """rz_grad_obj replays one captured graph across calls with new sources,
+    picks and models; every result equals the uncaptured path."""
+    w = synth.small_case(91, 110, 80, nshots=4)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    direct = make_ctx(R, w, mode=mode)
+    direct.set_graphs(False)
+    graph = make_ctx(R, w, mode=mode)
+    rng = np.random.default_rng(5)
+    for call in range(3):
+        sx = (w.srcx + rng.uniform(-30, 30, 4)).clip(10.0, (w.nx - 1) * w.dh).astype(np.float32)
+        Tobs = _noisy_picks(p, w, S, 4, 60 + call)
+        vp = (w.vp_true * np.float32(1.0 + 0.01 * call)).astype(np.float32)
+        for ctx in (direct, graph):
+            ctx.set_velocity(vp)
+        g0, l0 = direct.grad_obj(sx, w.srcz, Tobs)
+        g1, l1 = graph.grad_obj(sx, w.srcz, Tobs)
+        assert np.array_equal(g0, g1) and l0 == l1
+        assert [graph.shot_info(i) for i in range(4)] == [direct.shot_info(i) for i in range(4)]
+        f0 = direct.shot_fields(3)
+        f1 = graph.shot_fields(3)
+        assert all(np.array_equal(a, b) for a, b in zip(f0, f1))
+        # timings are read between replays, as bench.py does
+        launches, ms, calls = graph.kernel_stats()
+        assert calls == 1 and ms > 0
