@@ -223,6 +223,8 @@ def run_gpu_arm(args, rank, world, local_rank):
     def step():
         ctx.grad_obj_device(w.srcx, w.srcz, tobs_d.data_ptr(), grad_d.data_ptr(), l2_d.data_ptr())
 
+    tuned = ctx.autotune(w.srcx, w.srcz, Tobs)  # band width for this batch (set-up, not timed)
+
     for _ in range(max(args.warmup, 3)):
         step()
     torch.cuda.synchronize()
@@ -336,6 +338,7 @@ def run_gpu_arm(args, rank, world, local_rank):
                                "how": f"same kernels, one shot per launch, {nplain} shots, synchronised"},
         "batched_over_plain": value / plain_value,
         "gpu_launches": int(launches1 - launches0),
+        "autotune": tuned, "cuda_graphs": True,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)

@@ -108,6 +108,18 @@ int rz_set_velocity(rz_context *ctx, const float *vp, int flags);
    indices (recpos[1..2][1..ntr] of receiver.c).  Host pointers. */
 int rz_set_receivers(rz_context *ctx, int ntr, const int *recx, const int *recz);
 
+/* Autotuner (no counterpart in the reference): runs rz_grad_obj on the
+   caller's batch once per candidate band width -- warps per CTA, i.e. strips
+   swept together, the balanced width for the fewest bands of <= 16 strips
+   and for one and two more bands -- times each with CUDA events, and keeps
+   the fastest for later rz_grad_obj calls with the same number of shots,
+   mode and gradient kind.  The width changes no result.  Arguments as
+   rz_grad_obj (grad receives the gradient); best_warps / best_ms (may be
+   NULL) the choice; cand_warps / cand_ms [*ncand] (may be NULL) every
+   candidate, *ncand set to their number. */
+int rz_autotune(rz_context *ctx, int nshots, const float *srcx, const float *srcz, const float *Tobs, float *grad,
+                int flags, int *best_warps, double *best_ms, int *cand_warps, double *cand_ms, int *ncand);
+
 /* CUDA graphs (default on): rz_grad_obj captures its device sequence
    (per-shot resets, shot-kernel launches, stacks, frame copy, misfit sum)
    once and replays it while the buffers, shapes and settings it baked in are

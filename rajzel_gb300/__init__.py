@@ -81,6 +81,7 @@ def load_library(path: str = LIB_PATH):
     lib.rz_set_memory_cap.argtypes = [vp, C.c_size_t]
     lib.rz_shot_work.argtypes = [vp, C.c_int, vp, vp]
     lib.rz_set_graphs.argtypes = [vp, C.c_int]
+    lib.rz_autotune.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int, vp, vp, vp, vp, vp]
     lib.rz_grad_obj_multi.argtypes = [C.c_int, vp, vp, vp, vp, vp, vp, vp, C.c_int]
     lib.rz_fatt_defaults.argtypes = [vp]
     lib.rz_fatt.argtypes = [vp, vp, C.c_int, vp, vp, vp, vp, vp, vp, vp, vp]
@@ -88,7 +89,7 @@ def load_library(path: str = LIB_PATH):
     lib.rz_precond.argtypes = [vp, vp, vp, C.c_int]
     lib.rz_set_gradient.argtypes = [vp, C.c_int]
     lib.rz_backward.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
-    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_set_graphs", "rz_grad_obj_multi", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_misfit", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
+    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_set_graphs", "rz_autotune", "rz_grad_obj_multi", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_misfit", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
                  "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
                  "rz_eikonal_adj", "rz_shot_timeline", "rz_kernel_stats"):
         getattr(lib, name).restype = C.c_int
@@ -261,6 +262,18 @@ class Context:
         g = _f32(grad).reshape(self.ny, self.nx).copy()
         self._check(self.lib.rz_precond(self.h, C.byref(o), _ptr(g), 0), "rz_precond")
         return g
+
+    def autotune(self, srcx, srcz, Tobs):
+        """rz_autotune on this batch: {'warps': best, 'ms': time, 'candidates': {warps: ms}}."""
+        srcx, srcz = _f32(srcx), _f32(srcz)
+        n = len(srcx)
+        Tobs = _f32(Tobs).reshape(n, self.ntr) if self.ntr else np.zeros((n, 1), np.float32)
+        grad = np.empty((self.ny, self.nx), np.float32)
+        best, ms = C.c_int(0), C.c_double(0.0)
+        cw, cm, nc = (C.c_int * 8)(), (C.c_double * 8)(), C.c_int(8)
+        self._check(self.lib.rz_autotune(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(Tobs), _ptr(grad), 0, C.byref(best),
+                                         C.byref(ms), cw, cm, C.byref(nc)), "rz_autotune")
+        return {"warps": best.value, "ms": ms.value, "candidates": {cw[i]: cm[i] for i in range(min(nc.value, 8))}}
 
     def set_graphs(self, enable: bool):
         """Capture rz_grad_obj's device sequence as a CUDA graph and replay it (default on)."""

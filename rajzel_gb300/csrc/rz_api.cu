@@ -15,6 +15,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <array>
 #include <map>
 #include <string>
 #include <vector>
@@ -81,12 +82,18 @@ struct rz_context {
     int last_first = 0;       // first shot whose fields are still in the slots
     bool last_adj = false;
 
+    // band width (warps per CTA) of the shot-kernel launches: 0 = balanced
+    // default; rz_autotune records the fastest per (shots, mode, gradient kind)
+    int warps = 0;
+    bool tuning = false;
+    std::map<std::array<int, 3>, int> tuned;
+
     // CUDA graph of the rz_grad_obj sequence, replayed while its key is unchanged
     bool use_graphs = true;
     bool capturing = false;
     struct GraphKey {
         ShotParams P0;  // parameters of the first chunk (pointers, constants)
-        int nshots, chunk, mode, kind, cap_f, flags_dev;
+        int nshots, chunk, mode, kind, cap_f, flags_dev, warps;
         const void *gdst, *grad64, *cube, *S, *L2;
     } gkey;
     cudaGraph_t graph = nullptr;          // kept: its nodes name the exec's event records
@@ -439,7 +446,7 @@ static int run_batch(rz_context *c, int first, int n, bool adjoint, bool residua
     CK(cudaEventCreate(&e1));
     const unsigned evf = c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     CK(cudaEventRecordWithFlags(e0, c->st, evf));
-    CK(launch_shot_kernel(P, c->mode, c->mTld, c->mTrow, c->mLrow, c->st));
+    CK(launch_shot_kernel(P, c->mode, c->mTld, c->mTrow, c->mLrow, c->st, c->warps));
     CK(cudaEventRecordWithFlags(e1, c->st, evf));
     c->shot_events.emplace_back(e0, e1);
     c->launches += 1;
@@ -816,6 +823,10 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
     if ((c->mode == RZ_MODE_FAST || exact) && !c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
     if (!c->dL2) CK(dalloc(&c->dL2, 1));
     if ((r = ensure_div(c))) return r;
+    if (!c->tuning) {
+        auto it = c->tuned.find({nshots, c->mode, c->grad_kind});
+        c->warps = it != c->tuned.end() ? it->second : 0;
+    }
     // the device sequence: chunks in shot order, each stack continuing the
     // previous chunk's sums (the result does not depend on the chunk size)
     auto sequence = [&]() -> int {
@@ -842,7 +853,7 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
         fill_params(c, key.P0, 0, nshots < chunk ? nshots : chunk);
         key.nshots = nshots, key.chunk = chunk, key.mode = c->mode, key.kind = c->grad_kind, key.cap_f = c->cap_f;
         key.flags_dev = have_dev(flags), key.gdst = gdst, key.grad64 = c->dGrad64, key.cube = c->dCube;
-        key.S = c->dS, key.L2 = c->dL2;
+        key.S = c->dS, key.L2 = c->dL2, key.warps = c->warps;
         if (!c->gexec || memcmp(&key, &c->gkey, sizeof key) != 0) {
             drop_graph(c);
             const size_t ev0 = c->shot_events.size();
@@ -1072,6 +1083,59 @@ int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, co
     if (have_dev(flags)) return RZ_OK;
     for (int i = 0; i < ngrids; ++i)
         if ((r = collect_status(ctxs[i], nshots[i]))) return fail(c0, r, "grid %d: %s", i, ctxs[i]->err.c_str());
+    return RZ_OK;
+}
+
+int rz_autotune(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *Tobs, float *grad,
+                int flags, int *best_warps, double *best_ms, int *cand_warps, double *cand_ms, int *ncand) {
+    int r;
+    if ((r = ready(c, true))) return r;
+    if (nshots < 1 || !grad) return fail(c, RZ_EINVAL, "bad arguments");
+    cudaSetDevice(c->device);
+    // candidates: the balanced width for the fewest bands and one or two more bands
+    const int ns = c->nstrips, nb0 = (ns + kMaxWarps - 1) / kMaxWarps;
+    std::vector<int> cands;
+    for (int nb = nb0; nb <= nb0 + 2 && nb <= ns; ++nb) {
+        const int W = (ns + nb - 1) / nb;
+        if (std::find(cands.begin(), cands.end(), W) == cands.end()) cands.push_back(W);
+    }
+    const bool graphs = c->use_graphs;
+    c->use_graphs = false;
+    c->tuning = true;
+    double L2 = 0.0;
+    std::vector<double> ms(cands.size(), 0.0);
+    int best = 0;
+    for (size_t i = 0; i < cands.size() && !r; ++i) {
+        c->warps = cands[i];
+        cudaEvent_t e0, e1;
+        r = rz_grad_obj(c, nshots, srcx, srcz, Tobs, grad, &L2, flags);  // warm
+        if (!r && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
+            cudaEventRecord(e0, c->st);
+            r = rz_grad_obj(c, nshots, srcx, srcz, Tobs, grad, &L2, flags);
+            cudaEventRecord(e1, c->st);
+            cudaEventSynchronize(e1);
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            ms[i] = t;
+            cudaEventDestroy(e0), cudaEventDestroy(e1);
+            if (ms[i] < ms[best]) best = (int)i;
+        }
+    }
+    c->tuning = false;
+    c->use_graphs = graphs;
+    c->warps = 0;
+    if (r) return r;
+    c->tuned[{nshots, c->mode, c->grad_kind}] = cands[best];
+    if (best_warps) *best_warps = cands[best];
+    if (best_ms) *best_ms = ms[best];
+    if (ncand) {
+        const int cap = *ncand;
+        for (int i = 0; i < (int)cands.size() && i < cap; ++i) {
+            if (cand_warps) cand_warps[i] = cands[i];
+            if (cand_ms) cand_ms[i] = ms[i];
+        }
+        *ncand = (int)cands.size();
+    }
     return RZ_OK;
 }
 

@@ -118,8 +118,11 @@ int shot_kernel_warps(int nstrips);  // warps per CTA for a grid of nstrips stri
 cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int Wb, int *nctas, cudaStream_t st);
 // mapT_tile: [shots][ny][nx] traveltimes, 32x33 box (adjoint preparation);
 // mapT_row / mapL_row: traveltime / lambda, 32x1 box (the sweeps)
+// warps: warps per CTA (strips swept together per band); 0 = the balanced
+// choice of shot_kernel_warps(); a chosen value changes no result
 cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const CUtensorMap &mapT_tile, const CUtensorMap &mapT_row,
-                               const CUtensorMap &mapL_row, cudaStream_t st);
+                               const CUtensorMap &mapL_row, cudaStream_t st,
+                               int warps = 0);
 
 // launchers (rz_aux.cu)
 cudaError_t launch_skew_field(const float *src, int nx, int ny, int pitch, int nstrips, int nxb, float *dstA,

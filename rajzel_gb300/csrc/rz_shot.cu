@@ -1190,9 +1190,9 @@ cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int Wb, int
 }
 
 cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const CUtensorMap &mTld, const CUtensorMap &mTrow,
-                               const CUtensorMap &mLrow, cudaStream_t st) {
+                               const CUtensorMap &mLrow, cudaStream_t st, int warps) {
     if (P.nstrips < 1) return cudaErrorInvalidValue;
-    const int W = shot_kernel_warps(P.nstrips);
+    const int W = warps > 0 ? std::min(std::min(warps, kMaxWarps), P.nstrips) : shot_kernel_warps(P.nstrips);
     const size_t smem = shot_kernel_smem(W);
     dim3 grid(P.nshots), block(32 * W);
     cudaError_t e;

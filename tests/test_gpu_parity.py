@@ -351,3 +351,21 @@ def test_graph_replay_equals_direct_launches(R, mode):
         # timings are read between replays, as bench.py does
         launches, ms, calls = graph.kernel_stats()
         assert calls == 1 and ms > 0
+
+
+def test_autotuner_picks_a_width_that_changes_no_result(R):
+    """rz_autotune times the band-width candidates on the batch itself; the
+    chosen width is used afterwards and every width gives the same result."""
+    w = synth.small_case(17, 70, 700, nshots=3)  # 22 strips: 2, 3 or 4 bands
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    Tobs = _noisy_picks(p, w, S, 3, 71)
+    ctx = make_ctx(R, w)
+    g0, l0 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    res = ctx.autotune(w.srcx, w.srcz, Tobs)
+    assert set(res["candidates"]) == {11, 8, 6} and res["warps"] in res["candidates"]
+    assert all(ms > 0 for ms in res["candidates"].values())
+    g1, l1 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    assert np.array_equal(g0, g1) and l0 == l1
+    go, L2o, _, _, _ = O.grad_obj(p, S, w.srcx, w.srcz, w.recx, w.recz, Tobs)
+    assert np.array_equal(g1, go)
