@@ -97,8 +97,18 @@ __global__ void stack_kernel(const float *L, size_t fstride, int nshots, const d
         if (interior) {
             const float sv = S[(size_t)k * nx + h];
             const double cb = (double)sv * (double)sv * (double)sv;
-            for (int z = 0; z < nshots; ++z) acc += (double)__ldg(L + (size_t)z * fstride + o);
-            acc *= cb;
+            // four independent sums keep four shots' loads in flight per thread
+            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+            int z = 0;
+            for (; z + 3 < nshots; z += 4) {
+                const float *q = L + (size_t)z * fstride + o;
+                a0 += (double)__ldg(q);
+                a1 += (double)__ldg(q + fstride);
+                a2 += (double)__ldg(q + 2 * fstride);
+                a3 += (double)__ldg(q + 3 * fstride);
+            }
+            for (; z < nshots; ++z) a0 += (double)__ldg(L + (size_t)z * fstride + o);
+            acc = ((a0 + a1) + (a2 + a3)) * cb;
         }
         if (accumulate && grad64) acc += grad64[og];
         if (grad64) grad64[og] = acc;
