@@ -72,6 +72,11 @@ int main(int argc, char **argv) {
     rz_par P;
     io(rz_read_par(argv[1], &P));
     if (P.N_STREAMER > 0) die("receivers", "towed-streamer geometry (N_STREAMER > 0) is not supported");
+    if (P.INVMAT == 1 && (P.SWS_TAPER_GRAD_VERT || P.SWS_TAPER_GRAD_SOURCES || P.SWS_TAPER_CIRCULAR_PER_SHOT ||
+                          P.SWS_TAPER_FILE))
+        die("FATT", "only the horizontal gradient taper (SWS_TAPER_GRAD_HOR) is built");
+    if (P.INVMAT == 1 && (P.GRAD_FILTER || P.MODEL_FILTER))
+        die("FATT", "GRAD_FILTER and MODEL_FILTER are not built");
 
     int ntr = 0, nshots = 0;
     io(rz_read_receivers(P.REC_FILE, P.DH, P.REFREC, &ntr, NULL, NULL, 0));

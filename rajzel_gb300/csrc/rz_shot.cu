@@ -735,12 +735,32 @@ __device__ __noinline__ bool adjoint_is_fixpoint(const ShotParams &P, const floa
     return !__syncthreads_or(change);
 }
 
+// whole padded rows, a warp per row, 16-byte accesses (rows are 128-byte aligned)
 RZ_DEV void copy_field(const ShotParams &P, const float *src, float *dst) {
-    const int n = P.nx * P.ny;
-    for (int c = threadIdx.x; c < n; c += blockDim.x) {
-        int k = c / P.nx, h = c - k * P.nx;
-        size_t o = (size_t)k * P.nxp + h;
-        dst[o] = __ldcg(src + o);
+    const int W = blockDim.x >> 5, g = threadIdx.x >> 5, l = threadIdx.x & 31, nq = P.nxp >> 2;
+    for (int k = g; k < P.ny; k += W) {
+        const float4 *a = reinterpret_cast<const float4 *>(src + (size_t)k * P.nxp);
+        float4 *b = reinterpret_cast<float4 *>(dst + (size_t)k * P.nxp);
+        for (int q = l; q < nq; q += 32) b[q] = __ldcg(a + q);
+    }
+}
+
+// F := v on every padded row; with frame0 the frame (rows 0 and ny-1,
+// columns 0 and nx-1) is 0 instead
+RZ_DEV void fill_field(const ShotParams &P, float *F, float v, bool frame0) {
+    const int W = blockDim.x >> 5, g = threadIdx.x >> 5, l = threadIdx.x & 31, nq = P.nxp >> 2;
+    const int nx = P.nx, ny = P.ny;
+    for (int k = g; k < ny; k += W) {
+        float4 *row = reinterpret_cast<float4 *>(F + (size_t)k * P.nxp);
+        const bool zero_row = frame0 && (k == 0 || k == ny - 1);
+        for (int q = l; q < nq; q += 32) {
+            float x[4] = {v, v, v, v};
+            const int h = 4 * q;
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+                if (zero_row || (frame0 && (h + i == 0 || h + i == nx - 1))) x[i] = 0.0f;
+            row[q] = make_float4(x[0], x[1], x[2], x[3]);
+        }
     }
 }
 
@@ -844,10 +864,7 @@ __device__ __noinline__ void exact_prepare(const ShotParams &P, int z, const flo
         P.EU[(size_t)z * P.estride + (size_t)s * er + kEdgePad + col] = vu;
         P.ED[(size_t)z * P.estride + (size_t)s * er + kEdgePad + col] = vd;
     }
-    for (int c = tid; c < nx * ny; c += nthr) {
-        const int k = c / nx, h = c - k * nx;
-        L[(size_t)k * nxp + h] = 0.f;
-    }
+    fill_field(P, L, 0.0f, false);
     __syncthreads();
     for (int i = tid; i < P.nxcell; i += nthr) {
         const int h = P.xcell_h[i], k = P.xcell_k[i];
@@ -942,10 +959,9 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const CUtensorMap 
         // ---------------- forward ----------------
         const int hs = P.src_h[z], ks = P.src_k[z];
         const float tinit = (float)(2.0 * (double)P.time);  // zero_travel.c:22
-        for (int c = tid; c < n; c += blockDim.x) {
-            int k = c / P.nx, h = c - k * P.nx;
-            T[(size_t)k * P.nxp + h] = (h == hs && k == ks) ? 0.0f : tinit;
-        }
+        fill_field(P, T, tinit, false);
+        __syncthreads();
+        if (tid == 0) T[(size_t)ks * P.nxp + hs] = 0.0f;  // eikonal.c:35-36
         fence_proxy_async_global();
         __syncthreads();
 
@@ -1060,12 +1076,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const CUtensorMap 
     } else {
         for (int s = g; s < P.nstrips && g < W; s += W) relayout_strip<0>(P, w, pTld, s);
         // lambda: 0 on the frame, 10*TIME inside, residuals at receiver cells
-        const float linit = (float)(10.0 * (double)P.time);
-        for (int c = tid; c < n; c += blockDim.x) {
-            int k = c / P.nx, h = c - k * P.nx;
-            bool in = (h > 0 && h < P.nx - 1 && k > 0 && k < P.ny - 1);
-            L[(size_t)k * P.nxp + h] = in ? linit : 0.0f;
-        }
+        fill_field(P, L, (float)(10.0 * (double)P.time), true);
         __syncthreads();
         for (int i = tid; i < P.nrcell; i += blockDim.x)
             L[(size_t)P.rcell_k[i] * P.nxp + P.rcell_h[i]] = P.Tres[(size_t)z * P.ntr + P.rcell_rec[i]];
