@@ -46,6 +46,7 @@ struct rz_context {
     // model
     bool model_set = false;
     float *dS = nullptr, *dSA = nullptr, *dSB = nullptr, *dVp = nullptr;
+    float *dSp = nullptr;  // slowness in rows of nxp floats (fixpoint checks)
     double *dCube = nullptr;
     bool cube_valid = false;
     std::vector<float> hS;
@@ -66,7 +67,7 @@ struct rz_context {
           *dED = nullptr;
     float *dWZA = nullptr, *dWZB = nullptr, *dRA = nullptr, *dRB = nullptr;  // exact adjoint only
     bool fields_exact = false;
-    CUtensorMap mTld{}, mTrow{}, mLrow{};
+    ShotMaps maps{};  // tensor maps of the field buffers and the row-pitched slowness
     int grad_kind = RZ_GRADIENT_REFERENCE;
     // per-shot scalars and receiver arrays, sized for the whole batch
     int cap_s = 0;
@@ -174,13 +175,13 @@ static EncodeTiledFn encode_fn() {
     return fn;
 }
 
-// 3-D map over [cap][ny][nxp] float fields, logical extent [cap][ny][nx].
-static int make_map(rz_context *c, CUtensorMap *m, float *base, int box_rows) {
+// 3-D map over [depth][ny][nxp] float fields, logical extent [depth][ny][nx]
+static int make_map(rz_context *c, CUtensorMap *m, float *base, int depth, int box_cols, int box_rows) {
     EncodeTiledFn enc = encode_fn();
     if (!enc) return fail(c, RZ_ECUDA, "cuTensorMapEncodeTiled entry point unavailable");
-    cuuint64_t dims[3] = {(cuuint64_t)c->g.nx, (cuuint64_t)c->g.ny, (cuuint64_t)c->cap_f};
+    cuuint64_t dims[3] = {(cuuint64_t)c->g.nx, (cuuint64_t)c->g.ny, (cuuint64_t)depth};
     cuuint64_t strides[2] = {(cuuint64_t)c->nxp * 4, (cuuint64_t)c->nxp * c->g.ny * 4};
-    cuuint32_t box[3] = {(cuuint32_t)kBlk, (cuuint32_t)box_rows, 1};
+    cuuint32_t box[3] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -241,9 +242,11 @@ static int ensure_fields(rz_context *c, int n) {
     }
     c->cap_f = n;
     int r;
-    if ((r = make_map(c, &c->mTld, c->dT, kBoxRows))) return r;
-    if ((r = make_map(c, &c->mTrow, c->dT, 1))) return r;
-    if ((r = make_map(c, &c->mLrow, c->dL, 1))) return r;
+    if ((r = make_map(c, &c->maps.tld, c->dT, n, kBlk, kBoxRows))) return r;
+    if ((r = make_map(c, &c->maps.trow, c->dT, n, kBlk, 1))) return r;
+    if ((r = make_map(c, &c->maps.lrow, c->dL, n, kBlk, 1))) return r;
+    if ((r = make_map(c, &c->maps.tchk, c->dT, n, kCheckCols, kCheckBoxRows))) return r;
+    if ((r = make_map(c, &c->maps.lchk, c->dL, n, kCheckCols, kCheckBoxRows))) return r;
     return RZ_OK;
 }
 
@@ -446,7 +449,7 @@ static int run_batch(rz_context *c, int first, int n, bool adjoint, bool residua
     CK(cudaEventCreate(&e1));
     const unsigned evf = c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     CK(cudaEventRecordWithFlags(e0, c->st, evf));
-    CK(launch_shot_kernel(P, c->mode, c->mTld, c->mTrow, c->mLrow, c->st, c->warps));
+    CK(launch_shot_kernel(P, c->mode, c->maps, c->st, c->warps));
     CK(cudaEventRecordWithFlags(e1, c->st, evf));
     c->shot_events.emplace_back(e0, e1);
     c->launches += 1;
@@ -568,6 +571,7 @@ void rz_destroy(rz_context *c) {
     free_batch(c);
     for (auto &pr : c->shot_events) cudaEventDestroy(pr.first), cudaEventDestroy(pr.second);
     dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dVp), dfree(c->dCube), dfree(c->dGrad), dfree(c->dL2);
+    dfree(c->dSp);
     dfree(c->dRecH), dfree(c->dRecK), dfree(c->dRcH), dfree(c->dRcK), dfree(c->dRcRec), dfree(c->dSkip);
     dfree(c->dSkipP);
     dfree(c->dMA), dfree(c->dMB), dfree(c->dGrad64);
@@ -627,6 +631,8 @@ static int set_model_common(rz_context *c) {
         CK(dalloc(&c->dSB, skew));
     }
     CK(launch_skew_field(c->dS, nx, ny, nx, c->nstrips, c->nxb, c->dSA, c->dSB, c->st));
+    CK(cudaMemcpy2DAsync(c->dSp, (size_t)c->nxp * 4, c->dS, (size_t)nx * 4, (size_t)nx * 4, ny,
+                         cudaMemcpyDeviceToDevice, c->st));
     c->hS.resize((size_t)nx * ny);
     CK(cudaMemcpyAsync(c->hS.data(), c->dS, (size_t)nx * ny * 4, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
@@ -643,6 +649,12 @@ static int set_model_common(rz_context *c) {
 static int alloc_model(rz_context *c) {
     const size_t n = (size_t)c->g.nx * c->g.ny;
     if (!c->dS) CK(dalloc(&c->dS, n));
+    if (!c->dSp) {
+        CK(dalloc(&c->dSp, (size_t)c->g.ny * c->nxp));
+        CK(cudaMemsetAsync(c->dSp, 0, (size_t)c->g.ny * c->nxp * 4, c->st));
+        int r;
+        if ((r = make_map(c, &c->maps.schk, c->dSp, 1, 128, kCheckBoxRows))) return r;
+    }
     return RZ_OK;
 }
 
@@ -652,7 +664,7 @@ int rz_set_slowness(rz_context *c, const float *S, int flags) {
     cudaSetDevice(c->device);
     // allocations follow the grid; they are dropped when the shape changes
     if (c->dS && !c->model_set) {
-        dfree(c->dS), dfree(c->dSA), dfree(c->dSB);
+        dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dSp);
     }
     int r;
     if ((r = alloc_model(c))) return r;
@@ -666,7 +678,7 @@ int rz_set_velocity(rz_context *c, const float *vp, int flags) {
     if (!c->grid_set) return fail(c, RZ_ESTATE, "rz_set_grid first");
     cudaSetDevice(c->device);
     if (c->dS && !c->model_set) {
-        dfree(c->dS), dfree(c->dSA), dfree(c->dSB);
+        dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dSp);
     }
     int r;
     if ((r = alloc_model(c))) return r;
@@ -1027,9 +1039,7 @@ int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, co
         fill_params(c, G.P, 0, n);
         G.P.do_residual = 1;
         G.P.do_adjoint = 1;
-        G.tld = c->mTld;
-        G.trow = c->mTrow;
-        G.lrow = c->mLrow;
+        G.maps = c->maps;
         G.W = shot_kernel_warps(c->nstrips);
         Wb = std::max(Wb, G.W);
         const long cost = (long)c->g.ny * c->nxp;  // cells per shot: the larger grids go first

@@ -155,6 +155,13 @@ RZ_DEV void tma_store_3d_a(const CUtensorMap *map, int x, int y, int z, uint32_t
                  "r"(x), "r"(y), "r"(z), "r"(smem_src)
                  : "memory");
 }
+// untiled bulk copy global -> shared (16-byte aligned addresses, size a multiple of 16)
+RZ_DEV void bulk_load_a(uint32_t smem_dst, const void *src, uint32_t bytes, uint32_t bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_dst),
+                 "l"(src), "r"(bytes), "r"(bar)
+                 : "memory");
+}
 RZ_DEV void mbar_arrive_expect_tx_a(uint32_t bar, uint32_t bytes) {
     asm volatile("mbarrier.arrive.expect_tx.release.cta.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
                  : "memory");

@@ -97,10 +97,23 @@ struct ShotParams {
     unsigned long long *timeline;           // [nshots][kTimelineSlots] ns stamps, or null
 };
 
+// Tensor maps of a launch.  Field maps cover [shots][ny][nxp] floats with
+// logical extent [shots][ny][nx]:
+//   tld  traveltime, 32 x kBoxRows box (adjoint preparation)
+//   trow traveltime, 32 x 1 box (forward sweeps)
+//   lrow lambda, 32 x 1 box (adjoint sweeps)
+//   tchk traveltime, 136 x 4 box (fixpoint checks)
+//   lchk lambda, 136 x 4 box (adjoint fixpoint check)
+//   schk slowness in rows of nxp floats [1][ny][nxp], 128 x 4 box (forward check)
+constexpr int kCheckCols = 136, kCheckBoxRows = 4;  // box of tchk / lchk
+struct ShotMaps {
+    CUtensorMap tld, trow, lrow, tchk, lchk, schk;
+};
+
 // several grids in one persistent launch
 constexpr int kMaxGrids = 8;
 struct MultiGrid {
-    CUtensorMap tld, trow, lrow;  // as for launch_shot_kernel
+    ShotMaps maps;
     ShotParams P;
     int W;                        // warps of the CTA that sweep this grid's strips
 };
@@ -114,15 +127,12 @@ struct MultiParams {
 // launchers (rz_shot.cu)
 size_t shot_kernel_smem(int nwarps);
 int shot_kernel_warps(int nstrips);  // warps per CTA for a grid of nstrips strips
-// persistent CTAs of Wb warps (Wb >= every grid's W); nctas receives the grid size
-cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int Wb, int *nctas, cudaStream_t st);
-// mapT_tile: [shots][ny][nx] traveltimes, 32x33 box (adjoint preparation);
-// mapT_row / mapL_row: traveltime / lambda, 32x1 box (the sweeps)
-// warps: warps per CTA (strips swept together per band); 0 = the balanced
-// choice of shot_kernel_warps(); a chosen value changes no result
-cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const CUtensorMap &mapT_tile, const CUtensorMap &mapT_row,
-                               const CUtensorMap &mapL_row, cudaStream_t st,
-                               int warps = 0);
+// persistent CTAs of at least W warps (W >= every grid's W); nctas receives the grid size
+cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int W, int *nctas, cudaStream_t st);
+// warps: strips swept together per band; 0 = the balanced choice of
+// shot_kernel_warps.  The CTA may hold more warps than that (they share the
+// cell-parallel phases) where this costs no occupancy; no result changes.
+cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const ShotMaps &maps, cudaStream_t st, int warps = 0);
 
 // launchers (rz_aux.cu)
 cudaError_t launch_skew_field(const float *src, int nx, int ny, int pitch, int nstrips, int nxb, float *dstA,

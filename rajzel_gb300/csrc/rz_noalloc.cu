@@ -59,7 +59,7 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-bool encode_field_map(CUtensorMap *m, float *base, int nx, int ny, int nxp, int box_rows) {
+bool encode_field_map(CUtensorMap *m, float *base, int nx, int ny, int nxp, int box_cols, int box_rows) {
     static EncodeTiledFn fn = nullptr;
     if (!fn) {
         void *p = nullptr;
@@ -72,7 +72,7 @@ bool encode_field_map(CUtensorMap *m, float *base, int nx, int ny, int nxp, int 
     }
     cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, 1};
     cuuint64_t strides[2] = {(cuuint64_t)nxp * 4, (cuuint64_t)nxp * ny * 4};
-    cuuint32_t box[3] = {(cuuint32_t)kBlk, (cuuint32_t)box_rows, 1};
+    cuuint32_t box[3] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows, 1};
     cuuint32_t estr[3] = {1, 1, 1};
     return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
               CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
@@ -104,16 +104,21 @@ extern "C" int rz_eikonal_noalloc(const rz_grid *grid, const float *S, float src
     // working space inside the static array (offsets keep 128-byte alignment)
     const int nxb = (g.nx + kBlk - 1) / kBlk, nxp = nxb * kBlk, qn = skew_lines(nxb);
     const size_t field = (size_t)g.ny * nxp, skew = (size_t)nstrips * qn * 32;
-    const size_t need = 2 * field + 2 * skew + 32;
+    const size_t need = 3 * field + 2 * skew + 32;
     if (need > kNoAllocFloats) return RZ_EUNSUPPORTED;
     float *base = nullptr;
     if (int r = scratch_address(&base)) return r;
-    float *T = base, *Told = base + field, *SA = base + 2 * field, *SB = SA + skew;
+    float *T = base, *Told = base + field, *Sp = base + 2 * field, *SA = base + 3 * field, *SB = SA + skew;
     int *src = reinterpret_cast<int *>(SB + skew);
 
-    CUtensorMap mTile, mRow;
-    if (!encode_field_map(&mTile, T, g.nx, g.ny, nxp, kBoxRows) || !encode_field_map(&mRow, T, g.nx, g.ny, nxp, 1))
+    ShotMaps M;
+    if (!encode_field_map(&M.tld, T, g.nx, g.ny, nxp, kBlk, kBoxRows) ||
+        !encode_field_map(&M.trow, T, g.nx, g.ny, nxp, kBlk, 1) ||
+        !encode_field_map(&M.tchk, T, g.nx, g.ny, nxp, kCheckCols, kCheckBoxRows) ||
+        !encode_field_map(&M.schk, Sp, g.nx, g.ny, nxp, 128, kCheckBoxRows))
         return RZ_ECUDA;
+    M.lrow = M.trow;  // no adjoint here
+    M.lchk = M.tchk;
 
     ShotParams P;
     memset(&P, 0, sizeof P);
@@ -143,9 +148,12 @@ extern "C" int rz_eikonal_noalloc(const rz_grid *grid, const float *S, float src
 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     if (launch_skew_field(S, g.nx, g.ny, g.nx, nstrips, nxb, SA, SB, st) != cudaSuccess) return RZ_ECUDA;
+    if (cudaMemcpy2DAsync(Sp, (size_t)nxp * 4, S, (size_t)g.nx * 4, (size_t)g.nx * 4, g.ny, cudaMemcpyDeviceToDevice,
+                          st) != cudaSuccess)
+        return RZ_ECUDA;
     noalloc_prologue<<<1, 1, 0, st>>>(src, hs, ks, info);
     if (cudaGetLastError() != cudaSuccess) return RZ_ECUDA;
-    if (launch_shot_kernel(P, kModeReference, mTile, mRow, mRow, st) != cudaSuccess) return RZ_ECUDA;
+    if (launch_shot_kernel(P, kModeReference, M, st) != cudaSuccess) return RZ_ECUDA;
     if (launch_copy_rows(T, nxp, TT, g.nx, g.nx, g.ny, 1, 0, 0, st) != cudaSuccess) return RZ_ECUDA;
     return RZ_OK;
 }

@@ -30,12 +30,18 @@
 
 namespace rz {
 
+constexpr int kCheckSlots = 3;  // box slots in the ring of a fixpoint check
+
 struct WarpShared {
     float ring[kRing][kSlotFloats];  // TMA tiles: 3 x 33 rows x 32 columns
     float hb[kHandoff];              // boundary row handed down by warp g-1
     uint64_t full[kGroups];          // hand-off group written (producer -> this warp)
     uint64_t empty[kGroups];         // hand-off group consumed (this warp -> producer)
+    uint64_t cbar[kCheckSlots];      // fixpoint check: box slot filled
+    uint32_t cphase;                 // fixpoint check: expected parity per slot
+    uint32_t pad[(128 - 8 * kCheckSlots - 4) / 4];
 };
+static_assert(offsetof(WarpShared, hb) == sizeof(float) * kRing * kSlotFloats, "hb follows the ring");
 static_assert(sizeof(WarpShared) % 128 == 0, "TMA destinations need 128-byte alignment");
 
 struct CtaShared {
@@ -564,175 +570,220 @@ RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold,
 // pass has zero change, so the stopping rule ends the loop after it; the
 // caller counts it without sweeping it, and every result stays the same.
 // The checks split the grid into tasks of 128 columns x kCheckRows rows.  A
-// warp walks a task top to bottom, four cells per lane; the rows stream
-// through the warp's shared-memory ring by per-thread asynchronous copies
-// (cp.async, one group per row), several rows ahead of use.  Each lane
-// copies and reads back only its own 16 bytes per row (plus a one-column
-// halo for lanes 0 and 31); neighbours across lanes come by shuffle.
-constexpr int kCheckRows = 64;
+// warp walks a task top to bottom, four cells per lane.  Lane 0 loads the
+// task's rows in boxes of kCheckBox rows by tensor-map copies into a ring of
+// three slots (one mbarrier each) in the warp's shared memory.  A box of a
+// field whose east and west neighbours are needed is kCheckHaloCols wide and
+// starts 4 columns west of the task (a 16-byte aligned start), so it carries
+// the neighbours of the task's edge cells; cells outside the grid read as the
+// fill value and are never used.  Neighbours across lanes come by shuffle.
+// Boxes rather than row copies: small bulk copies are bound by the copy
+// engine's instruction rate, and a box moves four rows per instruction.
+constexpr int kCheckRows = 64, kCheckBox = kCheckBoxRows, kCheckHaloCols = kCheckCols;
+static_assert(kCheckBox == 4 && kCheckHaloCols == 128 + 8, "box rows are indexed with j >> 2, halos are 4 columns");
+constexpr uint32_t kRowH = kCheckHaloCols * 4;  // bytes of a box row with halos
+constexpr uint32_t kRowP = 128 * 4;             // bytes of a box row without
+constexpr uint32_t kCheckSlotF = kCheckBox * (kRowH + kRowP);  // forward: T box, slowness box
+constexpr uint32_t kCheckSlotA = kCheckBox * 2 * kRowH;        // adjoint: T box, lambda box
+static_assert(kCheckSlots * kCheckSlotF <= sizeof(float) * kRing * kSlotFloats, "forward check ring");
+static_assert(kCheckSlots * kCheckSlotA <= sizeof(float) * (kRing * kSlotFloats + kHandoff),
+              "adjoint check ring (the hand-off row is idle between sweeps)");
+static_assert(kCheckSlotF % 128 == 0 && kCheckSlotA % 128 == 0, "box slots stay 128-byte aligned");
 
-RZ_DEV void cp_async16(uint32_t dst, const void *src) {
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
-}
-RZ_DEV void cp_async4(uint32_t dst, const void *src) {
-    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
-}
-RZ_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
-template <int N>
-RZ_DEV void cp_async_wait() {
-    asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
-}
 RZ_DEV float4 lds4(uint32_t a) {
     float4 v;
     asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
     return v;
 }
-RZ_DEV uint32_t lds_u32(uint32_t a) {
-    uint32_t v;
-    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
-    return v;
-}
 
-// four cells of a row with their west and east neighbours
+// four cells of a row with their west and east neighbours; the row starts
+// with the 4 halo columns, lane l's cells are at 16 + 16 l
 struct Row4 {
     float w, v[4], e;
 };
-
-// own 16 bytes at slot + 16*l, halo of lanes 0 / 31 at hw / he
-RZ_DEV Row4 ring_row4(uint32_t slot, uint32_t hw, uint32_t he, int l) {
+RZ_DEV Row4 box_row4(uint32_t row, int l) {
     Row4 r;
-    const float4 c = lds4(slot + 16u * l);
+    const float4 c = lds4(row + 16u + 16u * l);
     r.v[0] = c.x, r.v[1] = c.y, r.v[2] = c.z, r.v[3] = c.w;
     r.w = __shfl_up_sync(0xffffffffu, c.w, 1);
     r.e = __shfl_down_sync(0xffffffffu, c.x, 1);
-    if (l == 0) r.w = lds(hw);
-    if (l == 31) r.e = lds(he);
+    if (l == 0) r.w = lds(row + 12u);
+    if (l == 31) r.e = lds(row + 16u + 512u);
     return r;
 }
 
+// box ring of a check: box b of a task sits in slot b % kCheckSlots
+struct CheckRing {
+    uint32_t base, bars, abort_s, phase;
+    int err;
+    RZ_DEV void wait(int b) {
+        const int s = b % kCheckSlots;
+        if (!mbar_wait_a(bars + 8u * s, (phase >> s) & 1u, abort_s)) err |= ERR_TMA_TIMEOUT;
+        phase ^= 1u << s;
+    }
+};
+
+// returns 1 when no cell would change, plus the error flags shifted left by one.
+// mT: traveltime fields, box kCheckHaloCols x kCheckBox; mS: slowness [ny][nxp],
+// box 128 x kCheckBox; z: this shot's field.
 template <int MODE>
-__device__ __noinline__ bool forward_is_fixpoint(const ShotParams &P, const float *T, uint32_t ring_s, int *found) {
-    // slot: T [0,512), S [512,1024), T halo west/east [1024,1032)
-    constexpr int RS = 12, SLOT = 1040;
-    static_assert(RS * SLOT <= (int)sizeof(float) * kRing * kSlotFloats, "check ring exceeds the warp's ring");
-    const int nx = P.nx, ny = P.ny, nxp = P.nxp;
+__device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUtensorMap *mT, const CUtensorMap *mS,
+                                                int z, WarpShared *ws, int *found, volatile int *abort_word) {
+    const int nx = P.nx, ny = P.ny;
     const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int nch = (nx + 127) >> 7, nrb = (ny + kCheckRows - 1) / kCheckRows;
     if (threadIdx.x == 0) *found = 0;
+    fence_proxy_async_smem();  // the ring's generic accesses precede the copies
     __syncthreads();
+    CheckRing R{smem_u32(&ws->ring[0][0]), smem_u32(ws->cbar), smem_u32((const void *)abort_word), ws->cphase, 0};
     bool change = false;
     for (int task = g; task < nch * nrb && !change; task += W) {
         if (__shfl_sync(0xffffffffu, *(volatile int *)found, 0)) break;  // warp-uniform
-        const int h0 = ((task % nch) << 7) + 4 * l;
-        const int k0 = (task / nch) * kCheckRows, k1 = min(ny, k0 + kCheckRows);
-        auto slot = [&](int k) { return ring_s + (uint32_t)(((k - k0 + 1) % RS) * SLOT); };
-        auto issue = [&](int k) {  // rows k0-1 .. k1 are read; later ones commit empty groups
-            if (k <= k1) {
-                const int kk = min(max(k, 0), ny - 1);
-                const uint32_t sl = slot(k);
-                const float *tr = T + (size_t)kk * nxp;
-                if (h0 < nxp) cp_async16(sl + 16u * l, tr + h0);
-#pragma unroll
-                for (int i = 0; i < 4; ++i)
-                    if (h0 + i < nx) cp_async4(sl + 512u + 16u * l + 4u * i, P.S + (size_t)kk * nx + h0 + i);
-                if (l == 0 && h0 > 0) cp_async4(sl + 1024u, tr + h0 - 1);
-                if (l == 31 && h0 + 4 < nxp) cp_async4(sl + 1028u, tr + h0 + 4);
-            }
-            cp_async_commit();
+        const int base = (task % nch) << 7, h0 = base + 4 * l;
+        // rows k0 .. k0+kk-1; window row j is grid row k0-1+j, j = 0 .. kk+1
+        const int k0 = (task / nch) * kCheckRows, kk = min(ny - k0, kCheckRows);
+        const int nb = ((kk + 1) >> 2) + 1;
+        auto issue = [&](int b) {
+            if (b >= nb || l != 0) return;
+            const uint32_t sl = R.base + (uint32_t)(b % kCheckSlots) * kCheckSlotF;
+            const uint32_t br = R.bars + 8u * (uint32_t)(b % kCheckSlots);
+            mbar_arrive_expect_tx_a(br, kCheckSlotF);
+            tma_load_3d_a(sl, mT, base - 4, k0 - 1 + kCheckBox * b, z, br);
+            tma_load_3d_a(sl + kCheckBox * kRowH, mS, base, k0 - 1 + kCheckBox * b, 0, br);
         };
-        for (int i = 0; i < RS; ++i) issue(k0 - 1 + i);
-        for (int k = k0; k < k1; ++k) {
-            cp_async_wait<RS - 3>();  // rows up to k+1 have landed
-            const uint32_t sc = slot(k);
-            const Row4 c = ring_row4(sc, sc + 1024u, sc + 1028u, l);
-            const float4 u = lds4(slot(k - 1) + 16u * l), d = lds4(slot(k + 1) + 16u * l);
-            const float4 sv4 = lds4(sc + 512u + 16u * l);
-            const float uv[4] = {u.x, u.y, u.z, u.w}, dv[4] = {d.x, d.y, d.z, d.w};
-            const float sv[4] = {sv4.x, sv4.y, sv4.z, sv4.w};
+        auto trow = [&](int j) {
+            return R.base + (uint32_t)((j >> 2) % kCheckSlots) * kCheckSlotF + (uint32_t)(j & 3) * kRowH;
+        };
+        issue(0), issue(1), issue(2);
+        __syncwarp();
+        R.wait(0);
+        for (int b = 0; b < nb; ++b) {
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const int h = h0 + i;
-                const float own = c.v[i];
-                const float tw = h > 0 ? (i == 0 ? c.w : c.v[i - 1]) : own;
-                const float te = h < nx - 1 ? (i == 3 ? c.e : c.v[i + 1]) : own;
-                const float tn = k > 0 ? uv[i] : own, ts = k < ny - 1 ? dv[i] : own;
-                const float a = fminf(tw, te), b = fminf(tn, ts);
-                const float tt = (MODE == kModeReference) ? godunov_ref(a, b, sv[i], P.dh) : godunov_fast(a, b, sv[i], P.dh);
-                change |= (h < nx) && (tt < own);
+            for (int r = 0; r < kCheckBox; ++r) {
+                const int j = kCheckBox * b + r, k = k0 - 1 + j;
+                if (j < 1 || j > kk) continue;  // warp-uniform
+                if (r == kCheckBox - 1) R.wait(b + 1);  // holds row j+1
+                const uint32_t rc = trow(j);
+                const Row4 c = box_row4(rc, l);
+                const float4 u = lds4(trow(j - 1) + 16u + 16u * l), d = lds4(trow(j + 1) + 16u + 16u * l);
+                const float4 s4 = lds4(rc - (uint32_t)(j & 3) * kRowH + kCheckBox * kRowH + (uint32_t)(j & 3) * kRowP +
+                                       16u * l);
+                const float uv[4] = {u.x, u.y, u.z, u.w}, dv[4] = {d.x, d.y, d.z, d.w};
+                const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int h = h0 + i;
+                    const float own = c.v[i];
+                    const float tw = h > 0 ? (i == 0 ? c.w : c.v[i - 1]) : own;
+                    const float te = h < nx - 1 ? (i == 3 ? c.e : c.v[i + 1]) : own;
+                    const float tn = k > 0 ? uv[i] : own, ts = k < ny - 1 ? dv[i] : own;
+                    const float a = fminf(tw, te), bb = fminf(tn, ts);
+                    const float tt = (MODE == kModeReference) ? godunov_ref(a, bb, sv[i], P.dh)
+                                                              : godunov_fast(a, bb, sv[i], P.dh);
+                    change |= (h < nx) && (tt < own);
+                }
             }
-            issue(k - 1 + RS);  // into the slot of row k-1, no longer read
+            // box b-1 is read by no later row: box b+2 takes its slot
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (b >= 1) issue(b + 2);
         }
-        cp_async_wait<0>();
         change = __any_sync(0xffffffffu, change);
         if (change && l == 0) *(volatile int *)found = 1;
     }
-    return !__syncthreads_or(change);
+    if (l == 0) ws->cphase = R.phase;
+    fence_proxy_async_smem();  // before the next sweep's copies into the ring
+    return (__syncthreads_or(change) ? 0 : 1) | (R.err << 1);
 }
 
 // the Leung-Qian update of interior, non-receiver cells (sweep_adj.c:26-30);
-// skip is the [ny][nxp] byte map of cells the adjoint sweeps leave unchanged
+// skip is the [ny][nxp] byte map of cells the adjoint sweeps leave unchanged.
+// mT / mL: traveltime / lambda fields, box kCheckHaloCols x kCheckBox.
 template <int MODE>
-__device__ __noinline__ bool adjoint_is_fixpoint(const ShotParams &P, const float *T, const float *L, uint32_t ring_s,
-                                                 int *found) {
-    // slot: T [0,512), lambda [512,1024), skip [1024,1152), T halo [1152,1160), lambda halo [1160,1168)
-    constexpr int RS = 10, SLOT = 1168;
-    static_assert(RS * SLOT <= (int)sizeof(float) * kRing * kSlotFloats, "check ring exceeds the warp's ring");
+__device__ __noinline__ int adjoint_is_fixpoint(const ShotParams &P, const CUtensorMap *mT, const CUtensorMap *mL,
+                                                int z, WarpShared *ws, int *found, volatile int *abort_word) {
     const int nx = P.nx, ny = P.ny, nxp = P.nxp;
     const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int nch = (nx + 127) >> 7, nrb = (ny - 2 + kCheckRows - 1) / kCheckRows;
     const DivDH div{P.dh, P.dh_rcp, P.div_fast != 0};
     if (threadIdx.x == 0) *found = 0;
+    fence_proxy_async_smem();  // the ring's generic accesses precede the copies
     __syncthreads();
+    CheckRing R{smem_u32(&ws->ring[0][0]), smem_u32(ws->cbar), smem_u32((const void *)abort_word), ws->cphase, 0};
     bool change = false;
     for (int task = g; task < nch * nrb && !change; task += W) {
         if (__shfl_sync(0xffffffffu, *(volatile int *)found, 0)) break;  // warp-uniform
-        const int h0 = ((task % nch) << 7) + 4 * l;
-        const int k0 = 1 + (task / nch) * kCheckRows, k1 = min(ny - 1, k0 + kCheckRows);
-        auto slot = [&](int k) { return ring_s + (uint32_t)(((k - k0 + 1) % RS) * SLOT); };
-        auto issue = [&](int k) {
-            if (k <= k1) {
-                const uint32_t sl = slot(k);
-                const size_t o = (size_t)k * nxp;
-                if (h0 < nxp) {
-                    cp_async16(sl + 16u * l, T + o + h0);
-                    cp_async16(sl + 512u + 16u * l, L + o + h0);
-                    cp_async4(sl + 1024u + 4u * l, P.skip + o + h0);
-                }
-                if (l == 0 && h0 > 0) cp_async4(sl + 1152u, T + o + h0 - 1), cp_async4(sl + 1160u, L + o + h0 - 1);
-                if (l == 31 && h0 + 4 < nxp) cp_async4(sl + 1156u, T + o + h0 + 4), cp_async4(sl + 1164u, L + o + h0 + 4);
-            }
-            cp_async_commit();
+        const int base = (task % nch) << 7, h0 = base + 4 * l;
+        // interior rows k0 .. k0+kk-1 (k0 >= 1, k0+kk <= ny-1); window row j is grid row k0-1+j
+        const int k0 = 1 + (task / nch) * kCheckRows, kk = min(ny - 1 - k0, kCheckRows);
+        const int nb = ((kk + 1) >> 2) + 1;
+        auto issue = [&](int b) {
+            if (b >= nb || l != 0) return;
+            const uint32_t sl = R.base + (uint32_t)(b % kCheckSlots) * kCheckSlotA;
+            const uint32_t br = R.bars + 8u * (uint32_t)(b % kCheckSlots);
+            mbar_arrive_expect_tx_a(br, kCheckSlotA);
+            tma_load_3d_a(sl, mT, base - 4, k0 - 1 + kCheckBox * b, z, br);
+            tma_load_3d_a(sl + kCheckBox * kRowH, mL, base - 4, k0 - 1 + kCheckBox * b, z, br);
         };
-        for (int i = 0; i < RS; ++i) issue(k0 - 1 + i);
-        for (int k = k0; k < k1; ++k) {
-            cp_async_wait<RS - 3>();
-            const uint32_t sc = slot(k), su = slot(k - 1), sd = slot(k + 1);
-            const Row4 tc = ring_row4(sc, sc + 1152u, sc + 1156u, l);
-            const Row4 lc = ring_row4(sc + 512u, sc + 1160u, sc + 1164u, l);
-            const float4 tu = lds4(su + 16u * l), td = lds4(sd + 16u * l);
-            const float4 lu = lds4(su + 512u + 16u * l), ld = lds4(sd + 512u + 16u * l);
-            const uint32_t sk = h0 < nxp ? lds_u32(sc + 1024u + 4u * l) : 0x01010101u;
-            const float tuv[4] = {tu.x, tu.y, tu.z, tu.w}, tdv[4] = {td.x, td.y, td.z, td.w};
-            const float luv[4] = {lu.x, lu.y, lu.z, lu.w}, ldv[4] = {ld.x, ld.y, ld.z, ld.w};
+        auto trow = [&](int j) {
+            return R.base + (uint32_t)((j >> 2) % kCheckSlots) * kCheckSlotA + (uint32_t)(j & 3) * kRowH;
+        };
+        // skip words (4 cells of a lane) of the rows of a box, two boxes ahead
+        auto skip_words = [&](int b, uint32_t(&sk)[kCheckBox]) {
 #pragma unroll
-            for (int i = 0; i < 4; ++i) {
-                const float te = i == 3 ? tc.e : tc.v[i + 1], tw = i == 0 ? tc.w : tc.v[i - 1];
-                const float le = i == 3 ? lc.e : lc.v[i + 1], lw = i == 0 ? lc.w : lc.v[i - 1];
-                const float own = lc.v[i];
-                const float r = (MODE == kModeReference)
-                                    ? leung_qian_ref(tc.v[i], te, tw, tdv[i], tuv[i], le, lw, ldv[i], luv[i], own, div,
-                                                     P.eps_adj)
-                                    : leung_qian_fast(tc.v[i], te, tw, tdv[i], tuv[i], le, lw, ldv[i], luv[i], own,
-                                                      P.dh_rcp, P.eps_adj);
-                change |= (((sk >> (8 * i)) & 0xffu) == 0) && (r != own);
+            for (int r = 0; r < kCheckBox; ++r) {
+                const int j = kCheckBox * b + r;
+                sk[r] = (h0 < nxp && j >= 1 && j <= kk)
+                            ? __ldg(reinterpret_cast<const uint32_t *>(P.skip + (size_t)(k0 - 1 + j) * nxp + h0))
+                            : 0x01010101u;
             }
-            issue(k - 1 + RS);
+        };
+        uint32_t sk0[kCheckBox], sk1[kCheckBox], sk2[kCheckBox];
+        skip_words(0, sk0);
+        skip_words(1, sk1);
+        issue(0), issue(1), issue(2);
+        __syncwarp();
+        R.wait(0);
+        for (int b = 0; b < nb; ++b) {
+            skip_words(b + 2, sk2);
+#pragma unroll
+            for (int r = 0; r < kCheckBox; ++r) {
+                const int j = kCheckBox * b + r;
+                if (j < 1 || j > kk) continue;  // warp-uniform
+                if (r == kCheckBox - 1) R.wait(b + 1);  // holds row j+1
+                const uint32_t rc = trow(j), ru = trow(j - 1), rd = trow(j + 1);
+                const uint32_t lo = kCheckBox * kRowH;  // lambda box follows the T box
+                const Row4 tc = box_row4(rc, l), lc = box_row4(rc + lo, l);
+                const float4 tu = lds4(ru + 16u + 16u * l), td = lds4(rd + 16u + 16u * l);
+                const float4 lu = lds4(ru + lo + 16u + 16u * l), ld = lds4(rd + lo + 16u + 16u * l);
+                const float tuv[4] = {tu.x, tu.y, tu.z, tu.w}, tdv[4] = {td.x, td.y, td.z, td.w};
+                const float luv[4] = {lu.x, lu.y, lu.z, lu.w}, ldv[4] = {ld.x, ld.y, ld.z, ld.w};
+                const uint32_t sk = sk0[r];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const float te = i == 3 ? tc.e : tc.v[i + 1], tw = i == 0 ? tc.w : tc.v[i - 1];
+                    const float le = i == 3 ? lc.e : lc.v[i + 1], lw = i == 0 ? lc.w : lc.v[i - 1];
+                    const float own = lc.v[i];
+                    const float rr = (MODE == kModeReference)
+                                         ? leung_qian_ref(tc.v[i], te, tw, tdv[i], tuv[i], le, lw, ldv[i], luv[i], own,
+                                                          div, P.eps_adj)
+                                         : leung_qian_fast(tc.v[i], te, tw, tdv[i], tuv[i], le, lw, ldv[i], luv[i],
+                                                           own, P.dh_rcp, P.eps_adj);
+                    change |= (((sk >> (8 * i)) & 0xffu) == 0) && (rr != own);
+                }
+            }
+#pragma unroll
+            for (int r = 0; r < kCheckBox; ++r) sk0[r] = sk1[r], sk1[r] = sk2[r];
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (b >= 1) issue(b + 2);
         }
-        cp_async_wait<0>();
         change = __any_sync(0xffffffffu, change);
         if (change && l == 0) *(volatile int *)found = 1;
     }
-    return !__syncthreads_or(change);
+    if (l == 0) ws->cphase = R.phase;
+    fence_proxy_async_smem();  // before the next sweep's copies into the ring
+    return (__syncthreads_or(change) ? 0 : 1) | (R.err << 1);
 }
 
 // whole padded rows, a warp per row, 16-byte accesses (rows are 128-byte aligned)
@@ -907,6 +958,13 @@ RZ_DEV void init_cta(const CtaShared &sh, int Wb, bool reinit) {
         }
     }
     handoff_init(&sh.w[g], reinit);
+    if (l == 0) {
+        for (int i = 0; i < kCheckSlots; ++i) {
+            if (reinit) mbar_inval(&sh.w[g].cbar[i]);
+            mbar_init(&sh.w[g].cbar[i], 1);
+        }
+        sh.w[g].cphase = 0;
+    }
     if (tid < 7) sh.ctl[tid] = 0;  // ctl[7] carries the job number of a persistent CTA
     if (tid < Wb) sh.done[tid] = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -917,11 +975,14 @@ RZ_DEV void init_cta(const CtaShared &sh, int Wb, bool reinit) {
 // the strips (further warps of the CTA only join its barriers and the
 // cell-parallel loops).
 template <int MODE>
-__device__ __forceinline__ void run_shot(const ShotParams &P, const CUtensorMap *pTld, const CUtensorMap *pTrow,
-                                      const CUtensorMap *pLrow, int z, const CtaShared &sh, int Wg) {
+__device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M, int z, const CtaShared &sh, int Wg) {
     const int W = Wg;
     const int tid = threadIdx.x, g = tid >> 5, l = tid & 31;
-    if (tid == 0) tma_prefetch_desc(pTld), tma_prefetch_desc(pTrow), tma_prefetch_desc(pLrow);
+    const CUtensorMap *pTld = &M.tld, *pTrow = &M.trow, *pLrow = &M.lrow;
+    if (tid == 0) {
+        tma_prefetch_desc(pTld), tma_prefetch_desc(pTrow), tma_prefetch_desc(pLrow);
+        tma_prefetch_desc(&M.tchk), tma_prefetch_desc(&M.lchk), tma_prefetch_desc(&M.schk);
+    }
 
     Warp w;
     w.g = g;
@@ -993,9 +1054,13 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const CUtensorMap 
                 double tot = block_sum((double)acc, sh);
                 go = (tot / (double)n) >= (double)P.ttnorm;
             }
-            if (go && pass < P.max_passes && forward_is_fixpoint<MODE>(P, T, smem_u32(&sh.w[g].ring[0][0]), &sh.ctl[2])) {
-                ++pass;  // the next pass would change nothing
-                go = false;
+            if (go && pass < P.max_passes) {
+                const int fx = forward_is_fixpoint<MODE>(P, &M.tchk, &M.schk, z, &sh.w[g], &sh.ctl[2], w.abort_word);
+                w.err |= fx >> 1;
+                if (fx & 1) {
+                    ++pass;  // the next pass would change nothing
+                    go = false;
+                }
             }
         }
         if (tid == 0) P.passes_fwd[z] = pass;
@@ -1074,7 +1139,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const CUtensorMap 
     if (P.exact) {
         exact_prepare(P, z, T, L);
     } else {
-        for (int s = g; s < P.nstrips && g < W; s += W) relayout_strip<0>(P, w, pTld, s);
+        for (int s = g; s < P.nstrips; s += (int)(blockDim.x >> 5)) relayout_strip<0>(P, w, pTld, s);
         // lambda: 0 on the frame, 10*TIME inside, residuals at receiver cells
         fill_field(P, L, (float)(10.0 * (double)P.time), true);
         __syncthreads();
@@ -1130,9 +1195,13 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const CUtensorMap 
             double tot = block_sum((double)acc, sh);
             go = (tot / (double)n) >= (double)P.ttnorm;
         }
-        if (go && !P.exact && P.skip && pass < P.max_passes && adjoint_is_fixpoint<MODE>(P, T, L, smem_u32(&sh.w[g].ring[0][0]), &sh.ctl[2])) {
-            ++pass;  // the next pass would change nothing
-            go = false;
+        if (go && !P.exact && P.skip && pass < P.max_passes) {
+            const int fx = adjoint_is_fixpoint<MODE>(P, &M.tchk, &M.lchk, z, &sh.w[g], &sh.ctl[2], w.abort_word);
+            w.err |= fx >> 1;
+            if (fx & 1) {
+                ++pass;  // the next pass would change nothing
+                go = false;
+            }
         }
     }
     if (tid == 0) P.passes_adj[z] = pass;
@@ -1147,14 +1216,13 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const CUtensorMap 
 // one CTA per shot
 template <int MODE>
 __global__ void __launch_bounds__(kMaxWarps * 32, 1)
-    shot_kernel(const __grid_constant__ ShotParams P, const __grid_constant__ CUtensorMap mTld,
-                const __grid_constant__ CUtensorMap mTrow, const __grid_constant__ CUtensorMap mLrow) {
+    shot_kernel(const __grid_constant__ ShotParams P, const __grid_constant__ ShotMaps M, int Wg) {
     extern __shared__ __align__(128) unsigned char smem_raw[];
     const int Wb = blockDim.x >> 5;
     if ((int)blockIdx.x >= P.nshots) return;
     const CtaShared sh = carve_smem(smem_raw, Wb);
     init_cta(sh, Wb, false);
-    run_shot<MODE>(P, &mTld, &mTrow, &mLrow, blockIdx.x, sh, Wb);
+    run_shot<MODE>(P, M, blockIdx.x, sh, Wg);
 }
 
 // Persistent CTAs over the shots of several grids: each CTA takes the next
@@ -1175,7 +1243,7 @@ __global__ void __launch_bounds__(kMaxWarps * 32, 1) multi_shot_kernel(const __g
         init_cta(sh, Wb, !first);
         first = false;
         const MultiGrid &G = M.grid[jb.x];
-        run_shot<MODE>(G.P, &G.tld, &G.trow, &G.lrow, jb.y, sh, G.W);
+        run_shot<MODE>(G.P, G.maps, jb.y, sh, G.W);
         __syncthreads();
     }
 }
@@ -1185,14 +1253,48 @@ int shot_kernel_warps(int nstrips) {
     return (nstrips + nb - 1) / nb;                         // warps per CTA, bands balanced
 }
 
-cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int Wb, int *nctas, cudaStream_t st) {
-    const size_t smem = shot_kernel_smem(Wb);
-    int dev = 0, sms = 0, per_sm = 0;
+// Warps of a CTA whose W warps sweep: further warps idle through the sweeps
+// but share the cell-parallel phases (fixpoint checks, field fills); the CTA
+// grows while as many CTAs fit on an SM as with W warps.
+template <class K>
+static cudaError_t block_warps(K kern, int W, int *Wb_out) {
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)shot_kernel_smem(kMaxWarps));
+    int base = 0;
+    if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&base, kern, 32 * W, shot_kernel_smem(W));
+    if (e) return e;
+    int Wb = W;
+    for (int v = W + 1; v <= kMaxWarps; ++v) {
+        int o = 0;
+        if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, 32 * v, shot_kernel_smem(v)))) return e;
+        if (o < base) break;
+        Wb = v;
+    }
+    *Wb_out = Wb;
+    return cudaSuccess;
+}
+
+// block_warps, remembered per kernel and W
+template <class K>
+static cudaError_t block_warps_cached(K kern, int slot, int W, int *Wb) {
+    static int cache[4][kMaxWarps + 1];
+    if (cache[slot][W] > 0) {
+        *Wb = cache[slot][W];
+        return cudaSuccess;
+    }
+    cudaError_t e = block_warps(kern, W, Wb);
+    if (!e) cache[slot][W] = *Wb;
+    return e;
+}
+
+cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int W, int *nctas, cudaStream_t st) {
+    int dev = 0, sms = 0, per_sm = 0, Wb = W;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (e != cudaSuccess) return e;
     auto kern = mode == kModeReference ? multi_shot_kernel<kModeReference> : multi_shot_kernel<kModeFast>;
-    if ((e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem))) return e;
+    if ((e = block_warps_cached(kern, mode == kModeReference ? 2 : 3, W, &Wb))) return e;
+    const size_t smem = shot_kernel_smem(Wb);
     if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * Wb, smem))) return e;
     const int n = std::max(1, std::min(M.njobs, sms * std::max(per_sm, 1)));
     kern<<<n, 32 * Wb, smem, st>>>(M);
@@ -1200,21 +1302,17 @@ cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int Wb, int
     return cudaGetLastError();
 }
 
-cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const CUtensorMap &mTld, const CUtensorMap &mTrow,
-                               const CUtensorMap &mLrow, cudaStream_t st, int warps) {
+cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const ShotMaps &M, cudaStream_t st, int warps) {
     if (P.nstrips < 1) return cudaErrorInvalidValue;
     const int W = warps > 0 ? std::min(std::min(warps, kMaxWarps), P.nstrips) : shot_kernel_warps(P.nstrips);
-    const size_t smem = shot_kernel_smem(W);
-    dim3 grid(P.nshots), block(32 * W);
+    int Wb = W;
     cudaError_t e;
     if (mode == kModeReference) {
-        e = cudaFuncSetAttribute(shot_kernel<kModeReference>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        shot_kernel<kModeReference><<<grid, block, smem, st>>>(P, mTld, mTrow, mLrow);
+        if ((e = block_warps_cached(shot_kernel<kModeReference>, 0, W, &Wb))) return e;
+        shot_kernel<kModeReference><<<P.nshots, 32 * Wb, shot_kernel_smem(Wb), st>>>(P, M, W);
     } else {
-        e = cudaFuncSetAttribute(shot_kernel<kModeFast>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        shot_kernel<kModeFast><<<grid, block, smem, st>>>(P, mTld, mTrow, mLrow);
+        if ((e = block_warps_cached(shot_kernel<kModeFast>, 1, W, &Wb))) return e;
+        shot_kernel<kModeFast><<<P.nshots, 32 * Wb, shot_kernel_smem(Wb), st>>>(P, M, W);
     }
     return cudaGetLastError();
 }
