@@ -17,9 +17,11 @@ constexpr int kBoxRows = kStrip + 1;
 constexpr int kSlotFloats = kBoxRows * kBlk;  // 1056 floats = 4224 B
 // warp-to-warp hand-off ring (values of the strip boundary row), guarded by
 // full/empty mbarrier pairs per group of kGroup columns
-constexpr int kHandoff = 128;
+constexpr int kHandoff = 64;
 constexpr int kGroup = 8;
 constexpr int kGroups = kHandoff / kGroup;
+constexpr int kGroupsLog2 = 3;
+static_assert(kGroups == 1 << kGroupsLog2, "hand-off groups");
 constexpr int kMaxWarps = 16;
 constexpr int kTimelineSlots = 8;
 

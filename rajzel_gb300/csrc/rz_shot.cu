@@ -32,24 +32,39 @@ namespace rz {
 
 constexpr int kCheckSlots = 3;  // box slots in the ring of a fixpoint check
 
-struct WarpShared {
-    float ring[kRing][kSlotFloats];  // TMA tiles: 3 x 33 rows x 32 columns
-    float hb[kHandoff];              // boundary row handed down by warp g-1
-    uint64_t full[kGroups];          // hand-off group written (producer -> this warp)
-    uint64_t empty[kGroups];         // hand-off group consumed (this warp -> producer)
-    uint64_t cbar[kCheckSlots];      // fixpoint check: box slot filled
-    uint32_t cphase;                 // fixpoint check: expected parity per slot
-    uint32_t pad[(128 - 8 * kCheckSlots - 4) / 4];
+// Read-only stream staging.  A sweep step reads per-cell values that no
+// shared-memory ring holds: the skewed slowness or traveltime line, and in
+// the adjoint the edge-row values of lanes 0 and 31 and the skip word.  Each
+// group of 8 steps finds them in the warp's stage slot, filled by cp.async
+// during the previous group (loads into registers 8 steps ahead would leave
+// the compiler free to issue them later than written).  The slot holds 8
+// lines of 32 floats, lane 0's 8 and lane 31's 12-float window of edge
+// values, and 8 skip words.
+constexpr uint32_t kStageEdge = 1024, kStageMask = 1104;
+constexpr uint32_t kStageSlot = 1152;
+static_assert(kStageMask + 32 <= kStageSlot, "stage slot");
+
+struct alignas(128) WarpShared {
+    float ring[kRing][kSlotFloats];   // TMA tiles: 3 x 33 rows x 32 columns
+    float hb[kHandoff];               // boundary row handed down by warp g-1
+    unsigned char stage[kStageSlot];  // staged streams of one group of steps
+    uint64_t full[kGroups];           // hand-off group written (producer -> this warp)
+    uint64_t empty[kGroups];          // hand-off group consumed (this warp -> producer)
+    uint64_t cbar[kCheckSlots];       // fixpoint check: box slot filled
+    uint32_t cphase;                  // fixpoint check: expected parity per slot
 };
-static_assert(offsetof(WarpShared, hb) == sizeof(float) * kRing * kSlotFloats, "hb follows the ring");
 static_assert(sizeof(WarpShared) % 128 == 0, "TMA destinations need 128-byte alignment");
+static_assert(offsetof(WarpShared, hb) == sizeof(float) * kRing * kSlotFloats, "hb follows the ring");
+static_assert(offsetof(WarpShared, stage) == offsetof(WarpShared, hb) + sizeof(float) * kHandoff &&
+                  offsetof(WarpShared, stage) % 16 == 0,
+              "the stage slot follows hb, 16-byte aligned");
 
 struct CtaShared {
     WarpShared *w;
-    uint64_t *mbar;  // [W][kRing]
-    double *red;     // [W] reduction scratch
-    int *ctl;        // [8] broadcast words
-    int *done;       // [W] sweeps each warp has completed (pipelined sweeps)
+    uint64_t *mbar;        // [W][kRing]
+    double *red;           // [W] reduction scratch
+    int *ctl;              // [8] broadcast words
+    int *done;             // [W] sweeps each warp has completed (pipelined sweeps)
 };
 
 __host__ __device__ inline size_t align_up(size_t v, size_t a) { return (v + a - 1) / a * a; }
@@ -99,6 +114,20 @@ RZ_DEV float lds(uint32_t a) {
     return v;
 }
 RZ_DEV void sts(uint32_t a, float v) { asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v)); }
+RZ_DEV uint32_t lds_u32(uint32_t a) {
+    uint32_t v;
+    asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
+    return v;
+}
+// cp.async: 16 bytes (both addresses 16-byte aligned, L2 only) or 4 bytes
+RZ_DEV void cp_async16(uint32_t dst, const void *src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(dst), "l"(src) : "memory");
+}
+RZ_DEV void cp_async4(uint32_t dst, const void *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(dst), "l"(src) : "memory");
+}
+RZ_DEV void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+RZ_DEV void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
 
 RZ_DEV unsigned long long global_ns() {
     unsigned long long t;
@@ -238,8 +267,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     constexpr int QOFF = ADJ ? 1 : 0;    // the adjoint streams the downstream traveltime
     const float *xs;
     const uint32_t *mk = nullptr;
-    const float *ep = nullptr;
     const float *zs = nullptr, *rs = nullptr;  // exact adjoint: z weights (one column ahead), own-cell R
+    const float *ewin0 = nullptr, *ewin31 = nullptr;  // adjoint: edge values of group 0 for lanes 0 / 31
     {
         const int q0 = (DX > 0 ? 0 : ncol + 30) + QS * QOFF + kSkewFront;
         if (!ADJ) {
@@ -251,11 +280,36 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 rs = (famA ? P.RA : P.RB) + (size_t)z * P.sstride + ((size_t)s * P.qn + (q0 - QS)) * 32 + j;
             }
             mk = (famA ? P.MA : P.MB) + (size_t)s * P.qn + (q0 - QS * QOFF);
-            const float *erow = ((l == 31) == (DY > 0) ? P.ED : P.EU) + (size_t)z * P.estride +
-                                (size_t)s * edge_row(P.nxp) + kEdgePad;
-            ep = erow + (DX > 0 ? -l : ncol - 1 + l);  // column of this lane at step 0
+            // lane 0 takes its north neighbour's (dy > 0) traveltime and lambda
+            // from the row above the strip, lane 31 its south one's from the row
+            // below.  At step t lane 0 needs column t (dx > 0) or ncol-1-t of its
+            // row, lane 31 column t-31 or ncol+30-t of its own: group G reads
+            // windows of 8 and 12 floats, 16-byte aligned
+            const size_t eo = (size_t)z * P.estride + (size_t)s * edge_row(P.nxp) + kEdgePad;
+            const float *row0 = (DY > 0 ? P.EU : P.ED) + eo, *row31 = (DY > 0 ? P.ED : P.EU) + eo;
+            ewin0 = DX > 0 ? row0 : row0 + (ncol - 8);
+            ewin31 = DX > 0 ? row31 - 32 : row31 + (ncol + 20);
         }
     }
+    // staging (see kStageSlot): the values of group G of 8 steps are copied
+    // into the stage slot while group G-1 runs; every copy lies inside the
+    // padded stream it reads (lines 0 .. 32*nxb+31 of the sweep)
+    const uint32_t sg = smem_u32(w.ws->stage);
+    const int ngroups = 4 * (nxb + 1);
+    const float *xline = xs - j;  // the 32-float line of step 0
+    auto stage_issue = [&](int G) {
+        const uint32_t dst = sg;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int c = l + 32 * h, line = c >> 3, piece = c & 7;
+            cp_async16(dst + 16u * (uint32_t)c, xline + QS * 32 * (8 * G + line) + 4 * piece);
+        }
+        if (ADJ && l < 2) cp_async16(dst + kStageEdge + 16u * (uint32_t)l, ewin0 + (DX > 0 ? 8 * G : -8 * G) + 4 * l);
+        if (ADJ && l >= 2 && l < 5)
+            cp_async16(dst + kStageEdge + 16u * (uint32_t)l, ewin31 + (DX > 0 ? 8 * G : -8 * G) + 4 * (l - 2));
+        if (ADJ && !EX && l < 8) cp_async4(dst + kStageMask + 4u * (uint32_t)l, mk + QS * (8 * G + l));
+        cp_async_commit();
+    };
 
     float xq[8];
     uint32_t mq[8];
@@ -263,19 +317,12 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     float zq[8], rq[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i) {
-        if (!ADJ) {
-            xq[i] = __ldg(xs + QS * 32 * i);
-        } else {
-            xq[i] = __ldca(xs + QS * 32 * i);
-            if (EX) {
-                zq[i] = __ldca(zs + QS * 32 * i);
-                rq[i] = __ldca(rs + QS * 32 * i);
-            } else {
-                mq[i] = __ldg(mk + QS * i);
-            }
-            eq[i] = __ldca(ep + QS * i);
+        if (EX) {
+            zq[i] = __ldca(zs + QS * 32 * i);
+            rq[i] = __ldca(rs + QS * 32 * i);
         }
     }
+    stage_issue(0);
     float c_tt = 0.f, w_tt = 0.f;  // exact adjoint: x weights of this and the previous column
     float c_wz = 0.f, w_wz = 0.f;  // exact adjoint: z weights of this and the previous column
     if (ADJ) c_tt = __ldca(xs - QS * 32);
@@ -325,7 +372,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 const int G = t0 >> 3;
                 if (G < ngrp) {
                     const int Gg = G + cons_base;  // group number in this ring's lifetime
-                    if (!mbar_wait_a(full_in + 8u * (Gg & (kGroups - 1)), (Gg >> 4) & 1, abort_s)) err |= ERR_FLAG_TIMEOUT;
+                    if (!mbar_wait_a(full_in + 8u * (Gg & (kGroups - 1)), (Gg >> kGroupsLog2) & 1, abort_s)) err |= ERR_FLAG_TIMEOUT;
                     const uint32_t hb_g = hb_in + 4u * (uint32_t)((t0 + cb8) & (kHandoff - 1));
 #pragma unroll
                     for (int i = 0; i < 8; ++i) hbq[i] = lds(hb_g + 4u * i);
@@ -351,13 +398,26 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 // lane 31 starts hand-off group Gp at step t0+7 (column t0-24)
                 const int Gp = (t0 - 24) >> 3, Gpg = Gp + prod_base;
                 if (t0 >= 24 && Gpg >= kGroups && Gp < ngrp &&
-                    !mbar_wait_a(empty_out + 8u * (Gpg & (kGroups - 1)), ((Gpg >> 4) - 1) & 1, abort_s))
+                    !mbar_wait_a(empty_out + 8u * (Gpg & (kGroups - 1)), ((Gpg >> kGroupsLog2) - 1) & 1, abort_s))
                     err |= ERR_FLAG_TIMEOUT;
             }
+            {
+                const int G = t0 >> 3;
+                cp_async_wait_all();  // group G's values (copied during group G-1) have landed
+                __syncwarp();         // ... for every lane
+#pragma unroll
+                for (int ii = 0; ii < 8; ++ii) {
+                    xq[ii] = lds(sg + 128u * (uint32_t)ii + 4u * (uint32_t)j);
+                    if (ADJ) {  // only lanes 0 and 31 use their edge value
+                        const int ei = l == 0 ? (DX > 0 ? ii : 7 - ii) : 8 + (DX > 0 ? ii + 1 : 10 - ii);
+                        eq[ii] = lds(sg + kStageEdge + 4u * (uint32_t)ei);
+                    }
+                    if (ADJ && !EX) mq[ii] = lds_u32(sg + kStageMask + 4u * (uint32_t)ii);
+                }
+                __syncwarp();  // every lane has read the slot: refill it
+                if (G + 1 < ngroups) stage_issue(G + 1);
+            }
             const int u0 = t0 - l;
-            const float *xr = xs + QS * 32 * t0;
-            const uint32_t *mr = ADJ ? mk + QS * t0 : nullptr;
-            const float *er = ADJ ? ep + QS * t0 : nullptr;
             const float *zr = EX ? zs + QS * 32 * t0 : nullptr;
             const float *rr = EX ? rs + QS * 32 * t0 : nullptr;
             // ---- 8 wavefront steps, straight-line code ----
@@ -384,7 +444,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 const bool valid = (unsigned)(up - lo) < (unsigned)(hi - lo);
                 float r;
                 if (!ADJ) {
-                    xq[ii] = __ldg(xr + QS * 32 * (ii + 8));
                     const bool hasW = up > lo;
                     const bool hasE = up < hi - 1;
                     const float tw = hasW ? res_prev : own;
@@ -397,13 +456,11 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     r = fminf(own, tt);
                     r = valid ? r : own;
                 } else if (EX) {
-                    xq[ii] = __ldca(xr + QS * 32 * (ii + 8));
                     const float e_wz = zq[ii];
                     zq[ii] = __ldca(zr + QS * 32 * (ii + 8));
                     const float rcell = rq[ii];
                     rq[ii] = __ldca(rr + QS * 32 * (ii + 8));
                     const float edge = eq[ii];
-                    eq[ii] = __ldca(er + QS * (ii + 8));
                     const float e_wx = xv;  // x weight one column downstream
                     float n_wz = __shfl_up_sync(0xffffffffu, w_wz, 1);
                     float s_wz = __shfl_down_sync(0xffffffffu, e_wz, 1);
@@ -426,11 +483,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     w_wz = c_wz;
                     c_wz = e_wz;
                 } else {
-                    xq[ii] = __ldca(xr + QS * 32 * (ii + 8));
                     const uint32_t mword = mq[ii];
-                    mq[ii] = __ldg(mr + QS * (ii + 8));
                     const float edge = eq[ii];
-                    eq[ii] = __ldca(er + QS * (ii + 8));
                     const float e_tt = xv;  // traveltime one column downstream
                     float n_tt = __shfl_up_sync(0xffffffffu, w_tt, 1);
                     float s_tt = __shfl_down_sync(0xffffffffu, e_tt, 1);
@@ -586,8 +640,8 @@ constexpr uint32_t kRowP = 128 * 4;             // bytes of a box row without
 constexpr uint32_t kCheckSlotF = kCheckBox * (kRowH + kRowP);  // forward: T box, slowness box
 constexpr uint32_t kCheckSlotA = kCheckBox * 2 * kRowH;        // adjoint: T box, lambda box
 static_assert(kCheckSlots * kCheckSlotF <= sizeof(float) * kRing * kSlotFloats, "forward check ring");
-static_assert(kCheckSlots * kCheckSlotA <= sizeof(float) * (kRing * kSlotFloats + kHandoff),
-              "adjoint check ring (the hand-off row is idle between sweeps)");
+static_assert(kCheckSlots * kCheckSlotA <= offsetof(WarpShared, full),
+              "adjoint check ring (hand-off row and stage slot are idle between sweeps)");
 static_assert(kCheckSlotF % 128 == 0 && kCheckSlotA % 128 == 0, "box slots stay 128-byte aligned");
 
 RZ_DEV float4 lds4(uint32_t a) {
@@ -1258,13 +1312,17 @@ int shot_kernel_warps(int nstrips) {
 // grows while as many CTAs fit on an SM as with W warps.
 template <class K>
 static cudaError_t block_warps(K kern, int W, int *Wb_out) {
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)shot_kernel_smem(kMaxWarps));
+    int dev = 0, optin = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (!e) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    if (!e && shot_kernel_smem(W) > (size_t)optin) e = cudaErrorInvalidConfiguration;
+    if (!e) e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)std::min(shot_kernel_smem(kMaxWarps), (size_t)optin));
     int base = 0;
     if (!e) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&base, kern, 32 * W, shot_kernel_smem(W));
     if (e) return e;
     int Wb = W;
-    for (int v = W + 1; v <= kMaxWarps; ++v) {
+    for (int v = W + 1; v <= kMaxWarps && shot_kernel_smem(v) <= (size_t)optin; ++v) {
         int o = 0;
         if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&o, kern, 32 * v, shot_kernel_smem(v)))) return e;
         if (o < base) break;
