@@ -243,8 +243,9 @@ static int ensure_fields(rz_context *c, int n) {
     c->cap_f = n;
     int r;
     if ((r = make_map(c, &c->maps.tld, c->dT, n, kBlk, kBoxRows))) return r;
-    if ((r = make_map(c, &c->maps.trow, c->dT, n, kBlk, 1))) return r;
-    if ((r = make_map(c, &c->maps.lrow, c->dL, n, kBlk, 1))) return r;
+    if ((r = make_map(c, &c->maps.tst, c->dT, n, kBlk, kStrip))) return r;
+    if ((r = make_map(c, &c->maps.lld, c->dL, n, kBlk, kBoxRows))) return r;
+    if ((r = make_map(c, &c->maps.lst, c->dL, n, kBlk, kStrip))) return r;
     if ((r = make_map(c, &c->maps.tchk, c->dT, n, kCheckCols, kCheckBoxRows))) return r;
     if ((r = make_map(c, &c->maps.lchk, c->dL, n, kCheckCols, kCheckBoxRows))) return r;
     return RZ_OK;

@@ -101,15 +101,16 @@ struct ShotParams {
 
 // Tensor maps of a launch.  Field maps cover [shots][ny][nxp] floats with
 // logical extent [shots][ny][nx]:
-//   tld  traveltime, 32 x kBoxRows box (adjoint preparation)
-//   trow traveltime, 32 x 1 box (forward sweeps)
-//   lrow lambda, 32 x 1 box (adjoint sweeps)
+//   tld  traveltime, 32 x kBoxRows box (forward sweeps, adjoint preparation)
+//   tst  traveltime, 32 x kStrip box (forward sweeps' write-back)
+//   lld  lambda, 32 x kBoxRows box (adjoint sweeps)
+//   lst  lambda, 32 x kStrip box (adjoint sweeps' write-back)
 //   tchk traveltime, 136 x 4 box (fixpoint checks)
 //   lchk lambda, 136 x 4 box (adjoint fixpoint check)
 //   schk slowness in rows of nxp floats [1][ny][nxp], 128 x 4 box (forward check)
 constexpr int kCheckCols = 136, kCheckBoxRows = 4;  // box of tchk / lchk
 struct ShotMaps {
-    CUtensorMap tld, trow, lrow, tchk, lchk, schk;
+    CUtensorMap tld, tst, lld, lst, tchk, lchk, schk;
 };
 
 // several grids in one persistent launch

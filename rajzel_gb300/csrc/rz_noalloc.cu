@@ -113,11 +113,12 @@ extern "C" int rz_eikonal_noalloc(const rz_grid *grid, const float *S, float src
 
     ShotMaps M;
     if (!encode_field_map(&M.tld, T, g.nx, g.ny, nxp, kBlk, kBoxRows) ||
-        !encode_field_map(&M.trow, T, g.nx, g.ny, nxp, kBlk, 1) ||
+        !encode_field_map(&M.tst, T, g.nx, g.ny, nxp, kBlk, kStrip) ||
         !encode_field_map(&M.tchk, T, g.nx, g.ny, nxp, kCheckCols, kCheckBoxRows) ||
         !encode_field_map(&M.schk, Sp, g.nx, g.ny, nxp, 128, kCheckBoxRows))
         return RZ_ECUDA;
-    M.lrow = M.trow;  // no adjoint here
+    M.lld = M.tld;  // no adjoint here
+    M.lst = M.tst;
     M.lchk = M.tchk;
 
     ShotParams P;

@@ -153,18 +153,19 @@ RZ_DEV void ring_wait(Warp &w, int slot) {
 //   ADJ=true : adjoint Leung-Qian sweep of lam (sweep_adj.c)
 //
 // Step t of the warp: lane l updates sweep-local column up = t - l of its row.
-// Shared layout during a sweep: each lane owns one row of 96 floats (three
-// 32-column blocks, a ring in sweep order), the halo row is a 33rd row.  Every
-// lane fills and drains its own row with 1-row TMA copies, so one warp
-// instruction moves a whole 33x32 block, and a lane's next cell is always its
-// current cell +-4 bytes (mod the ring).
+// Shared layout during a sweep: a ring of three slots, each a 33-row x
+// 32-column tile (the strip's rows and its halo row) of one block, in sweep
+// order.  Lane 0 fills a slot with one tile copy and drains the strip's 32
+// rows with one tile store; a lane's next cell is its current cell +-4 bytes,
+// or the same row of the next slot at a block boundary.
 // ---------------------------------------------------------------------------
-constexpr int kRowFloats = kRing * kBlk;          // 96
-constexpr int kRowBytes = kRowFloats * 4;         // 384
+constexpr uint32_t kTileRowBytes = kBlk * 4;                  // 128
+constexpr uint32_t kSlotBytes = kSlotFloats * 4;              // 4224
+constexpr uint32_t kRingBytes = kRing * kSlotBytes;           // 12672
 
 template <int DX, int DY, bool ADJ, int MODE>
-__device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mrow, float &acc, float &mag,
-                                   int band, int W, const SweepSeq &seq) {
+__device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mld, const CUtensorMap *mst,
+                                   float &acc, float &mag, int band, int W, const SweepSeq &seq) {
     // exact discrete adjoint: mu = R + sum of the weights neighbours put on this cell
     constexpr bool EX = ADJ && (MODE == kModeExact);
     const int l = w.l, g = w.g;
@@ -179,7 +180,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const int j = DY > 0 ? l : 31 - l;
     const int row = kStrip * s + j;
     const bool rowok = row < P.ny;
-    const int hrow = DY > 0 ? kStrip * s + 32 : kStrip * s - 1;  // next strip's first row (old values)
     const int boxrow = DY > 0 ? l : 32 - l;
     const int halorow = DY > 0 ? 32 : 0;
     const bool hasUp = DY > 0 ? (row > 0) : (row < P.ny - 1);
@@ -216,9 +216,12 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const int ngrp = ncol >> 3;  // hand-off groups per sweep
     float *ring = &w.ws->ring[0][0];
     const uint32_t ring_s = smem_u32(ring);
-    const uint32_t row_s = ring_s + (uint32_t)boxrow * kRowBytes;
-    const uint32_t row_end = row_s + kRowBytes;
-    const int hoff = (halorow - boxrow) * kRowBytes;
+    const uint32_t ring_end = ring_s + kRingBytes;
+    const uint32_t row_off = (uint32_t)boxrow * kTileRowBytes;  // this lane's row in a tile
+    const int hoff = (halorow - boxrow) * (int)kTileRowBytes;
+    // tile rows: the strip's rows and the halo row, from grid row y_tile
+    const int y_tile = DY > 0 ? kStrip * s : kStrip * s - 1;
+    const uint32_t store_off = DY > 0 ? 0u : kTileRowBytes;  // the strip's 32 rows within a tile
     const uint32_t hb_in = smem_u32(w.ws->hb);
     const uint32_t hb_out = smem_u32(down->hb);
     const float dh = P.dh;
@@ -243,22 +246,17 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
         phase ^= 1u << slot;
     };
 
-    // ring position (byte offset in a row) of sweep-local block k
-    auto slot_off = [&](int k) -> uint32_t {
-        const int m = mod3(k);
-        return (uint32_t)(DX > 0 ? m : 2 - m) * (kBlk * 4);
-    };
+    // the slot of sweep-local block k
+    auto slot_base = [&](int k) -> uint32_t { return ring_s + (uint32_t)mod3(k) * kSlotBytes; };
     auto gblk = [&](int k) { return DX > 0 ? k : nxb - 1 - k; };
-    // all lanes: TMA-load block k of their own row; lane 0 also the halo row
+    // lane 0: TMA-load block k (33 rows x 32 columns) into its slot
     auto issue = [&](int k) {
-        const int slot = mod3(k);
-        const uint32_t bar = mbar_s + 8u * slot;
-        if (l == 0) mbar_arrive_expect_tx_a(bar, kBoxRows * kBlk * 4);
+        const uint32_t bar = mbar_s + 8u * (uint32_t)mod3(k);
         __syncwarp();
-        const uint32_t so = slot_off(k);
-        const int x = kBlk * gblk(k);
-        tma_load_3d_a(row_s + so, mrow, x, row, z, bar);
-        if (l == 0) tma_load_3d_a(ring_s + (uint32_t)halorow * kRowBytes + so, mrow, x, hrow, z, bar);
+        if (l == 0) {
+            mbar_arrive_expect_tx_a(bar, kSlotBytes);
+            tma_load_3d_a(slot_base(k), mld, kBlk * gblk(k), y_tile, z, bar);
+        }
     };
 
     // read-only per-cell streams, skewed so one step reads one 128-byte line
@@ -335,15 +333,43 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     // ring address of this lane's cell at step t = 0 (column up = -l, which
     // for l > 0 lies before the sweep: any ring cell serves, nothing reads it)
     auto advance = [&](uint32_t a) -> uint32_t {
+        // (a - ring_s) % 128 is 4 * (column in the block): tiles and rows are 128-byte multiples
         if (DX > 0) {
             a += 4;
-            return a == row_end ? row_s : a;
+            if ((a & (kTileRowBytes - 1)) == 0) {  // past column 31: column 0 of the next slot
+                a += kSlotBytes - kTileRowBytes;
+                if (a >= ring_end) a -= kRingBytes;
+            }
+            return a;
         } else {
-            return a == row_s ? row_end - 4 : a - 4;
+            if ((a & (kTileRowBytes - 1)) == 0) {  // at column 0: column 31 of the next slot
+                a += kSlotBytes + kTileRowBytes - 4;
+                return a >= ring_end ? a - kRingBytes : a;
+            }
+            return a - 4;
         }
     };
-    uint32_t addr_c = row_s + slot_off(0) + (DX > 0 ? 0u : 31u * 4u);
-    for (int q = 0; q < l; ++q) addr_c = (DX > 0) ? (addr_c == row_s ? row_end - 4 : addr_c - 4) : (addr_c + 4 == row_end ? row_s : addr_c + 4);
+    // the inverse of advance
+    auto retreat = [&](uint32_t a) -> uint32_t {
+        if (DX > 0) {
+            if ((a & (kTileRowBytes - 1)) == 0) {  // at column 0: column 31 of the previous slot
+                a = a < ring_s + kSlotBytes ? a + kRingBytes : a;
+                return a - kSlotBytes + kTileRowBytes - 4;
+            }
+            return a - 4;
+        } else {
+            a += 4;
+            if ((a & (kTileRowBytes - 1)) == 0) {  // past column 31: column 0 of the previous slot
+                a -= kTileRowBytes;
+                a = a < ring_s + kSlotBytes ? a + kRingBytes : a;
+                a -= kSlotBytes;
+            }
+            return a;
+        }
+    };
+    static_assert((kSlotBytes % kTileRowBytes) == 0 && (kTileRowBytes & (kTileRowBytes - 1)) == 0, "tile layout");
+    uint32_t addr_c = slot_base(0) + row_off + (DX > 0 ? 0u : 31u * 4u);
+    for (int q = 0; q < l; ++q) addr_c = retreat(addr_c);
     uint32_t addr_e = advance(addr_c);
     float own_next = lds(addr_c);
     float ev_next = lds(addr_e);
@@ -516,12 +542,15 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 res_prev = r;
             }
         }
-        // block k-1 is complete: write it back (each lane its own row)
+        // block k-1 is complete: lane 0 writes the strip's 32 rows back (rows
+        // past the grid are clipped by the map)
         if (k >= 1) {
             fence_proxy_async_smem();
             __syncwarp();
-            if (rowok) tma_store_3d_a(mrow, kBlk * gblk(k - 1), row, z, row_s + slot_off(k - 1));
-            tma_store_commit();
+            if (l == 0) {
+                tma_store_3d_a(mst, kBlk * gblk(k - 1), kStrip * s, z, slot_base(k - 1) + store_off);
+                tma_store_commit();
+            }
         }
     }
     tma_store_wait_all<0>();
@@ -1032,9 +1061,9 @@ template <int MODE>
 __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M, int z, const CtaShared &sh, int Wg) {
     const int W = Wg;
     const int tid = threadIdx.x, g = tid >> 5, l = tid & 31;
-    const CUtensorMap *pTld = &M.tld, *pTrow = &M.trow, *pLrow = &M.lrow;
+    const CUtensorMap *pTld = &M.tld;
     if (tid == 0) {
-        tma_prefetch_desc(pTld), tma_prefetch_desc(pTrow), tma_prefetch_desc(pLrow);
+        tma_prefetch_desc(pTld), tma_prefetch_desc(&M.tst), tma_prefetch_desc(&M.lld), tma_prefetch_desc(&M.lst);
         tma_prefetch_desc(&M.tchk), tma_prefetch_desc(&M.lchk), tma_prefetch_desc(&M.schk);
     }
 
@@ -1061,10 +1090,10 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
     SweepSeq seq{nbands == 1 ? 1 : 0, 0, 0, 0};
     // one directional sweep of every band; banded sweeps synchronise the CTA
     // after each band, pipelined ones only at the end of a pass
-#define RZ_SWEEP(DX_, DY_, ADJ_, MODE_, MAP_)                                   \
+#define RZ_SWEEP(DX_, DY_, ADJ_, MODE_, LD_, ST_)                               \
     do {                                                                       \
         for (int b = 0; b < nbands; ++b) {                                     \
-            sweep<DX_, DY_, ADJ_, MODE_>(P, w, MAP_, acc, mag, b, W, seq);     \
+            sweep<DX_, DY_, ADJ_, MODE_>(P, w, LD_, ST_, acc, mag, b, W, seq); \
             if (!seq.pipelined) sweep_barrier(sh);                             \
         }                                                                      \
         seq.advance(DY_);                                                      \
@@ -1093,11 +1122,11 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                 __syncthreads();
             }
             float acc = 0.f, mag = 0.f;
-            RZ_SWEEP(+1, +1, false, MODE, pTrow);
+            RZ_SWEEP(+1, +1, false, MODE, pTld, &M.tst);
             if (pass == 0) stamp(P, z, 5);
-            RZ_SWEEP(-1, +1, false, MODE, pTrow);
-            RZ_SWEEP(-1, -1, false, MODE, pTrow);
-            RZ_SWEEP(+1, -1, false, MODE, pTrow);
+            RZ_SWEEP(-1, +1, false, MODE, pTld, &M.tst);
+            RZ_SWEEP(-1, -1, false, MODE, pTld, &M.tst);
+            RZ_SWEEP(+1, -1, false, MODE, pTld, &M.tst);
             if (seq.pipelined) __syncthreads();
             ++pass;
             ++swept;
@@ -1220,17 +1249,17 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
         float acc = 0.f, mag = 0.f;
         if (P.exact) {
             // same four orderings as the Leung-Qian sweeps (eikonal_adj.c:43-46)
-            RZ_SWEEP(+1, +1, true, kModeExact, pLrow);
+            RZ_SWEEP(+1, +1, true, kModeExact, &M.lld, &M.lst);
             if (pass == 0) stamp(P, z, 6);
-            RZ_SWEEP(+1, -1, true, kModeExact, pLrow);
-            RZ_SWEEP(-1, +1, true, kModeExact, pLrow);
-            RZ_SWEEP(-1, -1, true, kModeExact, pLrow);
+            RZ_SWEEP(+1, -1, true, kModeExact, &M.lld, &M.lst);
+            RZ_SWEEP(-1, +1, true, kModeExact, &M.lld, &M.lst);
+            RZ_SWEEP(-1, -1, true, kModeExact, &M.lld, &M.lst);
         } else {
-            RZ_SWEEP(+1, +1, true, MODE, pLrow);
+            RZ_SWEEP(+1, +1, true, MODE, &M.lld, &M.lst);
             if (pass == 0) stamp(P, z, 6);
-            RZ_SWEEP(+1, -1, true, MODE, pLrow);
-            RZ_SWEEP(-1, +1, true, MODE, pLrow);
-            RZ_SWEEP(-1, -1, true, MODE, pLrow);
+            RZ_SWEEP(+1, -1, true, MODE, &M.lld, &M.lst);
+            RZ_SWEEP(-1, +1, true, MODE, &M.lld, &M.lst);
+            RZ_SWEEP(-1, -1, true, MODE, &M.lld, &M.lst);
         }
         if (seq.pipelined) __syncthreads();
         ++pass;
