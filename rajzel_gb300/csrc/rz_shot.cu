@@ -899,43 +899,54 @@ RZ_DEV void fill_field(const ShotParams &P, float *F, float v, bool frame0) {
 }
 
 // Skewed copies of the converged traveltimes for the adjoint sweeps, plus the
-// rows bordering each strip (TMA tiles in, coalesced skew lines out).
-template <int DUMMY>
-__device__ __noinline__ void relayout_strip(const ShotParams &P, Warp &w, const CUtensorMap *mld, int s) {
+// rows bordering each strip (TMA tiles in, coalesced skew lines out).  The
+// work items are (strip s, block G), G = 0..nxb, numbered s*(nxb+1)+G; a warp
+// takes items [i0, i1) in order, so the warps of the CTA share the strips.
+__device__ __noinline__ void relayout_items(const ShotParams &P, Warp &w, const CUtensorMap *mld, int i0, int i1) {
     const int l = w.l, z = w.z;
     float *ring = &w.ws->ring[0][0];
-    const int nxb = P.nxb;
-    float *ta = P.TA + (size_t)z * P.sstride + ((size_t)s * P.qn + kSkewFront) * 32;
-    float *tb = P.TB + (size_t)z * P.sstride + ((size_t)s * P.qn + kSkewFront) * 32;
-    const int er = edge_row(P.nxp);
-    float *ed = P.ED + (size_t)z * P.estride + (size_t)s * er + kEdgePad;
-    float *eu_next = (s + 1 < P.nstrips) ? P.EU + (size_t)z * P.estride + (size_t)(s + 1) * er + kEdgePad : nullptr;
+    const int nxb = P.nxb, per = nxb + 1, er = edge_row(P.nxp);
     // tile index G (column block, may be -1 or nxb: zero-filled) -> ring slot
     auto slot_of = [&](int G) { return mod3(G + 1); };
-    auto issue = [&](int G) {
-        int sl = slot_of(G);
+    int s = -1;
+    float *ta = nullptr, *tb = nullptr, *ed = nullptr, *eu_next = nullptr;
+    auto issue = [&](int G) {  // lane 0
+        const int sl = slot_of(G);
         mbar_arrive_expect_tx(&w.mbar[sl], kSlotFloats * 4);
         tma_load_3d(ring + sl * kSlotFloats, mld, kBlk * G, kStrip * s, z, &w.mbar[sl]);
     };
-    if (l == 0) {
-        issue(-1);
-        issue(0);
-    }
-    __syncwarp();
-    ring_wait(w, slot_of(-1));
-    for (int G = 0; G <= nxb; ++G) {
+    for (int it = i0; it < i1; ++it) {
+        const int G = it % per;
+        if (it / per != s) {  // first item of a strip in this range: tiles G-1 and G
+            s = it / per;
+            ta = P.TA + (size_t)z * P.sstride + ((size_t)s * P.qn + kSkewFront) * 32;
+            tb = P.TB + (size_t)z * P.sstride + ((size_t)s * P.qn + kSkewFront) * 32;
+            ed = P.ED + (size_t)z * P.estride + (size_t)s * er + kEdgePad;
+            eu_next = (s + 1 < P.nstrips) ? P.EU + (size_t)z * P.estride + (size_t)(s + 1) * er + kEdgePad : nullptr;
+            fence_proxy_async_smem();  // the slots' earlier generic reads precede the copies
+            __syncwarp();
+            if (l == 0) {
+                issue(G - 1);
+                issue(G);
+            }
+            __syncwarp();
+            ring_wait(w, slot_of(G - 1));
+        }
         ring_wait(w, slot_of(G));
-        if (l == 0 && G + 1 <= nxb) issue(G + 1);  // slot of G-2: all its reads ended last iteration
+        // the next block of this strip goes where block G-2 was (read an item ago)
+        fence_proxy_async_smem();
         __syncwarp();
+        if (l == 0 && G + 1 <= nxb && it + 1 < i1) issue(G + 1);
         const float *t_prev = ring + slot_of(G - 1) * kSlotFloats;
         const float *t_cur = ring + slot_of(G) * kSlotFloats;
         // skew lines q in [32G, 32G+32): family A column q-j, family B column q+j-31
+#pragma unroll 8
         for (int qq = 0; qq < 32; ++qq) {
             const int q = kBlk * G + qq;
-            const int ca = qq - l;       // column offset relative to tile G (lane = j)
+            const int ca = qq - l;  // column offset relative to tile G (lane = j)
             const int cb = qq + l - 31;
-            float va = ca >= 0 ? t_cur[l * kBlk + ca] : t_prev[l * kBlk + ca + 32];
-            float vb = cb >= 0 ? t_cur[l * kBlk + cb] : t_prev[l * kBlk + cb + 32];
+            const float va = ca >= 0 ? t_cur[l * kBlk + ca] : t_prev[l * kBlk + ca + 32];
+            const float vb = cb >= 0 ? t_cur[l * kBlk + cb] : t_prev[l * kBlk + cb + 32];
             ta[(size_t)q * 32 + l] = va;
             tb[(size_t)q * 32 + l] = vb;
         }
@@ -1222,7 +1233,11 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
     if (P.exact) {
         exact_prepare(P, z, T, L);
     } else {
-        for (int s = g; s < P.nstrips; s += (int)(blockDim.x >> 5)) relayout_strip<0>(P, w, pTld, s);
+        {
+            const int items = P.nstrips * (P.nxb + 1), Wb = (int)(blockDim.x >> 5);
+            const int per_warp = (items + Wb - 1) / Wb;
+            relayout_items(P, w, pTld, min(items, g * per_warp), min(items, (g + 1) * per_warp));
+        }
         // lambda: 0 on the frame, 10*TIME inside, residuals at receiver cells
         fill_field(P, L, (float)(10.0 * (double)P.time), true);
         __syncthreads();
