@@ -108,6 +108,11 @@ struct SweepSeq {
 
 RZ_DEV int mod3(int v) { return v - 3 * (v / 3); }
 
+template <bool B>
+struct BoolTag {
+    static constexpr bool value = B;
+};
+
 RZ_DEV float lds(uint32_t a) {
     float v;
     asm volatile("ld.shared.f32 %0, [%1];" : "=f"(v) : "r"(a));
@@ -230,6 +235,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     // valid sweep-local columns [lo, hi) of this lane's row
     const int lo = DX > 0 ? 0 : ncol - nx;
     const int hi = rowok ? (DX > 0 ? nx : ncol) : lo;
+    const bool rows_in = kStrip * s + kStrip <= P.ny;  // every row of the strip inside the grid
+    const int hi_in = DX > 0 ? nx : ncol;               // hi of the rows inside the grid
     // everything the step loop touches lives in registers: shared-window
     // addresses of the barriers, the phase bits, the error bits
     const uint32_t abort_s = smem_u32((const void *)w.abort_word);
@@ -446,7 +453,12 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
             const int u0 = t0 - l;
             const float *zr = EX ? zs + QS * 32 * t0 : nullptr;
             const float *rr = EX ? rs + QS * 32 * t0 : nullptr;
-            // ---- 8 wavefront steps, straight-line code ----
+            // ---- 8 wavefront steps, straight-line code.  In an interior group
+            // (every lane's 8 columns strictly inside the grid, every row of the
+            // strip inside it) no cell is a boundary cell or outside the grid
+            // and every hand-off value is in range: those tests are left out.
+            auto steps8 = [&](auto interior_tag) {
+                constexpr bool INT = decltype(interior_tag)::value;
 #pragma unroll
             for (int ii = 0; ii < 8; ++ii) {
                 const int t = t0 + ii;
@@ -467,11 +479,11 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 nv = (l == 0) ? hbq[ii] : nv;
                 sv = (l == 31) ? halo : sv;
                 const float xv = xq[ii];
-                const bool valid = (unsigned)(up - lo) < (unsigned)(hi - lo);
+                const bool valid = INT || (unsigned)(up - lo) < (unsigned)(hi - lo);
                 float r;
                 if (!ADJ) {
-                    const bool hasW = up > lo;
-                    const bool hasE = up < hi - 1;
+                    const bool hasW = INT || up > lo;
+                    const bool hasE = INT || up < hi - 1;
                     const float tw = hasW ? res_prev : own;
                     const float te = hasE ? ev : own;
                     const float tn = hasUp ? nv : own;
@@ -536,11 +548,16 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 if (EX) acc_l += valid ? fabsf(own - r) : 0.0f;
                 // lane 31 hands its row down; after the 8th value of a group it signals
                 const int upp = t - 31;
-                sts_if(hb_out + 4u * (uint32_t)((upp + pb8) & (kHandoff - 1)), r, producer && upp >= 0 && upp < ncol);
+                sts_if(hb_out + 4u * (uint32_t)((upp + pb8) & (kHandoff - 1)), r,
+                       producer && (INT || (upp >= 0 && upp < ncol)));
                 if (ii == 6) mbar_arrive_if(full_out + 8u * (((t - 38 + pb8) >> 3) & (kGroups - 1)),
-                                            producer && t >= 38 && ((t - 38) >> 3) < ngrp);
+                                            producer && (INT || (t >= 38 && ((t - 38) >> 3) < ngrp)));
                 res_prev = r;
             }
+            };
+            // the columns of this group: t0-31 (lane 31) .. t0+7 (lane 0)
+            if (rows_in && t0 - 31 >= lo + 1 && t0 + 7 <= hi_in - 2) steps8(BoolTag<true>{});
+            else steps8(BoolTag<false>{});
         }
         // block k-1 is complete: lane 0 writes the strip's 32 rows back (rows
         // past the grid are clipped by the map)
