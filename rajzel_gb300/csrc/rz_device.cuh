@@ -69,6 +69,11 @@ RZ_DEV void sts_if(uint32_t a, float v, bool p) {
     asm volatile("{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %2, 0;\n\t@q st.shared.f32 [%0], %1;\n\t}" ::"r"(a), "f"(v),
                  "r"((uint32_t)p));
 }
+RZ_DEV void sts4_if(uint32_t a, float x, float y, float z, float w, bool p) {
+    asm volatile(
+        "{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %5, 0;\n\t@q st.shared.v4.f32 [%0], {%1, %2, %3, %4};\n\t}" ::"r"(a),
+        "f"(x), "f"(y), "f"(z), "f"(w), "r"((uint32_t)p));
+}
 RZ_DEV void mbar_arrive_if(uint32_t bar, bool p) {
     asm volatile(
         "{\n\t.reg .pred q;\n\tsetp.ne.u32 q, %1, 0;\n\t@q mbarrier.arrive.release.cta.shared::cta.b64 _, [%0];\n\t}" ::"r"(

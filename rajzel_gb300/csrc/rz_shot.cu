@@ -119,6 +119,11 @@ RZ_DEV float lds(uint32_t a) {
     return v;
 }
 RZ_DEV void sts(uint32_t a, float v) { asm volatile("st.shared.f32 [%0], %1;" ::"r"(a), "f"(v)); }
+RZ_DEV float4 lds4(uint32_t a) {
+    float4 v;
+    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
+    return v;
+}
 RZ_DEV uint32_t lds_u32(uint32_t a) {
     uint32_t v;
     asm volatile("ld.shared.u32 %0, [%1];" : "=r"(v) : "r"(a));
@@ -383,6 +388,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     float halo_next = lds(addr_c + hoff);
 
     float res_prev = 0.f;
+    float hand_carry = 0.f;  // the last step's value of the previous group (lane 31 hands it down)
     for (int k = 0; k <= nxb; ++k) {
 #pragma unroll 1
         for (int i0 = 0; i0 < 32; i0 += 8) {
@@ -406,9 +412,10 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 if (G < ngrp) {
                     const int Gg = G + cons_base;  // group number in this ring's lifetime
                     if (!mbar_wait_a(full_in + 8u * (Gg & (kGroups - 1)), (Gg >> kGroupsLog2) & 1, abort_s)) err |= ERR_FLAG_TIMEOUT;
-                    const uint32_t hb_g = hb_in + 4u * (uint32_t)((t0 + cb8) & (kHandoff - 1));
-#pragma unroll
-                    for (int i = 0; i < 8; ++i) hbq[i] = lds(hb_g + 4u * i);
+                    const uint32_t hb_g = hb_in + 4u * (uint32_t)((t0 + cb8) & (kHandoff - 1));  // 32-byte aligned
+                    const float4 h0 = lds4(hb_g), h1 = lds4(hb_g + 16u);
+                    hbq[0] = h0.x, hbq[1] = h0.y, hbq[2] = h0.z, hbq[3] = h0.w;
+                    hbq[4] = h1.x, hbq[5] = h1.y, hbq[6] = h1.z, hbq[7] = h1.w;
                     // the values are in registers: release the slot at once
                     mbar_arrive_if(empty_in + 8u * (Gg & (kGroups - 1)), l == 0);
                 } else {
@@ -428,9 +435,9 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 for (int q = 0; q < 8; ++q) hbq[q] = 0.f;
             }
             if (is_producer_warp) {
-                // lane 31 starts hand-off group Gp at step t0+7 (column t0-24)
-                const int Gp = (t0 - 24) >> 3, Gpg = Gp + prod_base;
-                if (t0 >= 24 && Gpg >= kGroups && Gp < ngrp &&
+                // lane 31 writes hand-off group Gp (columns t0-32 .. t0-25) in this group
+                const int Gp = (t0 - 32) >> 3, Gpg = Gp + prod_base;
+                if (t0 >= 32 && Gpg >= kGroups && Gp < ngrp &&
                     !mbar_wait_a(empty_out + 8u * (Gpg & (kGroups - 1)), ((Gpg >> kGroupsLog2) - 1) & 1, abort_s))
                     err |= ERR_FLAG_TIMEOUT;
             }
@@ -459,6 +466,13 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
             // and every hand-off value is in range: those tests are left out.
             auto steps8 = [&](auto interior_tag) {
                 constexpr bool INT = decltype(interior_tag)::value;
+                // lane 31 of a producing warp hands down the values of columns
+                // upp0 .. upp0+7 (steps t0-1 .. t0+6): two 16-byte stores, then
+                // the group's full barrier
+                const int upp0 = t0 - 32;
+                const bool hand = producer && (INT || (upp0 >= 0 && upp0 < ncol));
+                const uint32_t hq = hb_out + 4u * (uint32_t)((upp0 + pb8) & (kHandoff - 1));  // 32-byte aligned
+                float h0 = 0.f, h1 = 0.f, h3 = 0.f, h4 = 0.f, h5 = 0.f;
 #pragma unroll
             for (int ii = 0; ii < 8; ++ii) {
                 const int t = t0 + ii;
@@ -546,12 +560,17 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 sts(cur, r);
                 if (MODE == kModeFast) acc_l += valid ? own - r : 0.0f;
                 if (EX) acc_l += valid ? fabsf(own - r) : 0.0f;
-                // lane 31 hands its row down; after the 8th value of a group it signals
-                const int upp = t - 31;
-                sts_if(hb_out + 4u * (uint32_t)((upp + pb8) & (kHandoff - 1)), r,
-                       producer && (INT || (upp >= 0 && upp < ncol)));
-                if (ii == 6) mbar_arrive_if(full_out + 8u * (((t - 38 + pb8) >> 3) & (kGroups - 1)),
-                                            producer && (INT || (t >= 38 && ((t - 38) >> 3) < ngrp)));
+                if (ii == 0) h0 = r;
+                if (ii == 1) h1 = r;
+                if (ii == 2) sts4_if(hq, hand_carry, h0, h1, r, hand);
+                if (ii == 3) h3 = r;
+                if (ii == 4) h4 = r;
+                if (ii == 5) h5 = r;
+                if (ii == 6) {
+                    sts4_if(hq + 16u, h3, h4, h5, r, hand);
+                    mbar_arrive_if(full_out + 8u * (uint32_t)(((upp0 + pb8) >> 3) & (kGroups - 1)), hand);
+                }
+                if (ii == 7) hand_carry = r;
                 res_prev = r;
             }
             };
@@ -690,11 +709,6 @@ static_assert(kCheckSlots * kCheckSlotA <= offsetof(WarpShared, full),
               "adjoint check ring (hand-off row and stage slot are idle between sweeps)");
 static_assert(kCheckSlotF % 128 == 0 && kCheckSlotA % 128 == 0, "box slots stay 128-byte aligned");
 
-RZ_DEV float4 lds4(uint32_t a) {
-    float4 v;
-    asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a));
-    return v;
-}
 
 // four cells of a row with their west and east neighbours; the row starts
 // with the 4 halo columns, lane l's cells are at 16 + 16 l
