@@ -354,13 +354,17 @@ RZ_DEV float leung_qian_ref(float tc, float te, float tw, float ts, float tn, fl
     return r;
 }
 
+// Fast mode: the reference divides each difference and the sums by DH, a
+// common factor 1/DH^2 of lhs and rhs that cancels in rhs/lhs; the
+// differences stay unscaled and the threshold EPS_ADJ becomes EPS_ADJ*DH^2
+// (lq_eps_h2).
+RZ_DEV float lq_eps_h2(float eps_adj, float dh) { return eps_adj * (dh * dh); }
 RZ_DEV float leung_qian_fast(float tc, float te, float tw, float ts, float tn, float le, float lw, float ls, float ln,
-                             float own, float rdh, float eps_adj) {
-    float ap = (tc - te) * rdh, am = (tw - tc) * rdh;
-    float bp = (tc - ts) * rdh, bm = (tn - tc) * rdh;
-    float lhs = (fmaxf(ap, 0.0f) - fminf(am, 0.0f) + fmaxf(bp, 0.0f) - fminf(bm, 0.0f)) * rdh;
-    float rhs = (fmaxf(am, 0.0f) * lw - fminf(ap, 0.0f) * le + fmaxf(bm, 0.0f) * ln - fminf(bp, 0.0f) * ls) * rdh;
-    float lt = (lhs > eps_adj) ? __fdividef(rhs, lhs) : 0.0f;
+                             float own, float eps_h2) {
+    const float ap = tc - te, am = tw - tc, bp = tc - ts, bm = tn - tc;
+    const float lhs = (fmaxf(ap, 0.0f) - fminf(am, 0.0f)) + (fmaxf(bp, 0.0f) - fminf(bm, 0.0f));
+    const float rhs = (fmaxf(am, 0.0f) * lw - fminf(ap, 0.0f) * le) + (fmaxf(bm, 0.0f) * ln - fminf(bp, 0.0f) * ls);
+    const float lt = (lhs > eps_h2) ? __fdividef(rhs, lhs) : 0.0f;
     return fminf(own, lt);
 }
 

@@ -236,6 +236,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const uint32_t hb_out = smem_u32(down->hb);
     const float dh = P.dh;
     const float dh_rcp = P.dh_rcp, eps_adj = P.eps_adj;
+    const float eps_h2 = lq_eps_h2(eps_adj, dh);  // fast-mode Leung-Qian threshold
     const bool div_fast = P.div_fast != 0;
     // valid sweep-local columns [lo, hi) of this lane's row
     const int lo = DX > 0 ? 0 : ncol - nx;
@@ -550,7 +551,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                         DivDH div{dh, dh_rcp, div_fast};
                         r = leung_qian_ref(c_tt, tE, tW, tS, tN, lE, lW, lS, lN, own, div, eps_adj);
                     } else {
-                        r = leung_qian_fast(c_tt, tE, tW, tS, tN, lE, lW, lS, lN, own, dh_rcp, eps_adj);
+                        r = leung_qian_fast(c_tt, tE, tW, tS, tN, lE, lW, lS, lN, own, eps_h2);
                     }
                     const bool keep = !valid || ((mword >> j) & 1u);
                     r = keep ? own : r;
@@ -820,6 +821,7 @@ __device__ __noinline__ int adjoint_is_fixpoint(const ShotParams &P, const CUten
     const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int nch = (nx + 127) >> 7, nrb = (ny - 2 + kCheckRows - 1) / kCheckRows;
     const DivDH div{P.dh, P.dh_rcp, P.div_fast != 0};
+    const float eps_h2 = lq_eps_h2(P.eps_adj, P.dh);  // fast-mode Leung-Qian threshold
     if (threadIdx.x == 0) *found = 0;
     fence_proxy_async_smem();  // the ring's generic accesses precede the copies
     __syncthreads();
@@ -882,7 +884,7 @@ __device__ __noinline__ int adjoint_is_fixpoint(const ShotParams &P, const CUten
                                          ? leung_qian_ref(tc.v[i], te, tw, tdv[i], tuv[i], le, lw, ldv[i], luv[i], own,
                                                           div, P.eps_adj)
                                          : leung_qian_fast(tc.v[i], te, tw, tdv[i], tuv[i], le, lw, ldv[i], luv[i],
-                                                           own, P.dh_rcp, P.eps_adj);
+                                                           own, eps_h2);
                     change |= (((sk >> (8 * i)) & 0xffu) == 0) && (rr != own);
                 }
             }
