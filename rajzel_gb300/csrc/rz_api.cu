@@ -49,7 +49,7 @@ struct rz_context {
     float *dSp = nullptr;  // slowness in rows of nxp floats (fixpoint checks)
     double *dCube = nullptr;
     bool cube_valid = false;
-    std::vector<float> hS;
+    int *dBad = nullptr;  // launch_check_model result
 
     // receivers
     bool rec_set = false;
@@ -318,8 +318,11 @@ static int ensure_div(rz_context *c) {
 static int ensure_cube(rz_context *c) {
     if (c->cube_valid) return RZ_OK;
     const size_t n = (size_t)c->g.nx * c->g.ny;
+    std::vector<float> hS(n);
+    CK(cudaMemcpyAsync(hS.data(), c->dS, n * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
     std::vector<double> cube(n);
-    for (size_t i = 0; i < n; ++i) cube[i] = std::pow((double)c->hS[i], 3.0);
+    for (size_t i = 0; i < n; ++i) cube[i] = std::pow((double)hS[i], 3.0);
     if (!c->dCube) CK(dalloc(&c->dCube, n));  // kept across models (graphs hold the pointer)
     CK(cudaMemcpyAsync(c->dCube, cube.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));
@@ -572,6 +575,7 @@ void rz_destroy(rz_context *c) {
     free_batch(c);
     for (auto &pr : c->shot_events) cudaEventDestroy(pr.first), cudaEventDestroy(pr.second);
     dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dVp), dfree(c->dCube), dfree(c->dGrad), dfree(c->dL2);
+    dfree(c->dBad);
     dfree(c->dSp);
     dfree(c->dRecH), dfree(c->dRecK), dfree(c->dRcH), dfree(c->dRcK), dfree(c->dRcRec), dfree(c->dSkip);
     dfree(c->dSkipP);
@@ -634,14 +638,14 @@ static int set_model_common(rz_context *c) {
     CK(launch_skew_field(c->dS, nx, ny, nx, c->nstrips, c->nxb, c->dSA, c->dSB, c->st));
     CK(cudaMemcpy2DAsync(c->dSp, (size_t)c->nxp * 4, c->dS, (size_t)nx * 4, (size_t)nx * 4, ny,
                          cudaMemcpyDeviceToDevice, c->st));
-    c->hS.resize((size_t)nx * ny);
-    CK(cudaMemcpyAsync(c->hS.data(), c->dS, (size_t)nx * ny * 4, cudaMemcpyDeviceToHost, c->st));
+    CK(launch_check_model(c->dS, (long)nx * ny, c->dBad, c->st));
+    int bad = kModelOk;
+    CK(cudaMemcpyAsync(&bad, c->dBad, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
-    for (size_t i = 0; i < c->hS.size(); ++i)
-        if (!(c->hS[i] > 0.f) || !std::isfinite(c->hS[i])) {
-            c->model_set = false;
-            return fail(c, RZ_EINVAL, "slowness at cell %zu is not a positive finite number", i);
-        }
+    if (bad != kModelOk) {
+        c->model_set = false;
+        return fail(c, RZ_EINVAL, "slowness at cell %d is not a positive finite number", bad);
+    }
     c->model_set = true;
     c->cube_valid = false;
     return RZ_OK;
@@ -650,6 +654,7 @@ static int set_model_common(rz_context *c) {
 static int alloc_model(rz_context *c) {
     const size_t n = (size_t)c->g.nx * c->g.ny;
     if (!c->dS) CK(dalloc(&c->dS, n));
+    if (!c->dBad) CK(dalloc(&c->dBad, 1));
     if (!c->dSp) {
         CK(dalloc(&c->dSp, (size_t)c->g.ny * c->nxp));
         CK(cudaMemsetAsync(c->dSp, 0, (size_t)c->g.ny * c->nxp * 4, c->st));
@@ -679,14 +684,14 @@ int rz_set_velocity(rz_context *c, const float *vp, int flags) {
     if (!c->grid_set) return fail(c, RZ_ESTATE, "rz_set_grid first");
     cudaSetDevice(c->device);
     if (c->dS && !c->model_set) {
-        dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dSp);
+        dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dSp), dfree(c->dVp);
     }
     int r;
     if ((r = alloc_model(c))) return r;
     const size_t n = (size_t)c->g.nx * c->g.ny;
     const float *src = vp;
     if (!have_dev(flags)) {
-        CK(dalloc(&c->dVp, n));
+        if (!c->dVp) CK(dalloc(&c->dVp, n));
         CK(cudaMemcpyAsync(c->dVp, vp, n * 4, cudaMemcpyHostToDevice, c->st));
         src = c->dVp;
     }

@@ -1,4 +1,6 @@
 // rz_aux.cu -- per-model / per-geometry preparation and the gradient stack.
+#include <algorithm>
+
 #include "rz_device.cuh"
 #include "rz_internal.h"
 
@@ -235,6 +237,23 @@ __global__ void calc_s_kernel(const float *vp, float *S, long n) {
 
 cudaError_t launch_calc_s(const float *vp, float *S, long n, cudaStream_t st) {
     calc_s_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(vp, S, n);
+    return cudaGetLastError();
+}
+
+// the index of the first cell whose slowness is not a positive finite number
+// (atomicMin), or kModelOk when there is none
+__global__ void check_model_kernel(const float *S, long n, int *first_bad) {
+    for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
+        const float s = S[c];
+        if (!(s > 0.f) || !isfinite(s)) atomicMin(first_bad, (int)c);
+    }
+}
+
+cudaError_t launch_check_model(const float *S, long n, int *first_bad, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(first_bad, 0x7f, sizeof(int), st);  // kModelOk
+    if (e != cudaSuccess) return e;
+    const long blocks = std::min((n + 255) / 256, 152L * 8);
+    check_model_kernel<<<(unsigned)std::max(blocks, 1L), 256, 0, st>>>(S, n, first_bad);
     return cudaGetLastError();
 }
 

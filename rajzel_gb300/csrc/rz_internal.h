@@ -160,6 +160,8 @@ cudaError_t launch_copy_rows(const float *src, int src_pitch, float *dst, int ds
 cudaError_t launch_check_div(float dh, float rcp, unsigned int *bad, cudaStream_t st);
 // S = (float)(1.0/(double)vp) per cell (calc_S.c:21)
 cudaError_t launch_calc_s(const float *vp, float *S, long n, cudaStream_t st);
+constexpr int kModelOk = 0x7f7f7f7f;  // launch_check_model: no invalid cell (grids have fewer cells)
+cudaError_t launch_check_model(const float *S, long n, int *first_bad, cudaStream_t st);
 // *out = 0.5 * sum_z l2[z], summed in shot order in double (grad_obj.c:28,42,61)
 cudaError_t launch_sum_l2(const double *l2, int n, double *out, cudaStream_t st);
 
