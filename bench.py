@@ -292,18 +292,23 @@ def run_gpu_arm(args, rank, world, local_rank):
     ctx2 = R.Context(local_rank, args.mode)
     ctx2.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
     ctx2.set_receivers(w.recx, w.recz)
-    vp_host = np.ascontiguousarray(w.vp_start)
+    # the step's inputs (velocity, picks) and its gradient live in pinned host memory
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float32, pin_memory=True).numpy()
+    vp_host, tobs_host, g_host = pinned((w.ny, w.nx)), pinned(np.shape(Tobs)), pinned((w.ny, w.nx))
+    vp_host[...] = w.vp_start
+    tobs_host[...] = Tobs
     e2e_steps = max(3, args.steps // 2)
     for _ in range(2):
         ctx2.set_velocity(vp_host)
-        ctx2.grad_obj(w.srcx, w.srcz, Tobs)
+        ctx2.grad_obj(w.srcx, w.srcz, tobs_host, out=g_host)
     t0 = time.perf_counter()
     for _ in range(e2e_steps):
         ctx2.set_velocity(vp_host)
-        g_host, L2 = ctx2.grad_obj(w.srcx, w.srcz, Tobs)
+        g_host, L2 = ctx2.grad_obj(w.srcx, w.srcz, tobs_host, out=g_host)
     e2e_s = time.perf_counter() - t0
     e2e_value = world * w.nshots * e2e_steps / e2e_s
-    h2d = vp_host.nbytes + Tobs.nbytes + 2 * 4 * w.nshots
+    h2d = vp_host.nbytes + tobs_host.nbytes + 2 * 4 * w.nshots
     d2h = g_host.nbytes + 8 + 4 * w.nshots
 
     if rank != 0:

@@ -310,11 +310,18 @@ class Context:
                     "rz_forward")
         return TT, Tmod[:, : self.ntr], passes
 
-    def grad_obj(self, srcx, srcz, Tobs):
+    def grad_obj(self, srcx, srcz, Tobs, out=None):
+        """Misfit and stacked gradient (host buffers); `out`, if given, is a
+        C-contiguous float32 [ny][nx] array that receives the gradient."""
         srcx, srcz = _f32(srcx), _f32(srcz)
         n = len(srcx)
         Tobs = _f32(Tobs).reshape(n, self.ntr)
-        grad = np.empty((self.ny, self.nx), np.float32)
+        if out is not None:
+            if out.dtype != np.float32 or out.shape != (self.ny, self.nx) or not out.flags.c_contiguous:
+                raise ValueError("out must be a C-contiguous float32 array of shape (ny, nx)")
+            grad = out
+        else:
+            grad = np.empty((self.ny, self.nx), np.float32)
         L2 = C.c_double(0.0)
         self._check(self.lib.rz_grad_obj(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(Tobs), _ptr(grad), C.byref(L2), 0),
                     "rz_grad_obj")
