@@ -474,6 +474,13 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 const bool hand = producer && (INT || (upp0 >= 0 && upp0 < ncol));
                 const uint32_t hq = hb_out + 4u * (uint32_t)((upp0 + pb8) & (kHandoff - 1));  // 32-byte aligned
                 float h0 = 0.f, h1 = 0.f, h3 = 0.f, h4 = 0.f, h5 = 0.f;
+                // addr_e reaches sweep-local column t0+ii-l+2 at step ii: a new block
+                // (the next slot) when that column is a multiple of 32, at most once
+                // in 8 steps (at ii = cx); the jump there is advance's
+                const int cx = (l - t0 - 2) & 31;
+                const uint32_t m = (addr_e - ring_s) / kSlotBytes;  // slot before the crossing
+                const uint32_t jump = (DX > 0 ? 4u + kSlotBytes - kTileRowBytes : kSlotBytes + kTileRowBytes - 4u) -
+                                      (m == kRing - 1 ? kRingBytes : 0u);
 #pragma unroll
             for (int ii = 0; ii < 8; ++ii) {
                 const int t = t0 + ii;
@@ -484,7 +491,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 const uint32_t cur = addr_c;
                 // prefetch the next step's shared values
                 addr_c = addr_e;
-                addr_e = advance(addr_e);
+                addr_e += (ii == cx) ? jump : (uint32_t)(DX > 0 ? 4 : -4);
                 own_next = ev;
                 ev_next = lds(addr_e);
                 halo_next = lds(addr_c + hoff);
@@ -772,6 +779,10 @@ __device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUten
         issue(0), issue(1), issue(2);
         __syncwarp();
         R.wait(0);
+        // interior task: every cell has all four neighbours inside the grid
+        const bool interior = base > 0 && base + 128 < nx && k0 > 0 && k0 + kk < ny;
+        auto rows = [&](auto interior_tag) {
+            constexpr bool INT = decltype(interior_tag)::value;
         for (int b = 0; b < nb; ++b) {
 #pragma unroll
             for (int r = 0; r < kCheckBox; ++r) {
@@ -789,13 +800,13 @@ __device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUten
                 for (int i = 0; i < 4; ++i) {
                     const int h = h0 + i;
                     const float own = c.v[i];
-                    const float tw = h > 0 ? (i == 0 ? c.w : c.v[i - 1]) : own;
-                    const float te = h < nx - 1 ? (i == 3 ? c.e : c.v[i + 1]) : own;
-                    const float tn = k > 0 ? uv[i] : own, ts = k < ny - 1 ? dv[i] : own;
+                    const float tw = (INT || h > 0) ? (i == 0 ? c.w : c.v[i - 1]) : own;
+                    const float te = (INT || h < nx - 1) ? (i == 3 ? c.e : c.v[i + 1]) : own;
+                    const float tn = (INT || k > 0) ? uv[i] : own, ts = (INT || k < ny - 1) ? dv[i] : own;
                     const float a = fminf(tw, te), bb = fminf(tn, ts);
                     const float tt = (MODE == kModeReference) ? godunov_ref(a, bb, sv[i], P.dh)
                                                               : godunov_fast(a, bb, sv[i], P.dh);
-                    change |= (h < nx) && (tt < own);
+                    change |= (INT || h < nx) && (tt < own);
                 }
             }
             // box b-1 is read by no later row: box b+2 takes its slot
@@ -803,6 +814,9 @@ __device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUten
             __syncwarp();
             if (b >= 1) issue(b + 2);
         }
+        };
+        if (interior) rows(BoolTag<true>{});
+        else rows(BoolTag<false>{});
         change = __any_sync(0xffffffffu, change);
         if (change && l == 0) *(volatile int *)found = 1;
     }
