@@ -251,6 +251,30 @@ def test_certified_godunov_branch_matches_double(R):
     assert bad.value == 0
 
 
+def test_invalid_model_is_rejected_with_its_cell(R):
+    """The slowness is checked on the device (calc_S.c gives no error path):
+    a zero, negative or NaN velocity, or an infinite slowness, is refused
+    with the first bad cell, and the context works once a valid model is set."""
+    w = synth.small_case(7, 40, 24, nshots=1)
+    ctx = make_ctx(R, w)
+    TT0, _, _ = ctx.eikonal(w.srcx[0], w.srcz[0])
+    for bad_vp in (0.0, -1500.0, np.nan):
+        vp = w.vp_true.copy()
+        vp[5, 7] = bad_vp
+        vp[9, 3] = bad_vp
+        with pytest.raises(R.RajzelError) as e:
+            ctx.set_velocity(vp)
+        assert e.value.status == R.RZ_EINVAL and f"cell {5 * w.nx + 7} " in str(e.value)
+    S = synth.slowness(w.vp_true)
+    S[11, 2] = np.inf
+    with pytest.raises(R.RajzelError) as e:
+        ctx.set_slowness(S)
+    assert e.value.status == R.RZ_EINVAL and f"cell {11 * w.nx + 2} " in str(e.value)
+    ctx.set_velocity(w.vp_true)
+    TT1, _, _ = ctx.eikonal(w.srcx[0], w.srcz[0])
+    assert np.array_equal(TT0, TT1)
+
+
 def test_errors_are_status_codes(R):
     w = synth.small_case(1, 30, 20, nshots=1)
     ctx = R.Context(0)
