@@ -77,7 +77,7 @@ def build(verbose: bool = False) -> str:
         with ThreadPoolExecutor(max_workers=len(jobs)) as ex:
             list(ex.map(_run, jobs))
     if _stale(LIB, objs):
-        _run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs])
+        _run([nvcc(), *ARCH, "-shared", "-o", LIB, *objs, "-lpthread"])
     if os.path.exists(selftest_src) and _stale(SELFTEST, [selftest_obj]):
         _run([nvcc(), *ARCH, "-shared", "-o", SELFTEST, selftest_obj])
     compat_src = os.path.join(CSRC, "rz_compat.c")

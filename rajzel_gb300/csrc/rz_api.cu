@@ -18,6 +18,7 @@
 #include <array>
 #include <map>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/rajzel_gb300.h"
@@ -322,7 +323,17 @@ static int ensure_cube(rz_context *c) {
     CK(cudaMemcpyAsync(hS.data(), c->dS, n * 4, cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     std::vector<double> cube(n);
-    for (size_t i = 0; i < n; ++i) cube[i] = std::pow((double)hS[i], 3.0);
+    // pow of the host C library (reentrant), spread over the host cores
+    auto cubes = [&](size_t a, size_t b) {
+        for (size_t i = a; i < b; ++i) cube[i] = std::pow((double)hS[i], 3.0);
+    };
+    const unsigned nt = n < (size_t)1 << 16 ? 1u : std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> pool;
+    const size_t chunk = (n + nt - 1) / nt;
+    for (unsigned t = 1; t < nt; ++t)
+        if (t * chunk < n) pool.emplace_back(cubes, t * chunk, std::min(n, (t + 1) * chunk));
+    cubes(0, std::min(n, chunk));
+    for (auto &th : pool) th.join();
     if (!c->dCube) CK(dalloc(&c->dCube, n));  // kept across models (graphs hold the pointer)
     CK(cudaMemcpyAsync(c->dCube, cube.data(), n * sizeof(double), cudaMemcpyHostToDevice, c->st));
     CK(cudaStreamSynchronize(c->st));
