@@ -696,7 +696,8 @@ RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold,
 // is, hence so does the second, and so on through all four sweeps.  Such a
 // pass has zero change, so the stopping rule ends the loop after it; the
 // caller counts it without sweeping it, and every result stays the same.
-// The checks split the grid into tasks of 128 columns x kCheckRows rows.  A
+// The checks split the grid into tasks of 128 columns x at most kCheckRows
+// rows (check_task_rows balances the tasks over the warps).  A
 // warp walks a task top to bottom, four cells per lane.  Lane 0 loads the
 // task's rows in boxes of kCheckBox rows by tensor-map copies into a ring of
 // three slots (one mbarrier each) in the warp's shared memory.  A box of a
@@ -707,6 +708,20 @@ RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold,
 // Boxes rather than row copies: small bulk copies are bound by the copy
 // engine's instruction rate, and a box moves four rows per instruction.
 constexpr int kCheckRows = 64, kCheckBox = kCheckBoxRows, kCheckHaloCols = kCheckCols;
+
+// Rows per task for `rows` rows in nch column chunks and W warps: the fewest
+// rounds of W tasks times (rows per task + one box of start-up), at most
+// kCheckRows rows per task.
+RZ_DEV int check_task_rows(int rows, int nch, int W) {
+    const int n0 = (rows + kCheckRows - 1) / kCheckRows;
+    int best_r = kCheckRows, best = 0x7fffffff;
+    for (int nrb = n0; nrb <= 4 * n0 + 4; ++nrb) {
+        const int r = (rows + nrb - 1) / nrb;
+        const int cost = ((nch * nrb + W - 1) / W) * (r + kCheckBox);
+        if (cost < best) best = cost, best_r = r;
+    }
+    return best_r;
+}
 static_assert(kCheckBox == 4 && kCheckHaloCols == 128 + 8, "box rows are indexed with j >> 2, halos are 4 columns");
 constexpr uint32_t kRowH = kCheckHaloCols * 4;  // bytes of a box row with halos
 constexpr uint32_t kRowP = 128 * 4;             // bytes of a box row without
@@ -753,7 +768,7 @@ __device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUten
                                                 int z, WarpShared *ws, int *found, volatile int *abort_word) {
     const int nx = P.nx, ny = P.ny;
     const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
-    const int nch = (nx + 127) >> 7, nrb = (ny + kCheckRows - 1) / kCheckRows;
+    const int nch = (nx + 127) >> 7, rt = check_task_rows(ny, nch, W), nrb = (ny + rt - 1) / rt;
     if (threadIdx.x == 0) *found = 0;
     fence_proxy_async_smem();  // the ring's generic accesses precede the copies
     __syncthreads();
@@ -763,7 +778,7 @@ __device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUten
         if (__shfl_sync(0xffffffffu, *(volatile int *)found, 0)) break;  // warp-uniform
         const int base = (task % nch) << 7, h0 = base + 4 * l;
         // rows k0 .. k0+kk-1; window row j is grid row k0-1+j, j = 0 .. kk+1
-        const int k0 = (task / nch) * kCheckRows, kk = min(ny - k0, kCheckRows);
+        const int k0 = (task / nch) * rt, kk = min(ny - k0, rt);
         const int nb = ((kk + 1) >> 2) + 1;
         auto issue = [&](int b) {
             if (b >= nb || l != 0) return;
@@ -833,7 +848,7 @@ __device__ __noinline__ int adjoint_is_fixpoint(const ShotParams &P, const CUten
                                                 int z, WarpShared *ws, int *found, volatile int *abort_word) {
     const int nx = P.nx, ny = P.ny, nxp = P.nxp;
     const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
-    const int nch = (nx + 127) >> 7, nrb = (ny - 2 + kCheckRows - 1) / kCheckRows;
+    const int nch = (nx + 127) >> 7, rt = check_task_rows(ny - 2, nch, W), nrb = (ny - 2 + rt - 1) / rt;
     const DivDH div{P.dh, P.dh_rcp, P.div_fast != 0};
     const float eps_h2 = lq_eps_h2(P.eps_adj, P.dh);  // fast-mode Leung-Qian threshold
     if (threadIdx.x == 0) *found = 0;
@@ -845,7 +860,7 @@ __device__ __noinline__ int adjoint_is_fixpoint(const ShotParams &P, const CUten
         if (__shfl_sync(0xffffffffu, *(volatile int *)found, 0)) break;  // warp-uniform
         const int base = (task % nch) << 7, h0 = base + 4 * l;
         // interior rows k0 .. k0+kk-1 (k0 >= 1, k0+kk <= ny-1); window row j is grid row k0-1+j
-        const int k0 = 1 + (task / nch) * kCheckRows, kk = min(ny - 1 - k0, kCheckRows);
+        const int k0 = 1 + (task / nch) * rt, kk = min(ny - 1 - k0, rt);
         const int nb = ((kk + 1) >> 2) + 1;
         auto issue = [&](int b) {
             if (b >= nb || l != 0) return;
