@@ -173,7 +173,10 @@ constexpr uint32_t kTileRowBytes = kBlk * 4;                  // 128
 constexpr uint32_t kSlotBytes = kSlotFloats * 4;              // 4224
 constexpr uint32_t kRingBytes = kRing * kSlotBytes;           // 12672
 
-template <int DX, int DY, bool ADJ, int MODE>
+// DIV: reference-mode adjoint only, whether the verified Markstein division by
+// DH may be used (P.div_fast); a compile-time choice keeps the unused
+// division path out of the step code
+template <int DX, int DY, bool ADJ, int MODE, int DIV = 1>
 __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mld, const CUtensorMap *mst,
                                    float &acc, float &mag, int band, int W, const SweepSeq &seq) {
     // exact discrete adjoint: mu = R + sum of the weights neighbours put on this cell
@@ -237,7 +240,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const float dh = P.dh;
     const float dh_rcp = P.dh_rcp, eps_adj = P.eps_adj;
     const float eps_h2 = lq_eps_h2(eps_adj, dh);  // fast-mode Leung-Qian threshold
-    const bool div_fast = P.div_fast != 0;
+    constexpr bool div_fast = DIV != 0;
     // valid sweep-local columns [lo, hi) of this lane's row
     const int lo = DX > 0 ? 0 : ncol - nx;
     const int hi = rowok ? (DX > 0 ? nx : ncol) : lo;
@@ -843,13 +846,13 @@ __device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUten
 // the Leung-Qian update of interior, non-receiver cells (sweep_adj.c:26-30);
 // skip is the [ny][nxp] byte map of cells the adjoint sweeps leave unchanged.
 // mT / mL: traveltime / lambda fields, box kCheckHaloCols x kCheckBox.
-template <int MODE>
+template <int MODE, int DIV>
 __device__ __noinline__ int adjoint_is_fixpoint(const ShotParams &P, const CUtensorMap *mT, const CUtensorMap *mL,
                                                 int z, WarpShared *ws, int *found, volatile int *abort_word) {
     const int nx = P.nx, ny = P.ny, nxp = P.nxp;
     const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
     const int nch = (nx + 127) >> 7, rt = check_task_rows(ny - 2, nch, W), nrb = (ny - 2 + rt - 1) / rt;
-    const DivDH div{P.dh, P.dh_rcp, P.div_fast != 0};
+    const DivDH div{P.dh, P.dh_rcp, DIV != 0};
     const float eps_h2 = lq_eps_h2(P.eps_adj, P.dh);  // fast-mode Leung-Qian threshold
     if (threadIdx.x == 0) *found = 0;
     fence_proxy_async_smem();  // the ring's generic accesses precede the copies
@@ -1163,14 +1166,15 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
     SweepSeq seq{nbands == 1 ? 1 : 0, 0, 0, 0};
     // one directional sweep of every band; banded sweeps synchronise the CTA
     // after each band, pipelined ones only at the end of a pass
-#define RZ_SWEEP(DX_, DY_, ADJ_, MODE_, LD_, ST_)                               \
-    do {                                                                       \
-        for (int b = 0; b < nbands; ++b) {                                     \
-            sweep<DX_, DY_, ADJ_, MODE_>(P, w, LD_, ST_, acc, mag, b, W, seq); \
-            if (!seq.pipelined) sweep_barrier(sh);                             \
-        }                                                                      \
-        seq.advance(DY_);                                                      \
+#define RZ_SWEEP_D(DX_, DY_, ADJ_, MODE_, DIV_, LD_, ST_)                           \
+    do {                                                                           \
+        for (int b = 0; b < nbands; ++b) {                                         \
+            sweep<DX_, DY_, ADJ_, MODE_, DIV_>(P, w, LD_, ST_, acc, mag, b, W, seq); \
+            if (!seq.pipelined) sweep_barrier(sh);                                 \
+        }                                                                          \
+        seq.advance(DY_);                                                          \
     } while (0)
+#define RZ_SWEEP(DX_, DY_, ADJ_, MODE_, LD_, ST_) RZ_SWEEP_D(DX_, DY_, ADJ_, MODE_, 1, LD_, ST_)
 
     if (!P.start_adjoint) {
         // ---------------- forward ----------------
@@ -1331,6 +1335,12 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             RZ_SWEEP(+1, -1, true, kModeExact, &M.lld, &M.lst);
             RZ_SWEEP(-1, +1, true, kModeExact, &M.lld, &M.lst);
             RZ_SWEEP(-1, -1, true, kModeExact, &M.lld, &M.lst);
+        } else if (MODE == kModeReference && !P.div_fast) {
+            RZ_SWEEP_D(+1, +1, true, MODE, 0, &M.lld, &M.lst);
+            if (pass == 0) stamp(P, z, 6);
+            RZ_SWEEP_D(+1, -1, true, MODE, 0, &M.lld, &M.lst);
+            RZ_SWEEP_D(-1, +1, true, MODE, 0, &M.lld, &M.lst);
+            RZ_SWEEP_D(-1, -1, true, MODE, 0, &M.lld, &M.lst);
         } else {
             RZ_SWEEP(+1, +1, true, MODE, &M.lld, &M.lst);
             if (pass == 0) stamp(P, z, 6);
@@ -1356,7 +1366,9 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             go = (tot / (double)n) >= (double)P.ttnorm;
         }
         if (go && !P.exact && P.skip && pass < P.max_passes) {
-            const int fx = adjoint_is_fixpoint<MODE>(P, &M.tchk, &M.lchk, z, &sh.w[g], &sh.ctl[2], w.abort_word);
+            const int fx = (MODE == kModeReference && !P.div_fast)
+                               ? adjoint_is_fixpoint<MODE, 0>(P, &M.tchk, &M.lchk, z, &sh.w[g], &sh.ctl[2], w.abort_word)
+                               : adjoint_is_fixpoint<MODE, 1>(P, &M.tchk, &M.lchk, z, &sh.w[g], &sh.ctl[2], w.abort_word);
             w.err |= fx >> 1;
             if (fx & 1) {
                 ++pass;  // the next pass would change nothing
@@ -1366,6 +1378,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
     }
     if (tid == 0) P.passes_adj[z] = pass;
 #undef RZ_SWEEP
+#undef RZ_SWEEP_D
     if (tid == 0 && P.swept) P.swept[2 * z + 1] = swept;
     stamp(P, z, 4);
     __syncthreads();
