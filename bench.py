@@ -259,9 +259,8 @@ def run_gpu_arm(args, rank, world, local_rank):
     clocks.stop()
     launches1, shot_ms, shot_calls = ctx.kernel_stats()
     if dist:
-        t = torch.tensor([ms], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
+        from rajzel_gb300 import ranks
+        ms = ranks.max_over_ranks(ms, dist, device=f"cuda:{local_rank}")
     value = world * w.nshots * args.steps / (ms / 1e3)
     kernel_ms = shot_ms / max(shot_calls, 1)
     alg_bytes = (pu_fwd * ALG_BYTES_FWD + pu_adj * ALG_BYTES_ADJ + int(checks[0]) * CHECK_BYTES_FWD * w.nx * w.ny
