@@ -66,6 +66,7 @@ struct rz_context {
     size_t memcap = 0;  // bytes the field slots may occupy; 0 = 90% of free device memory
     float *dT = nullptr, *dTold = nullptr, *dL = nullptr, *dTA = nullptr, *dTB = nullptr, *dEU = nullptr,
           *dED = nullptr;
+    uint8_t *dChg = nullptr;  // [slot][nstrips][4*(nxb+1)] change votes of a pass's last sweep
     float *dWZA = nullptr, *dWZB = nullptr, *dRA = nullptr, *dRB = nullptr;  // exact adjoint only
     bool fields_exact = false;
     ShotMaps maps{};  // tensor maps of the field buffers and the row-pitched slowness
@@ -193,6 +194,7 @@ static int make_map(rz_context *c, CUtensorMap *m, float *base, int depth, int b
 
 static void free_fields(rz_context *c) {
     dfree(c->dT), dfree(c->dTold), dfree(c->dL), dfree(c->dTA), dfree(c->dTB), dfree(c->dEU), dfree(c->dED);
+    dfree(c->dChg);
     dfree(c->dWZA), dfree(c->dWZB), dfree(c->dRA), dfree(c->dRB);
     c->fields_exact = false;
     c->cap_f = 0;
@@ -209,13 +211,13 @@ static void free_batch(rz_context *c) {
     free_shots(c);
 }
 
-// device bytes of one field slot: T, pass snapshot, lambda, two skewed T copies, border rows
-// (the exact adjoint adds skewed z weights and receiver terms, two copies each)
+// device bytes of one field slot: T, pass snapshot, lambda, two skewed T copies, border rows,
+// change votes (the exact adjoint adds skewed z weights and receiver terms, two copies each)
 static size_t slot_bytes(const rz_context *c) {
     const size_t fs = (size_t)c->g.ny * c->nxp, ss = (size_t)c->nstrips * c->qn * 32,
                  es = (size_t)c->nstrips * edge_row(c->nxp);
     const size_t extra = c->grad_kind == RZ_GRADIENT_EXACT ? 4 * ss : 0;
-    return 4 * (3 * fs + 2 * ss + 2 * es + extra);
+    return 4 * (3 * fs + 2 * ss + 2 * es + extra) + (size_t)c->nstrips * 4 * (c->nxb + 1);  // + change votes
 }
 
 static int ensure_fields(rz_context *c, int n) {
@@ -228,6 +230,7 @@ static int ensure_fields(rz_context *c, int n) {
     CK(dalloc(&c->dT, fs * n));
     CK(dalloc(&c->dTold, fs * n));
     CK(dalloc(&c->dL, fs * n));
+    CK(dalloc(&c->dChg, (size_t)c->nstrips * 4 * (c->nxb + 1) * n));
     CK(dalloc(&c->dTA, ss * n));
     CK(dalloc(&c->dTB, ss * n));
     CK(dalloc(&c->dEU, es * n));
@@ -403,6 +406,8 @@ static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     P.status = c->dStat + first;
     P.timeline = c->dTl + (size_t)first * kTimelineSlots;
     P.swept = c->dSwept + (size_t)first * 2;
+    P.chg = c->dChg;
+    P.chg_stride = (size_t)c->nstrips * 4 * (c->nxb + 1);
 }
 
 static int status_to_code(int bits) {

@@ -97,6 +97,11 @@ struct ShotParams {
     // change nothing is counted in passes_* but not swept
     int *swept;
     unsigned long long *timeline;           // [nshots][kTimelineSlots] ns stamps, or null
+    // change votes of the last sweep of a pass, [nshots][nstrips][4*(nxb+1)]
+    // bytes: group G of strip s changed a cell (fixpoint checks skip the
+    // tasks no change can reach), or null
+    uint8_t *chg;
+    size_t chg_stride;                      // nstrips*4*(nxb+1)
 };
 
 // Tensor maps of a launch.  Field maps cover [shots][ny][nxp] floats with

@@ -310,6 +310,10 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     // padded stream it reads (lines 0 .. 32*nxb+31 of the sweep)
     const uint32_t sg = smem_u32(w.ws->stage);
     const int ngroups = 4 * (nxb + 1);
+    // the last sweep of a pass ((+x,-y) forward, (-x,-y) Leung-Qian adjoint)
+    // votes per group of 8 steps whether it changed a cell of the strip
+    constexpr bool REC = !EX && (ADJ ? (DX < 0 && DY < 0) : (DX > 0 && DY < 0));
+    uint8_t *const chg = (REC && P.chg) ? P.chg + (size_t)z * P.chg_stride + (size_t)s * ngroups : nullptr;
     const float *xline = xs - j;  // the 32-float line of step 0
     auto stage_issue = [&](int G) {
         const uint32_t dst = sg;
@@ -468,6 +472,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
             // (every lane's 8 columns strictly inside the grid, every row of the
             // strip inside it) no cell is a boundary cell or outside the grid
             // and every hand-off value is in range: those tests are left out.
+            bool changed = false;  // REC: this lane changed a cell in this group
             auto steps8 = [&](auto interior_tag) {
                 constexpr bool INT = decltype(interior_tag)::value;
                 // lane 31 of a producing warp hands down the values of columns
@@ -582,12 +587,17 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     mbar_arrive_if(full_out + 8u * (uint32_t)(((upp0 + pb8) >> 3) & (kGroups - 1)), hand);
                 }
                 if (ii == 7) hand_carry = r;
+                if (REC) changed |= valid && r != own;
                 res_prev = r;
             }
             };
             // the columns of this group: t0-31 (lane 31) .. t0+7 (lane 0)
             if (rows_in && t0 - 31 >= lo + 1 && t0 + 7 <= hi_in - 2) steps8(BoolTag<true>{});
             else steps8(BoolTag<false>{});
+            if (REC && chg) {
+                const bool any = __any_sync(0xffffffffu, changed);
+                if (l == 0) chg[t0 >> 3] = any ? 1 : 0;
+            }
         }
         // block k-1 is complete: lane 0 writes the strip's 32 rows back (rows
         // past the grid are clipped by the map)
@@ -752,6 +762,27 @@ RZ_DEV Row4 box_row4(uint32_t row, int l) {
     return r;
 }
 
+// Whether the last sweep of the pass (x direction dx) changed a cell of a
+// strip touching rows [r_lo, r_hi] in a group of 8 steps whose columns meet
+// [c_lo, c_hi]; true without votes.  A cell none of whose neighbours changed
+// after that sweep evaluated it has the same update now, which it did not
+// fall below: the checks skip a task when no vote covers the task and the
+// cells around it.  Group G of a sweep covers sweep-local columns
+// 8G-31 .. 8G+7 (lanes 31 .. 0).
+RZ_DEV bool votes_any(const ShotParams &P, int z, int r_lo, int r_hi, int c_lo, int c_hi, int dx) {
+    if (!P.chg) return true;
+    const int l = threadIdx.x & 31, ng = 4 * (P.nxb + 1), ncol = kBlk * P.nxb;
+    r_lo = max(r_lo, 0), r_hi = min(r_hi, P.ny - 1);
+    const int s_lo = r_lo >> 5, s_hi = r_hi >> 5;
+    const int u_lo = dx > 0 ? c_lo : ncol - 1 - c_hi, u_hi = dx > 0 ? c_hi : ncol - 1 - c_lo;  // sweep-local
+    const int g_lo = max(0, u_lo >> 3), g_hi = min(ng - 1, (u_hi + 31) >> 3);  // 8G+7 >= u_lo, 8G-31 <= u_hi
+    const int ngs = g_hi - g_lo + 1, total = (s_hi - s_lo + 1) * max(ngs, 0);
+    const uint8_t *v = P.chg + (size_t)z * P.chg_stride;
+    bool any = false;
+    for (int i = l; i < total; i += 32) any |= v[(size_t)(s_lo + i / ngs) * ng + g_lo + i % ngs] != 0;
+    return __any_sync(0xffffffffu, any);
+}
+
 // box ring of a check: box b of a task sits in slot b % kCheckSlots
 struct CheckRing {
     uint32_t base, bars, abort_s, phase;
@@ -782,6 +813,7 @@ __device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUten
         const int base = (task % nch) << 7, h0 = base + 4 * l;
         // rows k0 .. k0+kk-1; window row j is grid row k0-1+j, j = 0 .. kk+1
         const int k0 = (task / nch) * rt, kk = min(ny - k0, rt);
+        if (!votes_any(P, z, k0 - 1, k0 + kk, base - 1, base + 128, +1)) continue;  // (+x,-y) was last
         const int nb = ((kk + 1) >> 2) + 1;
         auto issue = [&](int b) {
             if (b >= nb || l != 0) return;
@@ -864,6 +896,7 @@ __device__ __noinline__ int adjoint_is_fixpoint(const ShotParams &P, const CUten
         const int base = (task % nch) << 7, h0 = base + 4 * l;
         // interior rows k0 .. k0+kk-1 (k0 >= 1, k0+kk <= ny-1); window row j is grid row k0-1+j
         const int k0 = 1 + (task / nch) * rt, kk = min(ny - 1 - k0, rt);
+        if (!votes_any(P, z, k0 - 1, k0 + kk, base - 1, base + 128, -1)) continue;  // (-x,-y) was last
         const int nb = ((kk + 1) >> 2) + 1;
         auto issue = [&](int b) {
             if (b >= nb || l != 0) return;
