@@ -73,9 +73,11 @@ cudaError_t launch_skip_masks(const uint8_t *skip, int nx, int ny, int nstrips, 
 // Interior cells only; frame cells stay 0 until the frame copy.
 //   reference: per shot RN32(RN64(lam * cube)) with cube = pow(S,3) from the
 //              host C library, summed in float in shot order
-//   fast:      lam * S^3 summed in double (grad64), rounded into grad
+//   fast:      S^3 (double) times the shots' lam summed by shot_sum_fixed,
+//              kept in double (grad64) and rounded into grad
 // With `accumulate` the sums continue from grad (reference) / grad64 (fast),
-// so a batch stacked chunk by chunk in shot order gives the same result.
+// so a batch stacked chunk by chunk in shot order gives the same result
+// (in fast mode up to the double roundings of the partial sums).
 __global__ void stack_kernel(const float *L, size_t fstride, int nshots, const double *cube, const float *S, int nx,
                              int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, bool accumulate) {
     const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
@@ -99,18 +101,7 @@ __global__ void stack_kernel(const float *L, size_t fstride, int nshots, const d
         if (interior) {
             const float sv = S[(size_t)k * nx + h];
             const double cb = (double)sv * (double)sv * (double)sv;
-            // four independent sums keep four shots' loads in flight per thread
-            double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
-            int z = 0;
-            for (; z + 3 < nshots; z += 4) {
-                const float *q = L + (size_t)z * fstride + o;
-                a0 += (double)__ldg(q);
-                a1 += (double)__ldg(q + fstride);
-                a2 += (double)__ldg(q + 2 * fstride);
-                a3 += (double)__ldg(q + 3 * fstride);
-            }
-            for (; z < nshots; ++z) a0 += (double)__ldg(L + (size_t)z * fstride + o);
-            acc = ((a0 + a1) + (a2 + a3)) * cb;
+            acc = shot_sum_fixed(L + o, fstride, nshots) * cb;
         }
         if (accumulate && grad64) acc += grad64[og];
         if (grad64) grad64[og] = acc;

@@ -409,4 +409,62 @@ RZ_DEV ExactCoef exact_coef(const float *T, int nxp, int nx, int ny, int h, int 
     return c;
 }
 
+// Sum of the n floats q[0], q[stride], ..., q[(n-1)*stride] as a double,
+// accumulated on the integer pipe.  GB300 issues FP64 at about two operations
+// per SM cycle, so a plain double sum (a float->double conversion and an add
+// per value) is bound by the FP64 pipe; this sum costs one conversion per 128
+// values.
+//
+// Each value m * 2^(e-150) (m the 24-bit significand, e the biased exponent,
+// 1 for subnormals) is added as the integer (m << 31) >> (emax - e) to a
+// 64-bit fixed-point word whose unit is 2^(emax-181), emax the largest
+// exponent seen so far; a larger exponent first shifts the word right
+// (arithmetic) by the difference.  Every term and every shift drops less than
+// one unit, i.e. less than 2^-54 of the largest |value|; with an exponent
+// span of at most 31 nothing is dropped and the word is the exact sum.
+// Blocks of 128 values stay below 2^62 (|term| < 2^55) and are converted to
+// double once each (one rounding), so the error is below
+// n * 2^-53 * max|q| + 2^-53 per block of the block sum -- within the bound
+// of a plain double sum, (n-1) * 2^-53 * sum|q|.  A block holding an Inf or
+// NaN is summed in double instead, so non-finite values propagate as there.
+RZ_DEV double shot_sum_fixed(const float *__restrict__ q, size_t stride, int n) {
+    constexpr int kBlock = 128;
+    double total = 0.0;
+    for (int z0 = 0; z0 < n; z0 += kBlock) {
+        const int z1 = min(n, z0 + kBlock);
+        long long acc = 0;
+        int emax = 1;
+        uint32_t special = 0;
+        auto add = [&](uint32_t u) {
+            const int ef = (int)((u >> 23) & 0xffu);
+            special |= (uint32_t)(ef == 0xff);
+            const int e = max(ef, 1);
+            const int up = max(e - emax, 0);
+            acc >>= min(up, 63);
+            emax += up;
+            const long long m = (long long)((u & 0x7fffffu) | (ef ? 0x800000u : 0u)) << 31;
+            const long long x = m >> min(emax - e, 63);
+            acc += (u >> 31) ? -x : x;
+        };
+        int z = z0;
+        for (; z + 7 < z1; z += 8) {
+            uint32_t u[8];
+#pragma unroll
+            for (int i = 0; i < 8; ++i) u[i] = __float_as_uint(__ldg(q + (size_t)(z + i) * stride));
+#pragma unroll
+            for (int i = 0; i < 8; ++i) add(u[i]);
+        }
+        for (; z < z1; ++z) add(__float_as_uint(__ldg(q + (size_t)z * stride)));
+        if (special) {
+            double s = 0.0;
+            for (z = z0; z < z1; ++z) s += (double)__ldg(q + (size_t)z * stride);
+            total += s;
+        } else {
+            // exact power-of-two scale 2^(emax-181), emax in [1, 254]
+            total += (double)acc * __longlong_as_double((long long)(emax - 181 + 1023) << 52);
+        }
+    }
+    return total;
+}
+
 }  // namespace rz

@@ -1,5 +1,6 @@
-// rz_selftest.cu -- device self-tests of the point-update arithmetic, built
-// into librz_selftest.so for the GPU test-suite only.
+// rz_selftest.cu -- device self-tests of the point-update arithmetic and of
+// the gradient stack's shot sum, built into librz_selftest.so for the GPU
+// test-suite only.
 //
 // rz_selftest_godunov draws n seeded random update inputs (neighbour minima
 // a, b within a few cell-times of each other, slowness 1/6000..1/1400 s/m,
@@ -58,4 +59,38 @@ extern "C" int rz_selftest_godunov(unsigned long long seed, long n, unsigned lon
     if (e != cudaSuccess) return 3;
     *bad_out = h[0];
     return 0;
+}
+
+namespace {
+
+__global__ void shot_sum_check(const float *vals, long ncells, int nshots, double *out) {
+    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (c >= ncells) return;
+    out[c] = rz::shot_sum_fixed(vals + c, (size_t)ncells, nshots);
+}
+
+}  // namespace
+
+// rz_selftest_shot_sum: out[c] = shot_sum_fixed over vals[z * ncells + c],
+// z < nshots, for host arrays vals [nshots][ncells] and out [ncells].
+extern "C" int rz_selftest_shot_sum(const float *vals, long ncells, int nshots, double *out) {
+    if (ncells <= 0 || nshots < 0) return 1;
+    float *dv = nullptr;
+    double *dout = nullptr;
+    const size_t nv = (size_t)ncells * (size_t)(nshots > 0 ? nshots : 1);
+    if (cudaMalloc(&dv, nv * sizeof(float)) != cudaSuccess) return 3;
+    if (cudaMalloc(&dout, (size_t)ncells * sizeof(double)) != cudaSuccess) {
+        cudaFree(dv);
+        return 3;
+    }
+    cudaError_t e = cudaSuccess;
+    if (nshots > 0) e = cudaMemcpy(dv, vals, (size_t)ncells * nshots * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        shot_sum_check<<<(unsigned)((ncells + 255) / 256), 256>>>(dv, ncells, nshots, dout);
+        e = cudaDeviceSynchronize();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(out, dout, (size_t)ncells * sizeof(double), cudaMemcpyDeviceToHost);
+    cudaFree(dv);
+    cudaFree(dout);
+    return e == cudaSuccess ? 0 : 3;
 }

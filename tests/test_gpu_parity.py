@@ -9,6 +9,7 @@ FP64 oracle than twice the reference's own float arithmetic plus 1e-4
 import ctypes as C
 import glob
 import hashlib
+import math
 import os
 
 import numpy as np
@@ -249,6 +250,60 @@ def test_certified_godunov_branch_matches_double(R):
     bad = C.c_ulonglong(1)
     assert lib.rz_selftest_godunov(12345, 20_000_000, C.byref(bad)) == 0
     assert bad.value == 0
+
+
+def _shot_sum(R, vals):
+    lib = C.CDLL(os.path.join(os.path.dirname(R.__file__), "librz_selftest.so"))
+    lib.rz_selftest_shot_sum.argtypes = [C.c_void_p, C.c_long, C.c_int, C.c_void_p]
+    vals = np.ascontiguousarray(vals, dtype=np.float32)
+    nshots, ncells = vals.shape
+    out = np.full(ncells, np.nan)
+    assert lib.rz_selftest_shot_sum(vals.ctypes.data, ncells, nshots, out.ctypes.data) == 0
+    return out
+
+
+def _exact_sums(vals):
+    """Correctly rounded sums of the columns (math.fsum of the exact values)."""
+    return np.array([math.fsum(col) for col in vals.astype(np.float64).T])
+
+
+def test_stack_shot_sum_fixed_point(R):
+    """The fast-mode stack sums a cell's shots in a 64-bit fixed-point word.
+    With an exponent span of at most 31 within 128 shots nothing is dropped
+    and the result is the correctly rounded exact sum; over any span and
+    shot count the error stays within n 2^-53 max|x| plus one double
+    rounding per 128-shot block and per block sum."""
+    rng = np.random.default_rng(5)
+    ncells = 3001  # not a multiple of the 256-thread block
+    for n in (0, 1, 7, 100, 128):
+        mag = (1.0 + rng.random((n, ncells))) * 2.0 ** rng.integers(-12, 13, (n, ncells))
+        v = (np.where(rng.random((n, ncells)) < 0.5, -mag, mag) * (rng.random((n, ncells)) > 0.05))
+        v = v.astype(np.float32)
+        got = _shot_sum(R, v)
+        assert np.array_equal(got, _exact_sums(v) if n else np.zeros(ncells))
+    # subnormals only: exact
+    v = (rng.integers(-2**20, 2**20, (50, ncells)) * 2.0**-149).astype(np.float32)
+    assert np.array_equal(_shot_sum(R, v), _exact_sums(v))
+    # exponents over +-100 (dropped low bits), several 128-shot blocks
+    for n in (129, 300, 1000):
+        mag = (1.0 + rng.random((n, ncells))) * 2.0 ** rng.integers(-100, 101, (n, ncells))
+        v = np.where(rng.random((n, ncells)) < 0.5, -mag, mag).astype(np.float32)
+        got = _shot_sum(R, v)
+        a = np.abs(v.astype(np.float64))
+        bound = 2.0**-53 * (n * a.max(axis=0) + 2 * (-(-n // 128)) * a.sum(axis=0))
+        assert np.all(np.abs(got - _exact_sums(v)) <= bound)
+    # cancellation inside one block, and non-finite values propagate as in double
+    v = np.zeros((6, 6), np.float32)
+    v[:3, 0] = [3.0e30, 1.0, -3.0e30]
+    v[:2, 1] = [np.inf, 1.0]
+    v[:2, 2] = [-np.inf, 2.0]
+    v[:2, 3] = [np.inf, -np.inf]
+    v[:3, 4] = [1.0, np.nan, 2.0]
+    v[:, 5] = -0.0
+    got = _shot_sum(R, v)
+    # 1.0 is 101 binades below 3e30: dropped, as a double sum drops it
+    assert got[0] == 0.0 and got[1] == np.inf and got[2] == -np.inf
+    assert np.isnan(got[3]) and np.isnan(got[4]) and got[5] == 0.0
 
 
 def test_invalid_model_is_rejected_with_its_cell(R):
