@@ -50,7 +50,16 @@ struct rz_context {
     float *dSp = nullptr;  // slowness in rows of nxp floats (fixpoint checks)
     double *dCube = nullptr;
     bool cube_valid = false;
-    int *dBad = nullptr;  // launch_check_model result
+    int *dBad = nullptr;  // launch_prep_model result
+    // words the device writes into mapped pinned host memory (host / device
+    // address), read after a stream wait without a copy
+    struct HostWords {
+        double l2;   // misfit of a gradient call
+        int status;  // OR of the shots' status words
+        int bad;     // launch_prep_model result
+    };
+    HostWords *hw = nullptr, *hwDev = nullptr;
+    bool host_coherent = false;  // the device reaches every host address coherently (Grace C2C)
 
     // receivers
     bool rec_set = false;
@@ -580,6 +589,18 @@ int rz_create(rz_context **out, int device) {
         return RZ_ECUDA;
     }
     c->st = c->own;
+    int coherent = 0;
+    if (cudaDeviceGetAttribute(&coherent, cudaDevAttrPageableMemoryAccessUsesHostPageTables, device) != cudaSuccess)
+        coherent = 0, (void)cudaGetLastError();
+    c->host_coherent = coherent != 0;
+    void *h = nullptr, *d = nullptr;
+    if (cudaHostAlloc(&h, sizeof(rz_context::HostWords), cudaHostAllocMapped) == cudaSuccess &&
+        cudaHostGetDevicePointer(&d, h, 0) == cudaSuccess) {
+        c->hw = (rz_context::HostWords *)h, c->hwDev = (rz_context::HostWords *)d;
+    } else {
+        if (h) cudaFreeHost(h);
+        (void)cudaGetLastError();  // results are then read back by copies
+    }
     *out = c;
     return RZ_OK;
 }
@@ -592,6 +613,7 @@ void rz_destroy(rz_context *c) {
     for (auto &pr : c->shot_events) cudaEventDestroy(pr.first), cudaEventDestroy(pr.second);
     dfree(c->dS), dfree(c->dSA), dfree(c->dSB), dfree(c->dVp), dfree(c->dCube), dfree(c->dGrad), dfree(c->dL2);
     dfree(c->dBad);
+    if (c->hw) cudaFreeHost(c->hw);
     dfree(c->dSp);
     dfree(c->dRecH), dfree(c->dRecK), dfree(c->dRcH), dfree(c->dRcK), dfree(c->dRcRec), dfree(c->dSkip);
     dfree(c->dSkipP);
@@ -644,20 +666,36 @@ int rz_set_grid(rz_context *c, const rz_grid *g) {
     return RZ_OK;
 }
 
-static int set_model_common(rz_context *c) {
+// The device address of pinned host memory at p when the device reads host
+// memory coherently (Grace's C2C link): a kernel then reads the caller's
+// buffer directly instead of a staging copy.  Null otherwise.
+static const float *coherent_host(const rz_context *c, const float *p) {
+    if (!c->host_coherent) return nullptr;
+    cudaPointerAttributes a{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        (void)cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost && a.devicePointer ? (const float *)a.devicePointer : nullptr;
+}
+
+// src: the velocity (is_vp) or slowness on the device, or pinned host memory
+// from coherent_host; one preparation launch, the skewed copies, one wait
+static int set_model_common(rz_context *c, const float *src, bool is_vp) {
     const int nx = c->g.nx, ny = c->g.ny;
     const size_t skew = (size_t)c->nstrips * c->qn * 32;
     if (!c->dSA) {
         CK(dalloc(&c->dSA, skew));
         CK(dalloc(&c->dSB, skew));
     }
-    CK(launch_skew_field(c->dS, nx, ny, nx, c->nstrips, c->nxb, c->dSA, c->dSB, c->st));
-    CK(cudaMemcpy2DAsync(c->dSp, (size_t)c->nxp * 4, c->dS, (size_t)nx * 4, (size_t)nx * 4, ny,
-                         cudaMemcpyDeviceToDevice, c->st));
-    CK(launch_check_model(c->dS, (long)nx * ny, c->dBad, c->st));
+    CK(launch_prep_model(src, is_vp, c->dS, c->dSp, nx, ny, c->nxp, c->dBad, c->st));
+    // the skew launch hands the check's result to pinned host memory
+    CK(launch_skew_field(c->dS, nx, ny, nx, c->nstrips, c->nxb, c->dSA, c->dSB, c->st, c->dBad,
+                         c->hw ? &c->hwDev->bad : nullptr));
     int bad = kModelOk;
-    CK(cudaMemcpyAsync(&bad, c->dBad, sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    if (!c->hw) CK(cudaMemcpyAsync(&bad, c->dBad, sizeof(int), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
+    if (c->hw) bad = *(volatile int *)&c->hw->bad;
     if (bad != kModelOk) {
         c->model_set = false;
         return fail(c, RZ_EINVAL, "slowness at cell %d is not a positive finite number", bad);
@@ -691,8 +729,12 @@ int rz_set_slowness(rz_context *c, const float *S, int flags) {
     int r;
     if ((r = alloc_model(c))) return r;
     const size_t n = (size_t)c->g.nx * c->g.ny;
-    CK(cudaMemcpyAsync(c->dS, S, n * 4, have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
-    return set_model_common(c);
+    const float *src = S;
+    if (!have_dev(flags) && !(src = coherent_host(c, S))) {
+        CK(cudaMemcpyAsync(c->dS, S, n * 4, cudaMemcpyHostToDevice, c->st));
+        src = c->dS;
+    }
+    return set_model_common(c, src, false);
 }
 
 int rz_set_velocity(rz_context *c, const float *vp, int flags) {
@@ -706,13 +748,12 @@ int rz_set_velocity(rz_context *c, const float *vp, int flags) {
     if ((r = alloc_model(c))) return r;
     const size_t n = (size_t)c->g.nx * c->g.ny;
     const float *src = vp;
-    if (!have_dev(flags)) {
+    if (!have_dev(flags) && !(src = coherent_host(c, vp))) {
         if (!c->dVp) CK(dalloc(&c->dVp, n));
         CK(cudaMemcpyAsync(c->dVp, vp, n * 4, cudaMemcpyHostToDevice, c->st));
         src = c->dVp;
     }
-    CK(launch_calc_s(src, c->dS, (long)n, c->st));
-    return set_model_common(c);
+    return set_model_common(c, src, true);
 }
 
 int rz_set_receivers(rz_context *c, int ntr, const int *recx, const int *recz) {
@@ -965,6 +1006,20 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
     }
     if (have_dev(flags)) {
         if (L2) CK(cudaMemcpyAsync(L2, c->dL2, sizeof(double), cudaMemcpyDeviceToDevice, c->st));
+        return RZ_OK;
+    }
+    float *gh = c->hw ? (float *)coherent_host(c, grad) : nullptr;
+    if (gh) {
+        // one launch writes the gradient into the caller's pinned buffer and
+        // the misfit and status words into mapped host words: no copies
+        CK(launch_finish_grad(gdst, gh, (long)c->g.nx * c->g.ny, c->dL2, &c->hwDev->l2, c->dStat, nshots,
+                              &c->hwDev->status, c->st));
+        c->launches += 1;
+        CK(cudaStreamSynchronize(c->st));
+        if (L2) *L2 = *(volatile double *)&c->hw->l2;
+        const int worst = *(volatile int *)&c->hw->status;
+        const int code = status_to_code(worst);
+        if (code != RZ_OK) return fail(c, code, "device status bits 0x%x", worst);
         return RZ_OK;
     }
     CK(cudaMemcpyAsync(grad, gdst, (size_t)c->g.nx * c->g.ny * 4, cudaMemcpyDeviceToHost, c->st));

@@ -7,9 +7,11 @@
 namespace rz {
 
 // X[s][q][j] <- src(row 32s+j, column h) for both skew families (see
-// rz_internal.h); cells outside the grid read as 0.
+// rz_internal.h); cells outside the grid read as 0.  With note_dst, thread 0
+// first copies *note_src there (a word an earlier launch on the stream wrote).
 __global__ void skew_field_kernel(const float *src, int nx, int ny, int pitch, int nstrips, int qn, float *A,
-                                  float *B) {
+                                  float *B, const int *note_src, int *note_dst) {
+    if (note_dst && blockIdx.x == 0 && threadIdx.x == 0) *note_dst = *note_src;
     const int j = threadIdx.x & 31;
     const long gline = (long)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     if (gline >= (long)nstrips * qn) return;
@@ -28,12 +30,12 @@ __global__ void skew_field_kernel(const float *src, int nx, int ny, int pitch, i
 }
 
 cudaError_t launch_skew_field(const float *src, int nx, int ny, int pitch, int nstrips, int nxb, float *dstA,
-                              float *dstB, cudaStream_t st) {
+                              float *dstB, cudaStream_t st, const int *note_src, int *note_dst) {
     const int qn = skew_lines(nxb);
     const long lines = (long)nstrips * qn;
     const int wpb = 8;
     skew_field_kernel<<<(unsigned)((lines + wpb - 1) / wpb), 32 * wpb, 0, st>>>(src, nx, ny, pitch, nstrips, qn, dstA,
-                                                                              dstB);
+                                                                              dstB, note_src, note_dst);
     return cudaGetLastError();
 }
 
@@ -221,30 +223,60 @@ cudaError_t launch_check_div(float dh, float rcp, unsigned int *bad, cudaStream_
     return cudaGetLastError();
 }
 
-__global__ void calc_s_kernel(const float *vp, float *S, long n) {
-    const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
-    if (c < n) S[c] = __double2float_rn(__drcp_rn((double)vp[c]));
-}
-
-cudaError_t launch_calc_s(const float *vp, float *S, long n, cudaStream_t st) {
-    calc_s_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(vp, S, n);
-    return cudaGetLastError();
-}
-
-// the index of the first cell whose slowness is not a positive finite number
-// (atomicMin), or kModelOk when there is none
-__global__ void check_model_kernel(const float *S, long n, int *first_bad) {
+// Model preparation, one pass over the cells: the slowness S (calc_S.c:21:
+// 1/vp in double, rounded to float; or the caller's slowness as given), its
+// copy Sp in rows of nxp floats (the fixpoint checks' layout), and the index
+// of the first cell whose slowness is not a positive finite number
+// (atomicMin into first_bad, set to kModelOk before the launch).  src may be
+// pinned host memory that the device reads directly.
+__global__ void prep_model_kernel(const float *src, bool is_vp, float *S, float *Sp, int nx, long n, int nxp,
+                                  int *first_bad) {
     for (long c = (long)blockIdx.x * blockDim.x + threadIdx.x; c < n; c += (long)gridDim.x * blockDim.x) {
-        const float s = S[c];
+        const float v = src[c];
+        const float s = is_vp ? __double2float_rn(__drcp_rn((double)v)) : v;
+        if (S != src) S[c] = s;
+        const long k = c / nx;
+        Sp[k * nxp + (c - k * nx)] = s;
         if (!(s > 0.f) || !isfinite(s)) atomicMin(first_bad, (int)c);
     }
 }
 
-cudaError_t launch_check_model(const float *S, long n, int *first_bad, cudaStream_t st) {
+cudaError_t launch_prep_model(const float *src, bool is_vp, float *S, float *Sp, int nx, int ny, int nxp,
+                              int *first_bad, cudaStream_t st) {
     cudaError_t e = cudaMemsetAsync(first_bad, 0x7f, sizeof(int), st);  // kModelOk
     if (e != cudaSuccess) return e;
+    const long n = (long)nx * ny;
     const long blocks = std::min((n + 255) / 256, 152L * 8);
-    check_model_kernel<<<(unsigned)std::max(blocks, 1L), 256, 0, st>>>(S, n, first_bad);
+    prep_model_kernel<<<(unsigned)std::max(blocks, 1L), 256, 0, st>>>(src, is_vp, S, Sp, nx, n, nxp, first_bad);
+    return cudaGetLastError();
+}
+
+// The end of a gradient call into host memory the device writes directly:
+// the n-float gradient g into gout, and from block 0 the misfit and the OR of
+// the nshots status words into mapped host words.
+__global__ void finish_grad_kernel(const float *g, float *gout, long n, const double *l2, double *l2_out,
+                                   const int *status, int nshots, int *status_out) {
+    for (long i = (long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (long)gridDim.x * blockDim.x)
+        gout[i] = g[i];
+    if (blockIdx.x != 0) return;
+    __shared__ int worst;
+    if (threadIdx.x == 0) worst = 0;
+    __syncthreads();
+    int v = 0;
+    for (int i = threadIdx.x; i < nshots; i += blockDim.x) v |= status[i];
+    if (v) atomicOr(&worst, v);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        *status_out = worst;
+        *l2_out = *l2;
+    }
+}
+
+cudaError_t launch_finish_grad(const float *g, float *gout, long n, const double *l2, double *l2_out,
+                               const int *status, int nshots, int *status_out, cudaStream_t st) {
+    const long blocks = std::min((n + 255) / 256, 152L * 4);
+    finish_grad_kernel<<<(unsigned)std::max(blocks, 1L), 256, 0, st>>>(g, gout, n, l2, l2_out, status, nshots,
+                                                                         status_out);
     return cudaGetLastError();
 }
 

@@ -144,7 +144,7 @@ cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const ShotMaps &ma
 
 // launchers (rz_aux.cu)
 cudaError_t launch_skew_field(const float *src, int nx, int ny, int pitch, int nstrips, int nxb, float *dstA,
-                              float *dstB, cudaStream_t st);
+                              float *dstB, cudaStream_t st, const int *note_src = nullptr, int *note_dst = nullptr);
 cudaError_t launch_skip_masks(const uint8_t *skip, int nx, int ny, int nstrips, int nxb, uint32_t *MA, uint32_t *MB,
                               cudaStream_t st);
 // gradient stack: grad = cp_grad_frame^2( sum_s  RN32(lam_s * cube) )
@@ -163,10 +163,15 @@ cudaError_t launch_cp_frame(float *A, double *A64, int nx, int ny, int pitch, in
 cudaError_t launch_copy_rows(const float *src, int src_pitch, float *dst, int dst_pitch, int nx, int ny,
                              size_t nbatch, size_t src_bstride, size_t dst_bstride, cudaStream_t st);
 cudaError_t launch_check_div(float dh, float rcp, unsigned int *bad, cudaStream_t st);
-// S = (float)(1.0/(double)vp) per cell (calc_S.c:21)
-cudaError_t launch_calc_s(const float *vp, float *S, long n, cudaStream_t st);
-constexpr int kModelOk = 0x7f7f7f7f;  // launch_check_model: no invalid cell (grids have fewer cells)
-cudaError_t launch_check_model(const float *S, long n, int *first_bad, cudaStream_t st);
+// S = (float)(1.0/(double)vp) per cell (calc_S.c:21), its nxp-pitch copy and
+// the first invalid cell, in one launch (after resetting *first_bad)
+constexpr int kModelOk = 0x7f7f7f7f;  // launch_prep_model: no invalid cell (grids have fewer cells)
+cudaError_t launch_prep_model(const float *src, bool is_vp, float *S, float *Sp, int nx, int ny, int nxp,
+                              int *first_bad, cudaStream_t st);
+// gout[0..n) = g, *l2_out = *l2, *status_out = OR of status[0..nshots): the
+// end of a gradient call whose outputs are host memory the device writes
+cudaError_t launch_finish_grad(const float *g, float *gout, long n, const double *l2, double *l2_out,
+                               const int *status, int nshots, int *status_out, cudaStream_t st);
 // *out = 0.5 * sum_z l2[z], summed in shot order in double (grad_obj.c:28,42,61)
 cudaError_t launch_sum_l2(const double *l2, int n, double *out, cudaStream_t st);
 

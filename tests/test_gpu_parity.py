@@ -330,6 +330,50 @@ def test_invalid_model_is_rejected_with_its_cell(R):
     assert np.array_equal(TT0, TT1)
 
 
+@pytest.mark.parametrize("mode", ["reference", "fast"])
+def test_pinned_host_models_match_pageable(R, mode):
+    """A velocity or slowness in pinned host memory (read by the device
+    directly where it reaches host memory coherently) gives the results of
+    the same model in pageable memory, and an invalid pinned model is refused
+    with its first bad cell."""
+    torch = pytest.importorskip("torch")
+    w = synth.small_case(31, 90, 70, nshots=3)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    Tobs = _noisy_picks(p, w, S, 3, 5)
+    ctx = make_ctx(R, w, mode=mode)
+    ctx.set_velocity(w.vp_start)
+    g0, l0 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    vp = torch.empty((w.ny, w.nx), dtype=torch.float32, pin_memory=True).numpy()
+    vp[...] = w.vp_start
+    ctx.set_velocity(vp)
+    g1, l1 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    assert np.array_equal(g1, g0) and l1 == l0
+    Sp = torch.empty((w.ny, w.nx), dtype=torch.float32, pin_memory=True).numpy()
+    Sp[...] = synth.slowness(w.vp_start)
+    ctx.set_slowness(Sp)
+    g2, l2 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    ctx.set_slowness(synth.slowness(w.vp_start))
+    g3, l3 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    assert np.array_equal(g2, g3) and l2 == l3
+    # the gradient into a pinned buffer (written by the device where it
+    # reaches host memory), the misfit and the status words alongside
+    ctx.set_velocity(w.vp_start)
+    gpin = torch.zeros((w.ny, w.nx), dtype=torch.float32, pin_memory=True).numpy()
+    g4, l4 = ctx.grad_obj(w.srcx, w.srcz, Tobs, out=gpin)
+    assert g4 is gpin and np.array_equal(gpin, g0) and l4 == l0
+    ctx1 = make_ctx(R, w, mode=mode, max_passes=1)
+    with pytest.raises(R.RajzelError) as e:
+        ctx1.grad_obj(w.srcx, w.srcz, Tobs, out=gpin)
+    assert e.value.status == R.RZ_ENOCONV
+    vp[4, 6] = -1.0
+    with pytest.raises(R.RajzelError) as e:
+        ctx.set_velocity(vp)
+    assert e.value.status == R.RZ_EINVAL and f"cell {4 * w.nx + 6} " in str(e.value)
+    ctx.set_velocity(w.vp_start)
+    assert np.array_equal(ctx.grad_obj(w.srcx, w.srcz, Tobs)[0], g0)
+
+
 def test_errors_are_status_codes(R):
     w = synth.small_case(1, 30, 20, nshots=1)
     ctx = R.Context(0)
