@@ -45,7 +45,7 @@ extern "C" {
 #define RZ_ENOMEM 4          /* device allocation failed */
 #define RZ_ETIMEOUT 5        /* a bounded device-side wait gave up (kernel returned cleanly) */
 #define RZ_ESTATE 6          /* call order: grid/model/receivers not set */
-#define RZ_EUNSUPPORTED 7    /* grid shape beyond this build's kernel limits */
+#define RZ_EUNSUPPORTED 7    /* grid shape beyond the kernels' limits */
 
 /* arithmetic modes */
 #define RZ_MODE_REFERENCE 0  /* bit-identical to the reference's float/double arithmetic */
