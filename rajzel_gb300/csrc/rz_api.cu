@@ -526,17 +526,24 @@ static bool contains(const std::vector<cudaEvent_t> &v, cudaEvent_t e) {
     return std::find(v.begin(), v.end(), e) != v.end();
 }
 
-// gradient contribution of the shots first..first+m-1 (fields in slots 0..m-1)
-static int stack_chunk(rz_context *c, int first, int m, float *gdst) {
+// gradient contribution of the shots first..first+m-1 (fields in slots 0..m-1).
+// whole: these are all the batch's shots.  *finished: the launch also wrote
+// the frame cells and the misfit (a whole Leung-Qian batch), so neither the
+// frame copy nor the misfit sum follows.
+static int stack_chunk(rz_context *c, int first, int m, float *gdst, bool whole = false, bool *finished = nullptr) {
     const size_t fs = (size_t)c->g.ny * c->nxp;
+    bool fin = false;
     if (c->grad_kind == RZ_GRADIENT_EXACT) {
         CK(launch_stack_exact(c->dT, c->dL, fs, m, c->dSrcH + first, c->dSrcK + first, c->dS, c->g.nx, c->g.ny,
                               c->nxp, c->g.dh, gdst, c->dGrad64, first > 0, c->st));
     } else {
+        fin = whole && first == 0 && c->g.nx >= 5 && c->g.ny >= 5 && c->dL2;
         CK(launch_stack(c->dL, fs, m, c->dCube, c->dS, c->g.nx, c->g.ny, c->nxp, c->mode, gdst, c->g.nx,
-                        c->mode == RZ_MODE_FAST ? c->dGrad64 : nullptr, first > 0, c->st));
+                        c->mode == RZ_MODE_FAST ? c->dGrad64 : nullptr, first > 0, c->st, fin,
+                        fin ? c->dl2 : nullptr, fin ? m : 0, fin ? c->dL2 : nullptr));
     }
     c->launches += 1;
+    if (finished) *finished = fin;
     return RZ_OK;
 }
 
@@ -907,11 +914,13 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
     auto sequence = [&]() -> int {
         int q;
         if ((q = reset_shots(c, nshots))) return q;
+        bool finished = false;
         for (int first = 0; first < nshots; first += chunk) {
             const int m = nshots - first < chunk ? nshots - first : chunk;
             if ((q = run_batch(c, first, m, true, true, false, exact))) return q;
-            if ((q = stack_chunk(c, first, m, gdst))) return q;
+            if ((q = stack_chunk(c, first, m, gdst, m == nshots, &finished))) return q;
         }
+        if (finished) return RZ_OK;
         if (!exact) {
             CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, c->st));
             c->launches += 1;
@@ -1157,11 +1166,14 @@ int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, co
             gdst = c->dGrad;
         }
         if (c->mode == RZ_MODE_FAST && !c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
-        if ((r = stack_chunk(c, 0, nshots[i], gdst))) return fail(c0, r, "%s", c->err.c_str());
-        CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, st));
         if (!c->dL2) CK(dalloc(&c->dL2, 1));
-        CK(launch_sum_l2(c->dl2, nshots[i], c->dL2, st));
-        c->launches += 2;
+        bool finished = false;
+        if ((r = stack_chunk(c, 0, nshots[i], gdst, true, &finished))) return fail(c0, r, "%s", c->err.c_str());
+        if (!finished) {
+            CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, st));
+            CK(launch_sum_l2(c->dl2, nshots[i], c->dL2, st));
+            c->launches += 2;
+        }
         CK(cudaMemcpyAsync(L2 + i, c->dL2, sizeof(double),
                            have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));
         if (!have_dev(flags))

@@ -80,13 +80,27 @@ cudaError_t launch_skip_masks(const uint8_t *skip, int nx, int ny, int nstrips, 
 // With `accumulate` the sums continue from grad (reference) / grad64 (fast),
 // so a batch stacked chunk by chunk in shot order gives the same result
 // (in fast mode up to the double roundings of the partial sums).
+// With `frame` (one chunk only, nx, ny >= 5) every cell takes the stack of
+// the cell nearest to it two cells inside the grid: what the frame copy
+// (cp_grad_frame.c:18-49) leaves there.  With l2_out, thread 0 also writes
+// 0.5 * the shot-order double sum of l2[0..nl2) (grad_obj.c:28,42,61).
 __global__ void stack_kernel(const float *L, size_t fstride, int nshots, const double *cube, const float *S, int nx,
-                             int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, bool accumulate) {
+                             int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, bool accumulate,
+                             bool frame, const double *l2, int nl2, double *l2_out) {
     const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (l2_out && c == 0) {
+        double sum = 0.0;
+        for (int i = 0; i < nl2; ++i) sum = __dadd_rn(sum, l2[i]);
+        *l2_out = __dmul_rn(0.5, sum);
+    }
     if (c >= (long)nx * ny) return;
-    const int k = (int)(c / nx), h = (int)(c - (long)k * nx);
-    const size_t o = (size_t)k * nxp + h;
+    int k = (int)(c / nx), h = (int)(c - (long)k * nx);
     const size_t og = (size_t)k * gpitch + h;
+    if (frame) {
+        k = min(max(k, 2), ny - 3);
+        h = min(max(h, 2), nx - 3);
+    }
+    const size_t o = (size_t)k * nxp + h;
     const bool interior = (h > 0 && h < nx - 1 && k > 0 && k < ny - 1);
     if (mode == kModeReference) {
         float acc = accumulate ? grad[og] : 0.f;
@@ -113,10 +127,11 @@ __global__ void stack_kernel(const float *L, size_t fstride, int nshots, const d
 
 cudaError_t launch_stack(const float *L, size_t fstride, int nshots, const double *cube, const float *S, int nx,
                          int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, bool accumulate,
-                         cudaStream_t st) {
+                         cudaStream_t st, bool frame, const double *l2, int nl2, double *l2_out) {
+    if (frame && (accumulate || nx < 5 || ny < 5)) return cudaErrorInvalidValue;
     const long n = (long)nx * ny;
     stack_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(L, fstride, nshots, cube, S, nx, ny, nxp, mode, grad,
-                                                           gpitch, grad64, accumulate);
+                                                           gpitch, grad64, accumulate, frame, l2, nl2, l2_out);
     return cudaGetLastError();
 }
 

@@ -147,13 +147,18 @@ cudaError_t launch_skew_field(const float *src, int nx, int ny, int pitch, int n
                               float *dstB, cudaStream_t st, const int *note_src = nullptr, int *note_dst = nullptr);
 cudaError_t launch_skip_masks(const uint8_t *skip, int nx, int ny, int nstrips, int nxb, uint32_t *MA, uint32_t *MB,
                               cudaStream_t st);
-// gradient stack: grad = cp_grad_frame^2( sum_s  RN32(lam_s * cube) )
+// gradient stack: grad = sum_s RN32(lam_s * cube) on the interior
 //   mode reference: per-shot float contribution RN32(RN64(lam*cube64)) added
-//   in float in shot order; mode fast: contributions added in double.
+//   in float in shot order; mode fast: lam summed exactly (shot_sum_fixed),
+//   times S^3 in double.
 //   accumulate: continue the sums already in grad / grad64 (chunked batches)
+//   frame: also the frame cells, as cp_grad_frame leaves them (a single
+//   chunk, nx, ny >= 5; else launch_cp_frame afterwards)
+//   l2_out: also *l2_out = 0.5 * sum of l2[0..nl2) (as launch_sum_l2)
 cudaError_t launch_stack(const float *L, size_t fstride, int nshots, const double *cube, const float *S, int nx,
                          int ny, int nxp, int mode, float *grad, int gpitch, double *grad64, bool accumulate,
-                         cudaStream_t st);
+                         cudaStream_t st, bool frame = false, const double *l2 = nullptr, int nl2 = 0,
+                         double *l2_out = nullptr);
 // exact-adjoint gradient dJ/dVp = -S^2 sum_s mu_s * dG/dS (G the Godunov
 // update at the converged traveltimes T_s); continues grad64 when accumulate
 cudaError_t launch_stack_exact(const float *T, const float *L, size_t fstride, int nshots, const int *src_h,
