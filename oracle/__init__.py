@@ -265,6 +265,14 @@ def ass_grad(p: Params, grad, S, lam):
     return g.reshape(p.ny, p.nx)
 
 
+def cp_grad_frame(p: Params, A):
+    """cp_grad_frame.c:18-49 on a copy of A [ny][nx]."""
+    lib = _load_port()
+    a = _f32(A).reshape(-1).copy()
+    lib.rzo_cp_grad_frame(C.byref(p.grid()), a)
+    return a.reshape(p.ny, p.nx)
+
+
 def shot_partition(nshots, np_, myid):
     lib = _load_port()
     a, b = C.c_int(0), C.c_int(0)
@@ -315,3 +323,8 @@ class Ref:
         g = _f32(grad).reshape(-1).copy()
         self.lib.ref_ass_grad(g, _f32(S).reshape(-1), _f32(lam).reshape(-1))
         return g.reshape(self.p.ny, self.p.nx)
+
+    def cp_grad_frame(self, A):
+        a = _f32(A).reshape(-1).copy()
+        self.lib.ref_cp_grad_frame(a)
+        return a.reshape(self.p.ny, self.p.nx)

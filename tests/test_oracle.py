@@ -135,6 +135,25 @@ def test_shot_partition_matches_init_mpishot(oracle_mod):
         assert max(sizes) - min(sizes) <= 1 and sizes == sorted(sizes, reverse=True)
 
 
+@pytest.mark.parametrize("nx,ny", [(5, 5), (5, 9), (6, 5), (7, 11), (20, 13), (64, 33)])
+def test_frame_copy_is_the_cell_two_inside(oracle_mod, nx, ny):
+    """cp_grad_frame.c:18-49 leaves in every cell the value of the cell
+    nearest to it two cells inside the grid (for nx, ny >= 5), and a second
+    application changes nothing: the rule by which the stack of a one-chunk
+    batch writes the frame cells itself."""
+    O = oracle_mod
+    p = O.Params(nx, ny, 10.0, 20.0)
+    rng = np.random.default_rng(nx * 100 + ny)
+    A = np.zeros((ny, nx), np.float32)
+    A[1:-1, 1:-1] = rng.standard_normal((ny - 2, nx - 2)).astype(np.float32)
+    framed = O.cp_grad_frame(p, A)
+    k, h = np.clip(np.arange(ny), 2, ny - 3), np.clip(np.arange(nx), 2, nx - 3)
+    assert np.array_equal(framed, A[np.ix_(k, h)])
+    assert np.array_equal(O.cp_grad_frame(p, framed), framed)
+    if O.ref_available():
+        assert np.array_equal(O.Ref(p).cp_grad_frame(A), framed)
+
+
 def _fd_case(O, seed, nx, ny, nshots, muted=False):
     w = synth.small_case(seed, nx, ny, nshots=nshots)
     p = O.Params(w.nx, w.ny, w.dh, w.time, 1e-14, w.eps_adj)
