@@ -38,6 +38,7 @@ ALG_BYTES_FWD = 12  # per forward point-update: slowness read, traveltime read +
 ALG_BYTES_ADJ = 16  # per adjoint point-update: traveltime, lambda read + write, receiver flag
 CHECK_BYTES_FWD = 8  # per cell of a forward fixpoint check: traveltime, slowness read
 CHECK_BYTES_ADJ = 9  # per interior cell of an adjoint fixpoint check: traveltime, lambda, receiver flag
+ALG_BYTES_EXACT_ADJ = 20  # per exact-adjoint point-update: mu read + write, x and z weight, receiver term
 
 
 def log(*a):
@@ -258,6 +259,11 @@ def run_gpu_arm(args, rank, world, local_rank):
     time.sleep(0.15)
     clocks.stop()
     launches1, shot_ms, shot_calls = ctx.kernel_stats()
+    # the device-pointer calls return before the device is done: read every
+    # shot's status bits now (a timeout or non-convergence voids the line)
+    bits = ctx.batch_status()
+    if bits:
+        raise SystemExit(f"device status bits 0x{bits:x} in the timed loop")
     if dist:
         from rajzel_gb300 import ranks
         ms = ranks.max_over_ranks(ms, dist, device=f"cuda:{local_rank}")
@@ -310,6 +316,14 @@ def run_gpu_arm(args, rank, world, local_rank):
     h2d = vp_host.nbytes + tobs_host.nbytes + 2 * 4 * w.nshots
     d2h = g_host.nbytes + 8 + 4 * w.nshots
 
+    # the other two arithmetic paths on the same batch, and every path's
+    # error against the FP64 GPU oracle (all outside the timed region above)
+    exact_line = time_mode(R, w, Tobs, stream, local_rank, "fast", "exact", args.steps, args.warmup, hbm_peak,
+                           peak_src)
+    refmode_line = time_mode(R, w, Tobs, stream, local_rank, "reference", "reference",
+                             max(3, args.steps // 4), args.warmup, hbm_peak, peak_src)
+    errors = fp64_errors(R, w, Tobs, local_rank)
+
     if rank != 0:
         return
     cores = os.cpu_count() or 1
@@ -343,11 +357,95 @@ def run_gpu_arm(args, rank, world, local_rank):
         "batched_over_plain": value / plain_value,
         "gpu_launches": int(launches1 - launches0),
         "autotune": tuned, "cuda_graphs": True,
+        "errors_vs_fp64": errors,
+        "exact_gradient": exact_line,
+        "reference_mode": refmode_line,
         "clocks": clk,
     }
     print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
+
+
+def time_mode(R, w, Tobs, stream, dev, mode, kind, steps, warmup, hbm_peak, peak_src):
+    """shots/s of the gradient step in another arithmetic mode or gradient
+    kind (device buffers, CUDA events on the launching stream) and the shot
+    kernel's byte-model roofline: fast mode with the exact discrete adjoint
+    (the gradient that meets the 1e-4 gate) or reference (bit-exact) mode."""
+    import numpy as np
+    import torch
+    ctx = R.Context(dev, mode)
+    ctx.set_stream(stream.cuda_stream)
+    ctx.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    ctx.set_receivers(w.recx, w.recz)
+    ctx.set_velocity(w.vp_start)
+    ctx.set_gradient(kind)
+    tobs_d = torch.from_numpy(np.ascontiguousarray(Tobs)).cuda()
+    grad_d = torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda")
+    l2_d = torch.empty(1, dtype=torch.float64, device="cuda")
+
+    def step():
+        ctx.grad_obj_device(w.srcx, w.srcz, tobs_d.data_ptr(), grad_d.data_ptr(), l2_d.data_ptr())
+
+    for _ in range(max(warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+    ctx.kernel_stats()
+    ms = _events_ms(step, stream, steps)
+    _, shot_ms, calls = ctx.kernel_stats()
+    bits = ctx.batch_status()
+    if bits:
+        raise SystemExit(f"{mode}/{kind}: device status bits 0x{bits:x}")
+    swept = np.array([ctx.shot_work(i) for i in range(w.nshots)])
+    passes = np.array([ctx.shot_info(i)[:2] for i in range(w.nshots)])
+    checks = (passes - swept).sum(axis=0)
+    adj_bytes = ALG_BYTES_EXACT_ADJ if kind == "exact" else ALG_BYTES_ADJ
+    pu_fwd = int(swept[:, 0].sum()) * 4 * w.nx * w.ny
+    pu_adj = int(swept[:, 1].sum()) * 4 * (w.nx * w.ny if kind == "exact" else (w.nx - 2) * (w.ny - 2))
+    alg = (pu_fwd * ALG_BYTES_FWD + pu_adj * adj_bytes + int(checks[0]) * CHECK_BYTES_FWD * w.nx * w.ny
+           + int(checks[1]) * CHECK_BYTES_ADJ * (w.nx - 2) * (w.ny - 2))
+    kernel_ms = shot_ms / max(calls, 1)
+    achieved = alg / (kernel_ms / 1e3) / 1e9
+    return {"mode": mode, "gradient": kind, "value": w.nshots / (ms / 1e3), "unit": "shots/s", "ms_per_step": ms,
+            "steps": steps, "passes_swept_fwd_adj": [int(swept[:, 0].sum()), int(swept[:, 1].sum())],
+            "point_updates_per_s": (pu_fwd + pu_adj) / (ms / 1e3),
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
+                         "frac": achieved / hbm_peak, "peak_source": peak_src, "kernel_ms": kernel_ms,
+                         "algorithmic_bytes_per_launch": alg}}
+
+
+def fp64_errors(R, w, Tobs, dev):
+    """Every path's error against the FP64 GPU oracle on the benchmark batch
+    (rz_set_error_check: the oracle runs the same 100 shots in double):
+    traveltimes (max-norm and relative L2, worst shot), picks, gradient
+    (rel. L2) and misfit.  Float32 traveltimes carry the rounding of every
+    update along paths of up to ~1800 cells, so on this workload even the
+    reference's own float arithmetic sits above 1e-5 (max-norm) from FP64; the
+    float paths are gated at the reference's own float error.  Gradient
+    gates: Leung-Qian no further from FP64 than twice the reference's own
+    float arithmetic plus 1e-4 (the receiver scaling of calc_FA_res.c
+    differences neighbouring float traveltimes); exact gradient 1e-4."""
+    out = {}
+    for label, mode, kind in (("fast", "fast", "reference"), ("reference", "reference", "reference"),
+                              ("exact", "fast", "exact")):
+        ctx = R.Context(dev, mode)
+        ctx.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+        ctx.set_receivers(w.recx, w.recz)
+        ctx.set_velocity(w.vp_start)
+        ctx.set_gradient(kind)
+        ctx.set_error_check(True)
+        ctx.grad_obj(w.srcx, w.srcz, Tobs)
+        out[label] = ctx.error_report()
+        ctx.close()
+    ref = out["reference"]
+    tt_gate = max(1e-5, ref["tt_rel"] * (1 + 1e-3) + 1e-7)
+    lq_gate = 2 * ref["grad_rel_l2"] + 1e-4
+    out["gates"] = {"tt_rel": tt_gate, "tt_rel_target": 1e-5, "fast_grad_rel_l2": lq_gate,
+                    "exact_grad_rel_l2": 1e-4}
+    out["pass"] = bool(out["fast"]["tt_rel"] <= tt_gate and out["exact"]["tt_rel"] <= tt_gate
+                       and out["fast"]["grad_rel_l2"] <= lq_gate and out["exact"]["grad_rel_l2"] <= 1e-4)
+    out["oracle"] = "FP64 GPU oracle (the reference's algorithm in double) on the same 100 shots"
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -50,6 +50,7 @@ extern "C" {
 /* arithmetic modes */
 #define RZ_MODE_REFERENCE 0  /* bit-identical to the reference's float/double arithmetic */
 #define RZ_MODE_FAST 1       /* FP32 sweeps, FP64 misfit and gradient stack */
+#define RZ_MODE_FP64 2       /* FP64 oracle: every sweep, residual and stack in double (validation, slow) */
 
 /* gradient kinds (rz_set_gradient) */
 #define RZ_GRADIENT_REFERENCE 0 /* Leung-Qian adjoint, lambda*S^3 + frame copy (ass_grad.c) */
@@ -227,9 +228,74 @@ int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, co
 int rz_misfit(rz_context *ctx, int nshots, const float *srcx, const float *srcz, const float *Tobs, double *L2,
               int flags);
 
+/* ----------------------------------------------------------------------
+ * FP64 oracle on the GPU (not in the reference, which computes in float
+ * with one double expression, sweep.c:94).  The same algorithm -- sweep.c,
+ * sweep_adj.c, norm1.c's stopping rule, calc_FA_res.c, ass_grad.c,
+ * cp_grad_frame.c -- carried out entirely in double, one CTA per shot; the
+ * exact gradient kind solves the exact discrete adjoint in double.  It is the
+ * yardstick of every float result:
+ *   - RZ_MODE_FP64 (rz_set_mode) runs rz_forward, rz_grad_obj, rz_misfit and
+ *     rz_backward in FP64 and rounds their results to float;
+ *   - rz_forward_f64 / rz_grad_obj_f64 return the double results;
+ *   - rz_set_error_check makes every later rz_forward / rz_grad_obj /
+ *     rz_misfit of a float mode also run the FP64 oracle on the same inputs
+ *     and record the error of its result (rz_error_report).
+ * ---------------------------------------------------------------------- */
+typedef struct {
+    int shots;           /* shots whose traveltime fields were compared (those
+                            kept in the field slots: all, unless the batch ran
+                            in chunks under the memory cap) */
+    double tt_rel;       /* worst shot's max|TT - TT64| / max|TT64| */
+    double tt_rel_l2;    /* worst shot's ||TT - TT64||_2 / ||TT64||_2 */
+    double tmod_rel;     /* max|Tmod - Tmod64| / max|Tmod64| over all picks */
+    double grad_rel_l2;  /* ||grad - grad64||_2 / ||grad64||_2 (gradient calls) */
+    double grad_rel_max; /* max|grad - grad64| / max|grad64| (gradient calls) */
+    double misfit_rel;   /* |L2 - L2_64| / |L2_64| (gradient and misfit calls) */
+} rz_error;
+
+/* Traveltimes TT [nshots][ny][nx] and picks Tmod [nshots][ntr] (either may
+   be NULL) of the FP64 oracle. */
+int rz_forward_f64(rz_context *ctx, int nshots, const float *srcx, const float *srcz, double *TT, double *Tmod,
+                   int flags);
+/* Gradient [ny][nx] and misfit of the FP64 oracle, of the context's
+   gradient kind (Leung-Qian with frame copy, or exact dJ/dVp). */
+int rz_grad_obj_f64(rz_context *ctx, int nshots, const float *srcx, const float *srcz, const float *Tobs,
+                    double *grad, double *L2, int flags);
+/* 1: later float calls also run the FP64 oracle on their inputs (the call
+   then synchronises and takes the oracle's time too); 0: off (default). */
+int rz_set_error_check(rz_context *ctx, int enable);
+/* The error of the last checked call's results against the FP64 oracle. */
+int rz_error_report(rz_context *ctx, rz_error *err);
+
+/* Test hook for the failure path (no counterpart in the reference, which
+   aborts through err()/MPI_Abort, util.c:7-17).  Every device wait for
+   another warp is bounded: after spin_limit polls (0 = the default budget of
+   2^21 polls) it records a status bit, raises the CTA's abort word so
+   every later wait of the CTA returns at once, and the kernel ends normally;
+   waits for the CTA's own tensor copies always let the copies land.  With
+   withhold_handoff != 0 the first warp of every CTA withholds one hand-off
+   signal in its first sweep, so the next warp's wait runs out: the call then
+   returns RZ_ETIMEOUT (status bit 1) and the context stays usable.  0, 0
+   restores normal operation. */
+int rz_set_wait_test(rz_context *ctx, unsigned spin_limit, int withhold_handoff);
+
 /* Per-shot results of the last rz_forward/rz_grad_obj (host pointers, any
    may be NULL): outer passes of forward/adjoint, device status bits. */
 int rz_shot_info(rz_context *ctx, int shot, int *fwd_passes, int *adj_passes, int *status);
+
+/* Device status bits, as rz_shot_info, rz_batch_status and
+   rz_eikonal_noalloc's info[1] report them: bit 0 a bounded wait for a tensor
+   copy gave up, bit 1 a bounded wait for another warp gave up (both
+   RZ_ETIMEOUT), bit 2 / bit 3 the forward / adjoint did not meet TTNORM
+   within max_passes (RZ_ENOCONV), bit 4 a source outside the grid, bit 5 an
+   invalid slowness (RZ_EINVAL).  rz_status_code maps them to the RZ_* code a
+   synchronous call would return. */
+int rz_status_code(int bits);
+/* OR of the status bits of every shot of the last batch: the check for
+   calls made with RZ_DEVICE_PTRS, which return before the device is done
+   (this call waits for the context stream). */
+int rz_batch_status(rz_context *ctx, int *bits);
 
 /* Passes of shot `shot` in the last batch that were actually swept.  A pass
    that a parallel fixpoint check proves to change no cell is counted in
@@ -262,17 +328,20 @@ int rz_eikonal_adj(rz_context *ctx, const float *TT, const float *Tres, float *l
 
 /* Allocation-free forward solve (no counterpart in the reference: RAJZEL
    always runs on the host and allocates its own scratch with matrix()).
-   For callers that cannot allocate GPU memory -- inside a CUDA-graph capture
-   or a fixed memory pool, or on a host with no allocator available -- this
-   computes one shot's traveltimes exactly like rz_eikonal() in reference
-   mode, with its working space in a static 32 MiB device array that every
-   GPU loading this library holds until exit.  S (slowness [ny][nx]), TT
-   (output [ny][nx]) and info (2 ints: outer passes, status bits) are device
-   pointers; the call is asynchronous on `stream` (NULL = legacy default).
-   Grids needing more than the static space return RZ_EUNSUPPORTED.  The
-   first call on a device sets up (looks up the array's address) and should
-   come before any stream capture; calls that overlap on the GPU share the
-   array and race. */
+   For callers that cannot allocate GPU memory -- a solver step working
+   inside a fixed memory pool or a memory budget fixed up front, or a host
+   with no allocator available -- this computes one shot's traveltimes
+   exactly like rz_eikonal() in reference mode, with its working space in a
+   static 32 MiB device array that every GPU loading this library holds until
+   exit.  S (slowness [ny][nx]), TT (output [ny][nx]) and info (2 ints: outer
+   passes, status bits as rz_status_code reads them) are device pointers; the
+   call is asynchronous on `stream` (NULL = legacy default).  The slowness is
+   checked on the device as rz_set_slowness checks it: a zero, negative or
+   non-finite value sets bit 5 of info[1] (RZ_EINVAL), no solve runs and TT
+   is undefined.  Grids needing more than the static space return
+   RZ_EUNSUPPORTED.  The first call on a device sets up (looks up the array's
+   address) and should come before any stream capture; calls that overlap on
+   the GPU share the array and race. */
 int rz_eikonal_noalloc(const rz_grid *grid, const float *S, float srcx, float srcz, float *TT, int *info,
                        void *stream);
 

@@ -112,6 +112,15 @@ def _load_ref():
         lib.ref_cp_grad_frame.restype = None
         lib.ref_counter.argtypes = [C.c_int]
         lib.ref_counter.restype = C.c_long
+        lib.ref_precond.argtypes = [_f32p, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_float]
+        lib.ref_precond.restype = None
+        lib.ref_fatt_stage.argtypes = [_f32p, C.c_int, _f32p, _f32p, C.c_int, _i32p, _i32p, _f32p, C.c_int,
+                                       C.c_int, C.c_int, C.c_float, C.c_float, C.c_float, C.c_float, C.c_float,
+                                       C.c_float, C.c_float, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                       C.c_float, _f64p, _f32p]
+        lib.ref_fatt_stage.restype = C.c_int
+        lib.ref_evals.argtypes = [_f64p, C.c_int]
+        lib.ref_evals.restype = C.c_int
         _ref = lib
     return _ref
 
@@ -328,3 +337,30 @@ class Ref:
         a = _f32(A).reshape(-1).copy()
         self.lib.ref_cp_grad_frame(a)
         return a.reshape(self.p.ny, self.p.nx)
+
+    def precond(self, grad, o):
+        """precond() of the reference (precond.c:12-58): SPATFILTER 4 and the
+        horizontal taper as the options (an rz_fatt_opts-like dict) select."""
+        g = _f32(grad).reshape(-1).copy()
+        self.lib.ref_precond(g, int(o["spatfilter"]), int(o["filt_size_grad"]), int(o["filt_size_grad1"]),
+                             int(o["taper_hor"]), int(o["gradt1"]), int(o["gradt2"]), float(o["exp_taper_grad_hor"]))
+        return g.reshape(self.p.ny, self.p.nx)
+
+    def fatt(self, vp0, srcx, srcz, recx, recz, Tobs, o):
+        """One FATT stage by the reference's own fatt() (l-BFGS + weak Wolfe).
+        Returns (vp, misfit per iteration, accepted step per iteration, the
+        misfit of every gradient evaluation in call order)."""
+        recx, recz = _i32(recx), _i32(recz)
+        vp = _f32(vp0).reshape(-1).copy()
+        n_it = int(o["itermax"])
+        mis = np.zeros(n_it, np.float64)
+        steps = np.zeros(n_it, np.float32)
+        it = self.lib.ref_fatt_stage(vp, len(srcx), _f32(srcx), _f32(srcz), len(recx), recx, recz,
+                                     _f32(Tobs).reshape(-1), n_it, int(o["nlbfgs"]), int(o["stepmax"]),
+                                     float(o["eps_scale"]), float(o["c1"]), float(o["c2"]), float(o["scalefac"]),
+                                     float(o["vp_lo"]), float(o["vp_hi"]), float(o["pro"]), int(o["spatfilter"]),
+                                     int(o["filt_size_grad"]), int(o["filt_size_grad1"]), int(o["taper_hor"]),
+                                     int(o["gradt1"]), int(o["gradt2"]), float(o["exp_taper_grad_hor"]), mis, steps)
+        ev = np.zeros(4096, np.float64)
+        n = self.lib.ref_evals(ev, len(ev))
+        return vp.reshape(self.p.ny, self.p.nx), mis[:it], steps[:it], ev[: min(n, len(ev))]

@@ -12,7 +12,9 @@
  * fastest, cell (h,k) at k*NX+h, 0-based) to and from the reference's
  * 1-based NR matrices and call the reference entry points.  Sweep and
  * norm1 calls are counted through the linker's --wrap so tests can compare
- * pass counts.  This library is the oracle's pin, never the product.
+ * pass counts, and the misfits grad_obj() returns are recorded in call order
+ * (a FATT stage's trajectory).  This library is the oracle's pin, never the
+ * product.
  */
 #include "fd.h"
 #include "globvar.h"
@@ -28,6 +30,24 @@ float __real_norm1(float **TT, float **TTold);
 
 static long g_sweeps = 0, g_sweeps_adj = 0, g_norm1 = 0;
 static float g_last_norm1 = 0.0f;
+
+/* every misfit grad_obj() returns, in call order (FATT trajectories) */
+double __real_grad_obj(float **grad, float **S, float **TT, float **lam, float *Tmod, float *Tobs, float *Tres,
+                       float **srcpos, int nshots, int **recpos, int ntr, int iter);
+#define REF_MAX_EVALS 4096
+static double g_evals[REF_MAX_EVALS];
+static int g_nevals = 0;
+double __wrap_grad_obj(float **grad, float **S, float **TT, float **lam, float *Tmod, float *Tobs, float *Tres,
+                       float **srcpos, int nshots, int **recpos, int ntr, int iter) {
+    double L2 = __real_grad_obj(grad, S, TT, lam, Tmod, Tobs, Tres, srcpos, nshots, recpos, ntr, iter);
+    if (g_nevals < REF_MAX_EVALS) g_evals[g_nevals] = L2;
+    g_nevals++;
+    return L2;
+}
+int ref_evals(double *out, int cap) {
+    for (int i = 0; i < g_nevals && i < cap; i++) out[i] = g_evals[i];
+    return g_nevals;
+}
 
 void __wrap_sweep(float **S, float **TT, int nxsrc, int nysrc, int nx1, int nx2, int ndx, int ny1, int ny2, int ndy) {
     g_sweeps++;
@@ -230,4 +250,112 @@ void ref_cp_grad_frame(float *A_flat) {
     cp_grad_frame(A);
     nr_to_flat(A, A_flat);
     free_matrix(A, 1, NY, 1, NX);
+}
+
+/* --- preconditioning and the FATT stage ------------------------------------ */
+/* The reference writes files into the working directory (taper_grad.c's
+   taper_coeff_hor.bin, fatt.c's logs and model files, LBFGS.c's history):
+   these calls run inside a fresh temporary directory. */
+static char g_cwd[4096];
+static char g_tmpdir[64];
+static void enter_tmpdir(void) {
+    if (!getcwd(g_cwd, sizeof g_cwd)) err("oracle driver: getcwd failed");
+    char tmpl[] = "/tmp/rzfattXXXXXX";
+    char *d = mkdtemp(tmpl);
+    if (!d) err("oracle driver: mkdtemp failed");
+    strncpy(g_tmpdir, d, sizeof g_tmpdir - 1);
+    if (chdir(g_tmpdir)) err("oracle driver: chdir failed");
+}
+static void leave_tmpdir(void) {
+    if (chdir(g_cwd)) err("oracle driver: chdir back failed");
+}
+
+static void set_precond_globals(int spatfilter, int fs, int fs1, int taper_hor, int gradt1, int gradt2,
+                                float exp_hor) {
+    SPATFILTER = spatfilter;
+    FILT_SIZE_GRAD = fs;
+    FILT_SIZE_GRAD1 = fs1;
+    SWS_TAPER_GRAD_HOR = taper_hor;
+    SWS_TAPER_GRAD_VERT = 0;
+    SWS_TAPER_GRAD_SOURCES = 0;
+    SWS_TAPER_FILE = 0;
+    GRADT1 = gradt1;
+    GRADT2 = gradt2;
+    EXP_TAPER_GRAD_HOR = exp_hor;
+}
+
+/* precond() (precond.c:12-58) on a flat gradient: SPATFILTER 4 (gauss_filt.c)
+   and / or the horizontal taper (taper_grad.c, sws 2). */
+void ref_precond(float *grad_flat, int spatfilter, int fs, int fs1, int taper_hor, int gradt1, int gradt2,
+                 float exp_hor) {
+    float **grad = matrix(1, NY, 1, NX);
+    flat_to_nr(grad_flat, grad);
+    set_precond_globals(spatfilter, fs, fs1, taper_hor, gradt1, gradt2, exp_hor);
+    enter_tmpdir();
+    precond(grad, 0, NULL, NULL, 0, 1);
+    leave_tmpdir();
+    set_precond_globals(0, 0, 0, 0, 0, 0, 0.0f);
+    nr_to_flat(grad, grad_flat);
+    free_matrix(grad, 1, NY, 1, NX);
+}
+
+/* One FATT workflow stage by the reference's own fatt() (fatt.c:10-258):
+   l-BFGS (GRAD_METHOD 2, LBFGS.c) with the weak-Wolfe line search
+   (LINESEARCH 1, wolfels.c), the workflow file holding one stage.  vp_flat:
+   start model in, final model out.  misfit_out / step_out [itermax]: the
+   columns of fatt.c's misfit log (L2 and the accepted step per iteration).
+   Returns the number of iterations logged. */
+int ref_fatt_stage(float *vp_flat, int nshots, const float *srcx, const float *srcz, int ntr, const int *recx,
+                   const int *recz, const float *Tobs_all, int itermax, int nlbfgs, int stepmax, float eps_scale,
+                   float c1, float c2, float scalefac, float vp_lo, float vp_hi, float pro, int spatfilter, int fs,
+                   int fs1, int taper_hor, int gradt1, int gradt2, float exp_hor, double *misfit_out,
+                   float *step_out) {
+    float **Vp = matrix(1, NY, 1, NX), **S = matrix(1, NY, 1, NX), **TT = matrix(1, NY, 1, NX);
+    float *Tmod = vector(1, ntr), *Tobs = vector(1, ntr), *Tres = vector(1, ntr);
+    float **srcpos = matrix(1, 8, 1, nshots);
+    int **recpos = make_recpos(ntr, recx, recz);
+    flat_to_nr(vp_flat, Vp);
+    for (int s = 1; s <= nshots; s++) { srcpos[1][s] = srcx[s - 1]; srcpos[2][s] = srcz[s - 1]; }
+    ensure_pickdir();
+    for (int s = 1; s <= nshots; s++) write_pick_file(s, ntr, Tobs_all + (size_t)(s - 1) * ntr);
+    NSHOT1 = 1;
+    NSHOT2 = nshots + 1;
+    set_precond_globals(spatfilter, fs, fs1, taper_hor, gradt1, gradt2, exp_hor);
+    GRAD_METHOD = 2; NLBFGS = nlbfgs; ITERMAX = itermax; LINESEARCH = 1; STEPMAX = stepmax;
+    EPS_SCALE = eps_scale; C1 = c1; C2 = c2; SCALEFAC = scalefac; VPLOWERLIM = vp_lo; VPUPPERLIM = vp_hi;
+    INVMAT = 1;
+    enter_tmpdir();
+    snprintf(MISFIT_LOG_FILE, STRING_SIZE, "misfit.log");
+    snprintf(JACOBIAN, STRING_SIZE, "jac");
+    snprintf(INV_MODELFILE, STRING_SIZE, "inv");
+    FILE *fp = fopen("workflow.inp", "w");
+    if (!fp) err("oracle driver: cannot write workflow file");
+    fprintf(fp, "PRO SPATFILTER WD_DAMP WD_DAMP1 FILT_SIZE_GRAD FILT_SIZE_GRAD1\n");
+    fprintf(fp, "%.9e %d 1e-3 1e-3 %d %d\n", pro, spatfilter, fs, fs1);
+    fclose(fp);
+    calc_S(Vp, S);
+    g_nevals = 0;
+    char wf[] = "workflow.inp";
+    fatt(Vp, S, TT, Tmod, Tobs, Tres, srcpos, nshots, recpos, ntr, wf);
+    int n = 0;
+    fp = fopen("misfit.log", "r");
+    if (fp) {
+        float step;
+        double l2;
+        int stage;
+        while (n < itermax && fscanf(fp, "%e %le %d", &step, &l2, &stage) == 3) {
+            step_out[n] = step;
+            misfit_out[n] = l2;
+            n++;
+        }
+        fclose(fp);
+    }
+    leave_tmpdir();
+    set_precond_globals(0, 0, 0, 0, 0, 0, 0.0f);
+    nr_to_flat(Vp, vp_flat);
+    free_matrix(Vp, 1, NY, 1, NX); free_matrix(S, 1, NY, 1, NX); free_matrix(TT, 1, NY, 1, NX);
+    free_vector(Tmod, 1, ntr); free_vector(Tobs, 1, ntr); free_vector(Tres, 1, ntr);
+    free_matrix(srcpos, 1, 8, 1, nshots);
+    free_imatrix(recpos, 1, 3, 1, ntr);
+    return n;
 }

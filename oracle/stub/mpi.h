@@ -1,7 +1,8 @@
 /*
- * Single-rank MPI stand-in used ONLY to compile the reference's hot-path C
- * sources into the test oracle library (oracle/_ref/libref.so).  It is test
- * infrastructure: nothing in the rajzel_gb300 product includes it.
+ * Single-rank MPI stand-in, used ONLY by test infrastructure: to compile the
+ * reference's hot-path C sources into the test oracle library
+ * (oracle/_ref/libref.so) and the shim's MPI branch into the compat test
+ * harness (tests/compat).  Nothing in the rajzel_gb300 product includes it.
  *
  * With one rank every collective the reference uses on this path is the
  * identity: MPI_Allreduce copies send->recv (grad_obj.c:60,

@@ -29,7 +29,7 @@ _HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(_HERE, "librajzel_gb300.so")
 
 RZ_OK, RZ_EINVAL, RZ_ENOCONV, RZ_ECUDA, RZ_ENOMEM, RZ_ETIMEOUT, RZ_ESTATE, RZ_EUNSUPPORTED = range(8)
-RZ_MODE_REFERENCE, RZ_MODE_FAST = 0, 1
+RZ_MODE_REFERENCE, RZ_MODE_FAST, RZ_MODE_FP64 = 0, 1, 2
 RZ_DEVICE_PTRS = 1
 RZ_GRADIENT_REFERENCE, RZ_GRADIENT_EXACT = 0, 1
 
@@ -42,6 +42,16 @@ class RajzelError(RuntimeError):
 class _Grid(C.Structure):
     _fields_ = [("nx", C.c_int), ("ny", C.c_int), ("dh", C.c_float), ("time", C.c_float),
                 ("ttnorm", C.c_float), ("eps_adj", C.c_float), ("max_passes", C.c_int)]
+
+
+class ErrorReport(C.Structure):
+    """rz_error: a float result's error against the FP64 oracle on the same inputs."""
+    _fields_ = [("shots", C.c_int), ("tt_rel", C.c_double), ("tt_rel_l2", C.c_double), ("tmod_rel", C.c_double),
+                ("grad_rel_l2", C.c_double),
+                ("grad_rel_max", C.c_double), ("misfit_rel", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 _lib = None
@@ -89,7 +99,17 @@ def load_library(path: str = LIB_PATH):
     lib.rz_precond.argtypes = [vp, vp, vp, C.c_int]
     lib.rz_set_gradient.argtypes = [vp, C.c_int]
     lib.rz_backward.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
-    for name in ("rz_set_memory_cap", "rz_shot_work", "rz_set_graphs", "rz_autotune", "rz_grad_obj_multi", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_misfit", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
+    lib.rz_status_code.argtypes = [C.c_int]
+    lib.rz_status_code.restype = C.c_int
+    lib.rz_batch_status.argtypes = [vp, vp]
+    lib.rz_batch_status.restype = C.c_int
+    lib.rz_set_wait_test.argtypes = [vp, C.c_uint, C.c_int]
+    lib.rz_set_wait_test.restype = C.c_int
+    lib.rz_forward_f64.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
+    lib.rz_grad_obj_f64.argtypes = [vp, C.c_int, vp, vp, vp, vp, vp, C.c_int]
+    lib.rz_set_error_check.argtypes = [vp, C.c_int]
+    lib.rz_error_report.argtypes = [vp, vp]
+    for name in ("rz_forward_f64", "rz_grad_obj_f64", "rz_set_error_check", "rz_error_report", "rz_set_memory_cap", "rz_shot_work", "rz_set_graphs", "rz_autotune", "rz_grad_obj_multi", "rz_fatt_defaults", "rz_fatt", "rz_precond", "rz_misfit", "rz_set_gradient", "rz_backward", "rz_create", "rz_set_stream", "rz_set_mode", "rz_set_grid", "rz_set_slowness", "rz_set_velocity",
                  "rz_set_receivers", "rz_forward", "rz_grad_obj", "rz_shot_info", "rz_shot_fields", "rz_eikonal",
                  "rz_eikonal_adj", "rz_shot_timeline", "rz_kernel_stats"):
         getattr(lib, name).restype = C.c_int
@@ -193,7 +213,7 @@ class Context:
         self._check(self.lib.rz_set_stream(self.h, C.c_void_p(stream_handle or 0)), "rz_set_stream")
 
     def set_mode(self, mode):
-        m = {"reference": RZ_MODE_REFERENCE, "fast": RZ_MODE_FAST}.get(mode, mode)
+        m = {"reference": RZ_MODE_REFERENCE, "fast": RZ_MODE_FAST, "fp64": RZ_MODE_FP64}.get(mode, mode)
         self._check(self.lib.rz_set_mode(self.h, int(m)), "rz_set_mode")
         self.mode = m
 
@@ -341,6 +361,49 @@ class Context:
         self._check(self.lib.rz_grad_obj(self.h, len(srcx), _ptr(srcx), _ptr(srcz), C.c_void_p(tobs_ptr),
                                          C.c_void_p(grad_ptr), C.c_void_p(l2_ptr), RZ_DEVICE_PTRS),
                     "rz_grad_obj(device)")
+
+    # -- the FP64 oracle and the error of float results ----------------------
+    def forward_f64(self, srcx, srcz, want_tt=True):
+        """FP64 oracle traveltimes [n][ny][nx] (or None) and picks [n][ntr], float64."""
+        srcx, srcz = _f32(srcx), _f32(srcz)
+        n = len(srcx)
+        TT = np.empty((n, self.ny, self.nx), np.float64) if want_tt else None
+        Tmod = np.empty((n, max(self.ntr, 1)), np.float64)
+        self._check(self.lib.rz_forward_f64(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(TT), _ptr(Tmod), 0),
+                    "rz_forward_f64")
+        return TT, Tmod[:, : self.ntr]
+
+    def grad_obj_f64(self, srcx, srcz, Tobs):
+        """FP64 oracle gradient [ny][nx] (float64) and misfit of the context's gradient kind."""
+        srcx, srcz = _f32(srcx), _f32(srcz)
+        n = len(srcx)
+        Tobs = _f32(Tobs).reshape(n, self.ntr)
+        grad = np.empty((self.ny, self.nx), np.float64)
+        L2 = C.c_double(0.0)
+        self._check(self.lib.rz_grad_obj_f64(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(Tobs), _ptr(grad),
+                                             C.byref(L2), 0), "rz_grad_obj_f64")
+        return grad, L2.value
+
+    def set_error_check(self, enable: bool):
+        """Later float calls also run the FP64 oracle and record their error (error_report)."""
+        self._check(self.lib.rz_set_error_check(self.h, int(bool(enable))), "rz_set_error_check")
+
+    def error_report(self):
+        """Error of the last checked call against the FP64 oracle, as a dict (rz_error)."""
+        e = ErrorReport()
+        self._check(self.lib.rz_error_report(self.h, C.byref(e)), "rz_error_report")
+        return e.as_dict()
+
+    def set_wait_test(self, spin_limit: int = 0, withhold_handoff: bool = False):
+        """Test hook of the timeout path (rz_set_wait_test)."""
+        self._check(self.lib.rz_set_wait_test(self.h, int(spin_limit), int(bool(withhold_handoff))),
+                    "rz_set_wait_test")
+
+    def batch_status(self):
+        """OR of the device status bits of every shot of the last batch (waits for the stream)."""
+        b = C.c_int(0)
+        self._check(self.lib.rz_batch_status(self.h, C.byref(b)), "rz_batch_status")
+        return b.value
 
     def shot_info(self, shot):
         a, b, s = C.c_int(0), C.c_int(0), C.c_int(0)

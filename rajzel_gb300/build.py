@@ -28,7 +28,7 @@ C_SOURCES = ["rz_io.c"]  # host C compiled into the library
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVFLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-Wall"]
-CU_SOURCES = ["rz_shot.cu", "rz_aux.cu", "rz_api.cu", "rz_noalloc.cu", "rz_fatt.cu"]
+CU_SOURCES = ["rz_shot.cu", "rz_aux.cu", "rz_api.cu", "rz_noalloc.cu", "rz_fatt.cu", "rz_fp64.cu"]
 HEADERS = ["rz_device.cuh", "rz_internal.h"]
 
 

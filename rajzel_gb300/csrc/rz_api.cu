@@ -17,6 +17,7 @@
 #include <cstring>
 #include <array>
 #include <map>
+#include <mutex>
 #include <string>
 #include <thread>
 #include <vector>
@@ -124,6 +125,27 @@ struct rz_context {
     // accounting: kernels launched, and CUDA-event timing of every shot-kernel launch
     long long launches = 0;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> shot_events;
+
+    // FP64 oracle (rz_fp64.cu): double field slots, sized for the largest
+    // chunk seen, and per-shot scalars for the whole batch
+    int cap64 = 0;
+    bool cap64_exact = false;
+    double *d64T = nullptr, *d64A = nullptr, *d64L = nullptr, *d64WX = nullptr, *d64WZ = nullptr, *d64GS = nullptr;
+    int cap64s = 0;
+    double *d64Tmod = nullptr, *d64Tres = nullptr, *d64l2 = nullptr;
+    int *d64Pf = nullptr, *d64Pa = nullptr, *d64Stat = nullptr;
+    double *d64Grad = nullptr, *d64L2 = nullptr;
+    double *dCmp = nullptr;  // comparison accumulators (4 doubles per entry)
+    int ncmp = 0;
+    const float *last_grad = nullptr;  // device gradient of the last rz_grad_obj
+    // bounded waits: polls before a wait for another warp gives up (0 =
+    // default) and the withheld hand-off of the timeout test (rz_set_wait_test)
+    unsigned spin = 0;
+    int withhold = 0;
+    // errors of float results against the FP64 oracle (rz_set_error_check)
+    bool err_check = false;
+    bool err_valid = false;
+    rz_error err_rep{};
 };
 
 // ---------------------------------------------------------------------------
@@ -173,16 +195,20 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// the driver's tensor-map encoder, looked up once for all host threads
 static EncodeTiledFn encode_fn() {
+    static std::once_flag once;
     static EncodeTiledFn fn = nullptr;
-    if (!fn) {
+    std::call_once(once, [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
         if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
                 cudaSuccess &&
             q == cudaDriverEntryPointSuccess)
             fn = (EncodeTiledFn)p;
-    }
+        else
+            (void)cudaGetLastError();
+    });
     return fn;
 }
 
@@ -215,9 +241,20 @@ static void free_shots(rz_context *c) {
     c->cap_s = 0;
 }
 
+static void free_fp64(rz_context *c) {
+    dfree(c->d64T), dfree(c->d64A), dfree(c->d64L), dfree(c->d64WX), dfree(c->d64WZ), dfree(c->d64GS);
+    c->cap64 = 0;
+    c->cap64_exact = false;
+    dfree(c->d64Tmod), dfree(c->d64Tres), dfree(c->d64l2), dfree(c->d64Pf), dfree(c->d64Pa), dfree(c->d64Stat);
+    c->cap64s = 0;
+    dfree(c->d64Grad), dfree(c->d64L2), dfree(c->dCmp);
+    c->ncmp = 0;
+}
+
 static void free_batch(rz_context *c) {
     free_fields(c);
     free_shots(c);
+    free_fp64(c);
 }
 
 // device bytes of one field slot: T, pass snapshot, lambda, two skewed T copies, border rows,
@@ -417,6 +454,8 @@ static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     P.swept = c->dSwept + (size_t)first * 2;
     P.chg = c->dChg;
     P.chg_stride = (size_t)c->nstrips * 4 * (c->nxb + 1);
+    P.spin = c->spin;
+    P.withhold = c->withhold;
 }
 
 static int status_to_code(int bits) {
@@ -547,6 +586,210 @@ static int stack_chunk(rz_context *c, int first, int m, float *gdst, bool whole 
     return RZ_OK;
 }
 
+// ---------------------------------------------------------------------------
+// FP64 oracle: the whole computation in double (rz_fp64.cu), for RZ_MODE_FP64,
+// rz_forward_f64 / rz_grad_obj_f64 and the error of float results
+// ---------------------------------------------------------------------------
+// Per-shot scalars for n shots and field slots for a chunk of them: all n
+// when they fit the memory cap (default 90% of free memory), else fewer.
+static int ensure_fp64(rz_context *c, int n, bool exact, int *chunk) {
+    const size_t fs = (size_t)c->g.nx * c->g.ny;
+    if (n > c->cap64s) {
+        dfree(c->d64Tmod), dfree(c->d64Tres), dfree(c->d64l2), dfree(c->d64Pf), dfree(c->d64Pa), dfree(c->d64Stat);
+        c->cap64s = 0;
+        const size_t nt = (size_t)(c->ntr > 0 ? c->ntr : 1) * n;
+        CK(dalloc(&c->d64Tmod, nt));
+        CK(dalloc(&c->d64Tres, nt));
+        CK(dalloc(&c->d64l2, (size_t)n));
+        CK(dalloc(&c->d64Pf, (size_t)n));
+        CK(dalloc(&c->d64Pa, (size_t)n));
+        CK(dalloc(&c->d64Stat, (size_t)n));
+        c->cap64s = n;
+    }
+    if (!c->d64Grad) CK(dalloc(&c->d64Grad, fs));
+    if (!c->d64L2) CK(dalloc(&c->d64L2, 1));
+    const size_t per = (exact ? 6 : 3) * fs * sizeof(double);
+    const size_t held = (size_t)c->cap64 * (c->cap64_exact ? 6 : 3) * fs * sizeof(double);
+    size_t limit = c->memcap;
+    if (limit == 0) {
+        size_t fr = 0, tot = 0;
+        CK(cudaMemGetInfo(&fr, &tot));
+        limit = (size_t)(0.9 * (double)(fr + held));
+    }
+    const int fit = (int)std::max<size_t>(1, std::min<size_t>(limit / per, (size_t)n));
+    if (c->cap64 < std::min(n, fit) || (exact && !c->cap64_exact) || (size_t)c->cap64 * per > limit) {
+        dfree(c->d64T), dfree(c->d64A), dfree(c->d64L), dfree(c->d64WX), dfree(c->d64WZ), dfree(c->d64GS);
+        c->cap64 = 0;
+        const int m = std::min(n, fit);
+        CK(dalloc(&c->d64T, fs * m));
+        CK(dalloc(&c->d64A, fs * m));
+        CK(dalloc(&c->d64L, fs * m));
+        if (exact) {
+            CK(dalloc(&c->d64WX, fs * m));
+            CK(dalloc(&c->d64WZ, fs * m));
+            CK(dalloc(&c->d64GS, fs * m));
+        }
+        c->cap64 = m;
+        c->cap64_exact = exact;
+    }
+    *chunk = std::min(n, c->cap64);
+    return RZ_OK;
+}
+
+static void fill_fp64(const rz_context *c, F64Params &P, int first, int m) {
+    memset(&P, 0, sizeof P);
+    P.nx = c->g.nx, P.ny = c->g.ny, P.nxp = c->nxp;
+    P.dh = c->g.dh, P.time = c->g.time, P.ttnorm = c->g.ttnorm, P.eps_adj = c->g.eps_adj;
+    P.max_passes = c->g.max_passes > 0 ? c->g.max_passes : 10000;
+    P.nshots = m;
+    P.S = c->dS;
+    P.skip = c->dSkipP;
+    P.src_h = c->dSrcH + first, P.src_k = c->dSrcK + first;
+    P.ntr = c->ntr;
+    P.rec_h = c->dRecH, P.rec_k = c->dRecK;
+    P.nrcell = c->nrcell, P.rcell_h = c->dRcH, P.rcell_k = c->dRcK, P.rcell_rec = c->dRcRec;
+    P.nxcell = c->nxcell, P.xcell_h = c->dXcH, P.xcell_k = c->dXcK, P.xcell_off = c->dXcOff, P.xcell_rec = c->dXcRec;
+    P.Tobs = c->dTobs + (size_t)first * c->ntr;
+    P.T = c->d64T, P.A = c->d64A, P.L = c->d64L, P.WX = c->d64WX, P.WZ = c->d64WZ, P.GS = c->d64GS;
+    P.Tmod = c->d64Tmod + (size_t)first * c->ntr;
+    P.Tres = c->d64Tres + (size_t)first * c->ntr;
+    P.l2 = c->d64l2 + first;
+    P.passes_fwd = c->d64Pf + first, P.passes_adj = c->d64Pa + first, P.status = c->d64Stat + first;
+    P.fstride = (size_t)c->g.nx * c->g.ny;
+}
+
+// The FP64 computation over the n shots whose sources (and picks, for
+// residual) are already on the device.  After each chunk's launch,
+// on_chunk(first, m) sees the double traveltimes of shots first..first+m-1
+// in the slots.  adjoint: gradient into d64Grad, misfit into d64L2 (also for
+// residual alone).  Returns the status of the shots.
+template <class F>
+static int run_fp64(rz_context *c, int n, bool adjoint, bool residual, bool exact, bool cotangent, F &&on_chunk) {
+    int chunk = 0, r;
+    if ((r = ensure_fp64(c, n, adjoint && exact, &chunk))) return r;
+    if (!c->rec_set && (r = rz_set_receivers(c, 0, nullptr, nullptr))) return r;
+    CK(cudaMemsetAsync(c->d64Stat, 0, n * sizeof(int), c->st));
+    for (int first = 0; first < n; first += chunk) {
+        const int m = std::min(chunk, n - first);
+        F64Params P;
+        fill_fp64(c, P, first, m);
+        P.do_residual = residual ? 1 : 0;
+        P.do_adjoint = adjoint ? 1 : 0;
+        P.exact = exact ? 1 : 0;
+        P.cotangent = cotangent ? 1 : 0;
+        CK(launch_fp64_shots(P, c->st));
+        c->launches += 1;
+        if ((r = on_chunk(first, m))) return r;
+        if (adjoint) {
+            CK(launch_fp64_stack(P, c->d64Grad, first > 0, c->st));
+            c->launches += 1;
+        }
+    }
+    const long ncell = (long)c->g.nx * c->g.ny;
+    if (adjoint && exact) CK(launch_fp64_vp_scale(c->dS, ncell, c->d64Grad, c->st));
+    if (adjoint && !exact) CK(launch_cp_frame(nullptr, c->d64Grad, c->g.nx, c->g.ny, c->g.nx, 1, c->st));
+    if (residual) CK(launch_sum_l2(c->d64l2, n, c->d64L2, c->st));
+    c->launches += (adjoint ? 1 : 0) + (residual ? 1 : 0);
+    std::vector<int> st(n);
+    CK(cudaMemcpyAsync(st.data(), c->d64Stat, n * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    int worst = 0;
+    for (int v : st) worst |= v;
+    const int code = status_to_code(worst);
+    if (code != RZ_OK) return fail(c, code, "FP64 oracle: device status bits 0x%x", worst);
+    return RZ_OK;
+}
+
+static int no_chunk_work(int, int) { return RZ_OK; }
+
+static int ensure_cmp(rz_context *c, int entries) {
+    if (entries > c->ncmp) {
+        CK(dalloc(&c->dCmp, (size_t)4 * entries));
+        c->ncmp = entries;
+    }
+    CK(cudaMemsetAsync(c->dCmp, 0, sizeof(double) * 4 * entries, c->st));
+    return RZ_OK;
+}
+
+// Error of the float results of the last call against the FP64 oracle on the
+// same inputs.  what: 0 forward (traveltimes, picks), 1 gradient (also the
+// gradient and misfit), 2 misfit (picks and misfit).  Traveltimes are
+// compared for the shots whose float fields are still in the slots (all of
+// them unless the batch ran in chunks).
+static int error_check(rz_context *c, int n, int what) {
+    const bool adjoint = what == 1, residual = what != 0;
+    const bool exact = adjoint && c->grad_kind == RZ_GRADIENT_EXACT;
+    const int t0 = c->last_first, t1 = c->last_n, ntt = std::max(0, t1 - t0);
+    const size_t fsf = (size_t)c->g.ny * c->nxp, fs64 = (size_t)c->g.nx * c->g.ny;
+    int r;
+    if ((r = ensure_cmp(c, ntt + 2))) return r;
+    r = run_fp64(c, n, adjoint, residual, exact, false, [&](int first, int m) -> int {
+        const int a = std::max(first, t0), b = std::min(first + m, t1);
+        if (a < b)
+            CK(launch_compare(c->dT + (size_t)(a - t0) * fsf, c->nxp, c->d64T + (size_t)(a - first) * fs64, c->g.nx,
+                              c->g.nx, c->g.ny, b - a, fsf, fs64, c->dCmp + 4 * (size_t)(a - t0), c->st));
+        return RZ_OK;
+    });
+    if (r) return r;
+    if (c->ntr > 0)
+        CK(launch_compare(c->dTmod, c->ntr, c->d64Tmod, c->ntr, c->ntr, n, 1, 0, 0, c->dCmp + 4 * (size_t)ntt, c->st));
+    if (adjoint)
+        CK(launch_compare(c->last_grad, c->g.nx, c->d64Grad, c->g.nx, c->g.nx, c->g.ny, 1, 0, 0,
+                          c->dCmp + 4 * (size_t)(ntt + 1), c->st));
+    std::vector<double> acc(4 * (size_t)(ntt + 2));
+    double l2[2] = {0.0, 0.0};
+    CK(cudaMemcpyAsync(acc.data(), c->dCmp, acc.size() * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    if (residual) {
+        CK(cudaMemcpyAsync(&l2[0], c->dL2, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaMemcpyAsync(&l2[1], c->d64L2, sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    }
+    CK(cudaStreamSynchronize(c->st));
+    rz_error e;
+    memset(&e, 0, sizeof e);
+    e.shots = ntt;
+    for (int z = 0; z < ntt; ++z) {
+        const double *q = &acc[4 * (size_t)z];
+        e.tt_rel = std::max(e.tt_rel, q[3] > 0 ? q[2] / q[3] : 0.0);
+        e.tt_rel_l2 = std::max(e.tt_rel_l2, q[1] > 0 ? std::sqrt(q[0] / q[1]) : 0.0);
+    }
+    const double *q = &acc[4 * (size_t)ntt];
+    e.tmod_rel = q[3] > 0 ? q[2] / q[3] : 0.0;
+    q = &acc[4 * (size_t)(ntt + 1)];
+    e.grad_rel_l2 = adjoint && q[1] > 0 ? std::sqrt(q[0] / q[1]) : 0.0;
+    e.grad_rel_max = adjoint && q[3] > 0 ? q[2] / q[3] : 0.0;
+    e.misfit_rel = residual && l2[1] != 0.0 ? std::fabs(l2[0] - l2[1]) / std::fabs(l2[1]) : 0.0;
+    c->err_rep = e;
+    c->err_valid = true;
+    return RZ_OK;
+}
+
+// copy n doubles from the device to dst as float (dst on the device with
+// dev, else host memory)
+static int out_as_float(rz_context *c, const double *src, float *dst, size_t n, bool dev) {
+    if (dev) {
+        CK(launch_d2f(src, dst, (long)n, c->st));
+        c->launches += 1;
+        return RZ_OK;
+    }
+    std::vector<double> h(n);
+    CK(cudaMemcpyAsync(h.data(), src, n * sizeof(double), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    for (size_t i = 0; i < n; ++i) dst[i] = (float)h[i];
+    return RZ_OK;
+}
+
+// upload sources (and picks) of an FP64 call; the float slots are not touched
+static int fp64_inputs(rz_context *c, int n, const float *srcx, const float *srcz, const float *Tobs, int flags) {
+    int r;
+    if ((r = ensure_shots(c, n))) return r;
+    if ((r = set_sources(c, n, srcx, srcz))) return r;
+    const size_t nt = (size_t)n * c->ntr;
+    if (Tobs && nt)
+        CK(cudaMemcpyAsync(c->dTobs, Tobs, nt * 4,
+                           have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, c->st));
+    return RZ_OK;
+}
+
 int rz_context_query(rz_context *c, int *nx, int *ny, float *dh, int *ntr, cudaStream_t *stream) {
     if (!c) return RZ_EINVAL;
     if (!c->grid_set) return fail(c, RZ_ESTATE, "rz_set_grid has not been called");
@@ -642,7 +885,8 @@ int rz_set_stream(rz_context *c, void *stream) {
 
 int rz_set_mode(rz_context *c, int mode) {
     if (!c) return RZ_EINVAL;
-    if (mode != RZ_MODE_REFERENCE && mode != RZ_MODE_FAST) return fail(c, RZ_EINVAL, "unknown mode %d", mode);
+    if (mode != RZ_MODE_REFERENCE && mode != RZ_MODE_FAST && mode != RZ_MODE_FP64)
+        return fail(c, RZ_EINVAL, "unknown mode %d", mode);
     c->mode = mode;
     return RZ_OK;
 }
@@ -855,8 +1099,8 @@ int rz_set_memory_cap(rz_context *c, size_t bytes) {
     return RZ_OK;
 }
 
-int rz_forward(rz_context *c, int nshots, const float *srcx, const float *srcz, float *TT, float *Tmod, int *passes,
-               int flags) {
+static int forward_impl(rz_context *c, int nshots, const float *srcx, const float *srcz, float *TT, float *Tmod,
+                        int *passes, int flags) {
     int r;
     if ((r = ready(c, false))) return r;
     if (nshots < 1) return fail(c, RZ_EINVAL, "nshots must be >= 1");
@@ -883,8 +1127,8 @@ int rz_forward(rz_context *c, int nshots, const float *srcx, const float *srcz, 
     return collect_status(c, nshots);
 }
 
-int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *Tobs, float *grad,
-                double *L2, int flags) {
+static int grad_obj_impl(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *Tobs,
+                         float *grad, double *L2, int flags) {
     int r;
     if ((r = ready(c, true))) return r;
     if (nshots < 1 || !Tobs || !grad) return fail(c, RZ_EINVAL, "bad arguments");
@@ -901,6 +1145,7 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
         if (!c->dGrad) CK(dalloc(&c->dGrad, (size_t)c->g.nx * c->g.ny));
         gdst = c->dGrad;
     }
+    c->last_grad = gdst;
     const bool exact = c->grad_kind == RZ_GRADIENT_EXACT;
     if ((c->mode == RZ_MODE_FAST || exact) && !c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
     if (!c->dL2) CK(dalloc(&c->dL2, 1));
@@ -1036,8 +1281,8 @@ int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz,
     return collect_status(c, nshots);
 }
 
-int rz_misfit(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *Tobs, double *L2,
-              int flags) {
+static int misfit_impl(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *Tobs,
+                       double *L2, int flags) {
     int r;
     if ((r = ready(c, true))) return r;
     if (nshots < 1 || !Tobs || !L2) return fail(c, RZ_EINVAL, "bad arguments");
@@ -1064,6 +1309,124 @@ int rz_misfit(rz_context *c, int nshots, const float *srcx, const float *srcz, c
     return collect_status(c, nshots);
 }
 
+
+int rz_forward(rz_context *c, int nshots, const float *srcx, const float *srcz, float *TT, float *Tmod, int *passes,
+               int flags) {
+    int r;
+    if (c && c->mode == RZ_MODE_FP64) {
+        if ((r = ready(c, false))) return r;
+        if (nshots < 1) return fail(c, RZ_EINVAL, "nshots must be >= 1");
+        cudaSetDevice(c->device);
+        if ((r = fp64_inputs(c, nshots, srcx, srcz, nullptr, flags))) return r;
+        const size_t fs = (size_t)c->g.nx * c->g.ny;
+        r = run_fp64(c, nshots, false, false, false, false, [&](int first, int m) -> int {
+            return TT ? out_as_float(c, c->d64T, TT + (size_t)first * fs, (size_t)m * fs, have_dev(flags)) : RZ_OK;
+        });
+        if (r) return r;
+        if (Tmod && c->ntr > 0 && (r = out_as_float(c, c->d64Tmod, Tmod, (size_t)nshots * c->ntr, have_dev(flags))))
+            return r;
+        if (passes) CK(cudaMemcpyAsync(passes, c->d64Pf, nshots * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+        CK(cudaStreamSynchronize(c->st));
+        return RZ_OK;
+    }
+    if ((r = forward_impl(c, nshots, srcx, srcz, TT, Tmod, passes, flags))) return r;
+    return c->err_check ? error_check(c, nshots, 0) : RZ_OK;
+}
+
+int rz_grad_obj(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *Tobs, float *grad,
+                double *L2, int flags) {
+    int r;
+    if (c && c->mode == RZ_MODE_FP64) {
+        if ((r = ready(c, true))) return r;
+        if (nshots < 1 || !Tobs || !grad) return fail(c, RZ_EINVAL, "bad arguments");
+        cudaSetDevice(c->device);
+        if ((r = fp64_inputs(c, nshots, srcx, srcz, Tobs, flags))) return r;
+        if ((r = run_fp64(c, nshots, true, true, c->grad_kind == RZ_GRADIENT_EXACT, false, no_chunk_work))) return r;
+        if ((r = out_as_float(c, c->d64Grad, grad, (size_t)c->g.nx * c->g.ny, have_dev(flags)))) return r;
+        if (L2)
+            CK(cudaMemcpyAsync(L2, c->d64L2, sizeof(double),
+                               have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
+        if (!have_dev(flags)) CK(cudaStreamSynchronize(c->st));
+        return RZ_OK;
+    }
+    if ((r = grad_obj_impl(c, nshots, srcx, srcz, Tobs, grad, L2, flags))) return r;
+    return c->err_check ? error_check(c, nshots, 1) : RZ_OK;
+}
+
+int rz_misfit(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *Tobs, double *L2,
+              int flags) {
+    int r;
+    if (c && c->mode == RZ_MODE_FP64) {
+        if ((r = ready(c, true))) return r;
+        if (nshots < 1 || !Tobs || !L2) return fail(c, RZ_EINVAL, "bad arguments");
+        cudaSetDevice(c->device);
+        if ((r = fp64_inputs(c, nshots, srcx, srcz, Tobs, flags))) return r;
+        if ((r = run_fp64(c, nshots, false, true, false, false, no_chunk_work))) return r;
+        CK(cudaMemcpyAsync(L2, c->d64L2, sizeof(double),
+                           have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, c->st));
+        if (!have_dev(flags)) CK(cudaStreamSynchronize(c->st));
+        return RZ_OK;
+    }
+    if ((r = misfit_impl(c, nshots, srcx, srcz, Tobs, L2, flags))) return r;
+    return c->err_check ? error_check(c, nshots, 2) : RZ_OK;
+}
+
+int rz_forward_f64(rz_context *c, int nshots, const float *srcx, const float *srcz, double *TT, double *Tmod,
+                   int flags) {
+    int r;
+    if ((r = ready(c, false))) return r;
+    if (nshots < 1) return fail(c, RZ_EINVAL, "nshots must be >= 1");
+    cudaSetDevice(c->device);
+    if ((r = fp64_inputs(c, nshots, srcx, srcz, nullptr, flags))) return r;
+    const size_t fs = (size_t)c->g.nx * c->g.ny;
+    const cudaMemcpyKind k = have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    r = run_fp64(c, nshots, false, false, false, false, [&](int first, int m) -> int {
+        if (TT) CK(cudaMemcpyAsync(TT + (size_t)first * fs, c->d64T, (size_t)m * fs * sizeof(double), k, c->st));
+        return RZ_OK;
+    });
+    if (r) return r;
+    if (Tmod && c->ntr > 0)
+        CK(cudaMemcpyAsync(Tmod, c->d64Tmod, (size_t)nshots * c->ntr * sizeof(double), k, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return RZ_OK;
+}
+
+int rz_grad_obj_f64(rz_context *c, int nshots, const float *srcx, const float *srcz, const float *Tobs, double *grad,
+                    double *L2, int flags) {
+    int r;
+    if ((r = ready(c, true))) return r;
+    if (nshots < 1 || !Tobs || !grad) return fail(c, RZ_EINVAL, "bad arguments");
+    cudaSetDevice(c->device);
+    if ((r = fp64_inputs(c, nshots, srcx, srcz, Tobs, flags))) return r;
+    if ((r = run_fp64(c, nshots, true, true, c->grad_kind == RZ_GRADIENT_EXACT, false, no_chunk_work))) return r;
+    const cudaMemcpyKind k = have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost;
+    CK(cudaMemcpyAsync(grad, c->d64Grad, (size_t)c->g.nx * c->g.ny * sizeof(double), k, c->st));
+    if (L2) CK(cudaMemcpyAsync(L2, c->d64L2, sizeof(double), k, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    return RZ_OK;
+}
+
+int rz_set_wait_test(rz_context *c, unsigned spin_limit, int withhold_handoff) {
+    if (!c) return RZ_EINVAL;
+    c->spin = spin_limit;
+    c->withhold = withhold_handoff != 0;
+    return RZ_OK;
+}
+
+int rz_set_error_check(rz_context *c, int enable) {
+    if (!c) return RZ_EINVAL;
+    c->err_check = enable != 0;
+    c->err_valid = false;
+    return RZ_OK;
+}
+
+int rz_error_report(rz_context *c, rz_error *err) {
+    if (!c || !err) return RZ_EINVAL;
+    if (!c->err_valid) return fail(c, RZ_ESTATE, "no error report: enable rz_set_error_check before the call");
+    *err = c->err_rep;
+    return RZ_OK;
+}
+
 int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, const float *const *srcx,
                       const float *const *srcz, const float *const *Tobs, float *const *grad, double *L2, int flags) {
     if (ngrids < 1 || ngrids > kMaxGrids || !ctxs || !nshots || !srcx || !srcz || !Tobs || !grad || !L2)
@@ -1078,6 +1441,7 @@ int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, co
         if ((r = ready(c, true))) return fail(c0, r, "grid %d: %s", i, c->err.c_str());
         if (c->device != c0->device || c->mode != c0->mode)
             return fail(c0, RZ_EINVAL, "grid %d: every context must use the same device and mode", i);
+        if (c->mode == RZ_MODE_FP64) return fail(c0, RZ_EUNSUPPORTED, "grid %d: FP64 mode has no multi-grid launch", i);
         if (c->grad_kind != RZ_GRADIENT_REFERENCE)
             return fail(c0, RZ_EUNSUPPORTED, "grid %d: the exact gradient is not available in multi-grid launches", i);
         if (nshots[i] < 1 || !Tobs[i] || !grad[i]) return fail(c0, RZ_EINVAL, "grid %d: bad arguments", i);
@@ -1189,6 +1553,7 @@ int rz_autotune(rz_context *c, int nshots, const float *srcx, const float *srcz,
                 int flags, int *best_warps, double *best_ms, int *cand_warps, double *cand_ms, int *ncand) {
     int r;
     if ((r = ready(c, true))) return r;
+    if (c->mode == RZ_MODE_FP64) return fail(c, RZ_EUNSUPPORTED, "the autotuner times the float kernels only");
     if (nshots < 1 || !grad) return fail(c, RZ_EINVAL, "bad arguments");
     cudaSetDevice(c->device);
     // candidates: the balanced width for the fewest bands and one or two more bands
@@ -1262,6 +1627,13 @@ int rz_backward(rz_context *c, int nshots, const float *srcx, const float *srcz,
     if ((r = ready(c, true))) return r;
     if (nshots < 1 || !grad || (c->ntr > 0 && !dTmod)) return fail(c, RZ_EINVAL, "bad arguments");
     cudaSetDevice(c->device);
+    if (c->mode == RZ_MODE_FP64) {
+        if ((r = fp64_inputs(c, nshots, srcx, srcz, dTmod, flags))) return r;
+        if ((r = run_fp64(c, nshots, true, true, true, true, no_chunk_work))) return r;
+        if ((r = out_as_float(c, c->d64Grad, grad, (size_t)c->g.nx * c->g.ny, have_dev(flags)))) return r;
+        if (!have_dev(flags)) CK(cudaStreamSynchronize(c->st));
+        return RZ_OK;
+    }
     const int kind = c->grad_kind;
     c->grad_kind = RZ_GRADIENT_EXACT;  // the slots need the exact-adjoint arrays
     int chunk = 0;
@@ -1293,6 +1665,21 @@ int rz_backward(rz_context *c, int nshots, const float *srcx, const float *srcz,
     if (have_dev(flags)) return RZ_OK;
     CK(cudaMemcpyAsync(grad, gdst, (size_t)c->g.nx * c->g.ny * 4, cudaMemcpyDeviceToHost, c->st));
     return collect_status(c, nshots);
+}
+
+int rz_status_code(int bits) { return status_to_code(bits); }
+
+int rz_batch_status(rz_context *c, int *bits) {
+    if (!c || !bits) return RZ_EINVAL;
+    cudaSetDevice(c->device);
+    const int n = c->last_n;
+    std::vector<int> st(n > 0 ? n : 1, 0);
+    if (n > 0) CK(cudaMemcpyAsync(st.data(), c->dStat, n * sizeof(int), cudaMemcpyDeviceToHost, c->st));
+    CK(cudaStreamSynchronize(c->st));
+    int worst = 0;
+    for (int i = 0; i < n; ++i) worst |= st[i];
+    *bits = worst;
+    return RZ_OK;
 }
 
 int rz_shot_info(rz_context *c, int shot, int *fwd_passes, int *adj_passes, int *status) {
@@ -1381,6 +1768,7 @@ int rz_eikonal(rz_context *c, float srcx, float srcz, float *TT, float *Tmod, in
 int rz_eikonal_adj(rz_context *c, const float *TT, const float *Tres, float *lam, int *passes, int flags) {
     int r;
     if ((r = ready(c, true))) return r;
+    if (c->mode == RZ_MODE_FP64) return fail(c, RZ_EUNSUPPORTED, "eikonal_adj takes float traveltimes; use rz_grad_obj");
     if (!TT || !lam || (c->ntr > 0 && !Tres)) return fail(c, RZ_EINVAL, "bad arguments");
     cudaSetDevice(c->device);
     if ((r = ensure_shots(c, 1)) || (r = ensure_fields(c, 1))) return r;

@@ -195,7 +195,7 @@ __device__ void cp_frame_pass(V *A, int nx, int ny, int nxp) {
 
 __global__ void cp_frame_kernel(float *A, double *A64, int nx, int ny, int nxp, int times) {
     for (int t = 0; t < times; ++t) {
-        cp_frame_pass(A, nx, ny, nxp);
+        if (A) cp_frame_pass(A, nx, ny, nxp);
         if (A64) cp_frame_pass(A64, nx, ny, nxp);
     }
 }

@@ -32,10 +32,14 @@ extern void write_picks(float *Tmod, int ntr, int ishot);
 extern void precond(float **grad, int nsrc, float **srcpos, int **recpos, int ntr, int iter);
 #ifdef RZ_COMPAT_MPI
 extern void sum_grad_MPI(float **grad);
+extern void cp_grad_frame(float **A);
 #endif
 
 static rz_context *g_ctx = NULL;
 static int g_device = -1, g_mode = -1;
+/* the receiver geometry the engine holds (see receivers()) */
+static int g_ntr = -1;
+static int *g_recx = NULL, *g_recz = NULL;
 
 int rz_compat_configure(int device, int mode) {
     g_device = device;
@@ -43,6 +47,7 @@ int rz_compat_configure(int device, int mode) {
     if (g_ctx) {
         rz_destroy(g_ctx);
         g_ctx = NULL;
+        g_ntr = -1;
     }
     return RZ_OK;
 }
@@ -73,15 +78,34 @@ static void engine(void) {
     g.ttnorm = TTNORM;
     g.eps_adj = EPS_ADJ;
     g.max_passes = 0;
+    static int last_nx = -1, last_ny = -1;
     int st = rz_set_grid(g_ctx, &g);
     if (st) fail("rz_set_grid", st);
+    if (NX != last_nx || NY != last_ny) g_ntr = -1; /* a new shape drops the engine's receivers */
+    last_nx = NX, last_ny = NY;
+}
+
+/* The receiver geometry is uploaded only when it differs from the last one
+   the engine received: FATT calls grad_obj() for every line-search trial with
+   the same recpos, and only the model changes between them. */
+static void receivers(int **recpos, int ntr) {
+    const size_t bytes = sizeof(int) * (size_t)(ntr > 0 ? ntr : 1);
+    if (ntr == g_ntr && (ntr == 0 || (!memcmp(g_recx, &recpos[1][1], sizeof(int) * ntr) &&
+                                      !memcmp(g_recz, &recpos[2][1], sizeof(int) * ntr))))
+        return;
+    int st = rz_set_receivers(g_ctx, ntr, ntr > 0 ? &recpos[1][1] : NULL, ntr > 0 ? &recpos[2][1] : NULL);
+    if (st) fail("rz_set_receivers", st);
+    free(g_recx), free(g_recz);
+    g_recx = (int *)malloc(bytes), g_recz = (int *)malloc(bytes);
+    if (!g_recx || !g_recz) err("rz_compat: host allocation failed");
+    if (ntr > 0) memcpy(g_recx, &recpos[1][1], sizeof(int) * ntr), memcpy(g_recz, &recpos[2][1], sizeof(int) * ntr);
+    g_ntr = ntr;
 }
 
 static void model_and_receivers(float **S, int **recpos, int ntr) {
     int st = rz_set_slowness(g_ctx, &S[1][1], 0);
     if (st) fail("rz_set_slowness", st);
-    st = rz_set_receivers(g_ctx, ntr, ntr > 0 ? &recpos[1][1] : NULL, ntr > 0 ? &recpos[2][1] : NULL);
-    if (st) fail("rz_set_receivers", st);
+    receivers(recpos, ntr);
 }
 
 /* eikonal.c:10-76 */
@@ -104,15 +128,54 @@ void eikonal_adj(float **TT, float *Tres, float **lam, int **recpos, int ntr, in
     (void)ishot;
     (void)recflag;
     engine();
-    int st = rz_set_receivers(g_ctx, ntr, ntr > 0 ? &recpos[1][1] : NULL, ntr > 0 ? &recpos[2][1] : NULL);
-    if (st) fail("rz_set_receivers", st);
-    st = rz_eikonal_adj(g_ctx, &TT[1][1], ntr > 0 ? &Tres[1] : NULL, &lam[1][1], NULL, 0);
+    receivers(recpos, ntr);
+    int st = rz_eikonal_adj(g_ctx, &TT[1][1], ntr > 0 ? &Tres[1] : NULL, &lam[1][1], NULL, 0);
     if (st) fail("rz_eikonal_adj", st);
 }
 
-/* forward.c:10-26: this rank's shots NSHOT1..NSHOT2-1 */
+/* forward.c:10-26: this rank's shots NSHOT1..NSHOT2-1 in batched engine calls
+   (chunks of kForwardChunk shots bound the host copy of their traveltime
+   fields, which only the snapshot files need), then per shot in shot order
+   what eikonal() does after its solve: the snapshot file (SNAP == 1) and the
+   picks file (SEISMO == 1).  TT and Tmod are left holding the last shot's
+   fields, as the reference's loop leaves them. */
+enum { kForwardChunk = 64 };
 void forward(float **S, float **TT, float *Tmod, float **srcpos, int nshots, int **recpos, int ntr) {
-    for (int ishot = NSHOT1; ishot < NSHOT2; ishot++) eikonal(S, TT, Tmod, srcpos, ishot, nshots, recpos, ntr);
+    (void)nshots;
+    const int n = NSHOT2 - NSHOT1;
+    if (n <= 0) return;
+    engine();
+    model_and_receivers(S, recpos, ntr);
+    const size_t cells = (size_t)NX * NY, nt = (size_t)(ntr > 0 ? ntr : 1);
+    const int chunk = n < kForwardChunk ? n : kForwardChunk;
+    float *sx = (float *)malloc(sizeof(float) * chunk), *sz = (float *)malloc(sizeof(float) * chunk);
+    float *tm = (float *)malloc(sizeof(float) * nt * chunk);
+    float *tt = SNAP == 1 ? (float *)malloc(sizeof(float) * cells * chunk) : NULL;
+    if (!sx || !sz || !tm || (SNAP == 1 && !tt)) err("forward: host allocation failed");
+    int m = 0;
+    for (int first = NSHOT1; first < NSHOT2; first += chunk) {
+        m = NSHOT2 - first < chunk ? NSHOT2 - first : chunk;
+        for (int s = 0; s < m; s++) sx[s] = srcpos[1][first + s], sz[s] = srcpos[2][first + s];
+        int st = rz_forward(g_ctx, m, sx, sz, tt, ntr > 0 ? tm : NULL, NULL, 0);
+        if (st) fail("rz_forward", st);
+        for (int s = 0; s < m; s++) {
+            const int ishot = first + s;
+            for (int i = 0; i < ntr; i++) Tmod[i + 1] = tm[(size_t)s * ntr + i];
+            if (SNAP == 1) {
+                char filename[RZ_STRING_SIZE];
+                memcpy(&TT[1][1], tt + (size_t)s * cells, sizeof(float) * cells);
+                snprintf(filename, sizeof filename, "%s_shot_%d.tt", SNAP_FILE, ishot);
+                writemod(filename, TT, 3);
+            }
+            if (SEISMO == 1) write_picks(Tmod, ntr, ishot);
+        }
+    }
+    /* the last shot's traveltimes, where the reference's loop leaves them */
+    if (SNAP != 1) {
+        int st = rz_shot_fields(g_ctx, m - 1, &TT[1][1], NULL, NULL, 0);
+        if (st) fail("rz_shot_fields", st);
+    }
+    free(sx), free(sz), free(tm), free(tt);
 }
 
 /* picks of one shot from DATA_DIR_<ishot>.dat, one value per line (calc_FA_res.c:28-37) */
@@ -165,9 +228,14 @@ double grad_obj(float **grad, float **S, float **TT, float **lam, float *Tmod, f
     MPI_Barrier(MPI_COMM_WORLD);
     MPI_Allreduce(&L2, &L2sum, 1, MPI_DOUBLE, MPI_SUM, MPI_COMM_WORLD);
     L2 = L2sum;
+    /* sum_grad_MPI reduces NX*NY floats from index 0 of a vector filled from
+       index 1, so the corner cell grad[NY][NX] comes back uninitialised
+       (sum_grad_MPI.c:24-36); the reference's frame copy after it
+       (grad_obj.c:68-70) overwrites that corner, and so does this one */
     sum_grad_MPI(grad);
+    cp_grad_frame(grad);
 #endif
-    /* the engine already applied cp_grad_frame (grad_obj.c:70) */
+    /* single rank: the engine already applied cp_grad_frame (grad_obj.c:70) */
     precond(grad, nshots, srcpos, recpos, ntr, iter); /* grad_obj.c:73 */
     return 0.5 * L2;
 }

@@ -23,6 +23,7 @@ enum : int {
     ERR_NOCONV_FWD = 1 << 2,     // forward did not meet TTNORM within max passes
     ERR_NOCONV_ADJ = 1 << 3,     // adjoint did not meet TTNORM within max passes
     ERR_BAD_SOURCE = 1 << 4,     // source index outside the grid
+    ERR_BAD_MODEL = 1 << 5,      // a slowness is not a positive finite number (no solve ran)
 };
 
 // Bounded waits.  Legitimate waits in these kernels last microseconds; a
@@ -97,10 +98,12 @@ RZ_DEV bool mbar_try_wait_a(uint32_t bar, uint32_t parity) {
         : "memory");
     return ok != 0;
 }
-// Bounded wait; returns false on timeout or abort (abort word in shared memory).
-RZ_DEV bool mbar_wait_a(uint32_t bar, uint32_t parity, uint32_t abort_word) {
+// Bounded wait for another warp's signal; returns false on timeout (after
+// `limit` polls, raising the abort word) or at once when the CTA's abort word
+// (shared memory) is up.
+RZ_DEV bool mbar_wait_a(uint32_t bar, uint32_t parity, uint32_t abort_word, uint32_t limit = kSpinLimit) {
     if (mbar_try_wait_a(bar, parity)) return true;
-    for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    for (uint32_t i = 0; i < limit; ++i) {
         if (mbar_try_wait_a(bar, parity)) return true;
         int ab;
         asm volatile("ld.volatile.shared.b32 %0, [%1];" : "=r"(ab) : "r"(abort_word) : "memory");
@@ -110,13 +113,12 @@ RZ_DEV bool mbar_wait_a(uint32_t bar, uint32_t parity, uint32_t abort_word) {
     return false;
 }
 
-// Bounded wait on an mbarrier phase.  Returns false on timeout or abort.
-RZ_DEV bool mbar_wait(uint64_t *bar, uint32_t parity, volatile int *abort_word) {
-    for (uint32_t i = 0; i < kSpinLimit; ++i) {
-        if (mbar_try_wait(bar, parity)) return true;
-        if (*abort_word) return false;
-    }
-    *abort_word = 1;
+// Bounded wait for a tensor copy issued by this warp.  A copy always lands,
+// and a warp must not leave its copies in flight, so this wait ignores the
+// abort word; false only if kSpinLimit polls pass (broken hardware).
+RZ_DEV bool mbar_wait_copy(uint32_t bar, uint32_t parity) {
+    for (uint32_t i = 0; i < kSpinLimit; ++i)
+        if (mbar_try_wait_a(bar, parity)) return true;
     return false;
 }
 
@@ -201,11 +203,11 @@ RZ_DEV int ld_acquire_smem(const int *p) {
 // Hand-off waits are short and frequent (a consumer warp trails its producer
 // by a few dozen steps), so the first polls spin; only a long wait backs off
 // with __nanosleep, whose wake-up latency is microseconds.
-RZ_DEV bool wait_flag_ge(const int *flag, int need, volatile int *abort_word) {
+RZ_DEV bool wait_flag_ge(const int *flag, int need, volatile int *abort_word, uint32_t limit = kSpinLimit) {
     for (int i = 0; i < 2048; ++i)
         if (ld_acquire_smem(flag) >= need) return true;
     uint32_t ns = 32;
-    for (uint32_t i = 0; i < kSpinLimit; ++i) {
+    for (uint32_t i = 0; i < limit; ++i) {
         __nanosleep(ns);
         if (ns < 256) ns <<= 1;
         if (ld_acquire_smem(flag) >= need) return true;

@@ -102,6 +102,14 @@ struct ShotParams {
     // tasks no change can reach), or null
     uint8_t *chg;
     size_t chg_stride;                      // nstrips*4*(nxb+1)
+    // launch_prep_model's first-invalid-cell word (kModelOk: none), or null:
+    // an invalid model ends every shot at once with ERR_BAD_MODEL
+    const int *model_bad;
+    // waits for another warp give up after `spin` polls (0: kSpinLimit);
+    // withhold (test hook): warp 0 of every CTA withholds one hand-off
+    // signal in its first sweep, so warp 1's bounded wait runs out
+    uint32_t spin;
+    int withhold;
 };
 
 // Tensor maps of a launch.  Field maps cover [shots][ny][nxp] floats with
@@ -179,6 +187,41 @@ cudaError_t launch_finish_grad(const float *g, float *gout, long n, const double
                                const int *status, int nshots, int *status_out, cudaStream_t st);
 // *out = 0.5 * sum_z l2[z], summed in shot order in double (grad_obj.c:28,42,61)
 cudaError_t launch_sum_l2(const double *l2, int n, double *out, cudaStream_t st);
+
+// FP64 oracle (rz_fp64.cu): one CTA per shot, double fields [shot][ny][nx]
+struct F64Params {
+    int nx, ny, nxp;
+    double dh, time, ttnorm, eps_adj;  // the float globals, widened
+    int max_passes;
+    int nshots;
+    int do_residual, do_adjoint;
+    int exact;                   // adjoint: 0 Leung-Qian, 1 exact discrete adjoint
+    int cotangent;               // exact: Tobs holds dJ/dTmod itself
+    const float *S;              // slowness [ny][nx]
+    const uint8_t *skip;         // [ny][nxp]: cells the Leung-Qian sweeps leave unchanged
+    const int *src_h, *src_k;    // [nshots]
+    int ntr;
+    const int *rec_h, *rec_k;
+    int nrcell;
+    const int *rcell_h, *rcell_k, *rcell_rec;
+    int nxcell;
+    const int *xcell_h, *xcell_k, *xcell_off, *xcell_rec;
+    const float *Tobs;           // [nshots][ntr]
+    double *T, *A, *L;           // traveltime, snapshot (exact: R), adjoint field (exact: mu)
+    double *WX, *WZ, *GS;        // exact: signed weights and dG/dS per cell
+    double *Tmod, *Tres, *l2;    // [nshots][ntr], [nshots][ntr], [nshots]
+    int *passes_fwd, *passes_adj, *status;
+    size_t fstride;              // nx*ny
+};
+cudaError_t launch_fp64_shots(const F64Params &P, cudaStream_t st);
+// gradient of the launch's shots added to grad64 [ny][nx] in shot order
+cudaError_t launch_fp64_stack(const F64Params &P, double *grad64, bool accumulate, cudaStream_t st);
+cudaError_t launch_fp64_vp_scale(const float *S, long n, double *grad64, cudaStream_t st);
+// acc[4 z + 0..3] += sum (a-b)^2, sum b^2, max |a-b|, max |b| over rows of
+// ncol values of batch entry z (a float with row pitch pa, b double with pb)
+cudaError_t launch_compare(const float *a, int pa, const double *b, int pb, int ncol, long nrow, int nbatch,
+                           size_t bstride_a, size_t bstride_b, double *acc, cudaStream_t st);
+cudaError_t launch_d2f(const double *src, float *dst, long n, cudaStream_t st);
 
 }  // namespace rz
 

@@ -1,15 +1,16 @@
 // rz_noalloc.cu -- forward Eikonal for callers that cannot allocate memory.
 //
-// Some callers must not allocate GPU memory at all: code running inside a
-// CUDA-graph capture or a pre-sized memory pool, allocator-less embedded
-// hosts, or a time step of a larger solver that has fixed its memory budget
-// up front.  rz_eikonal_noalloc() serves them: it computes one shot's
+// Some callers must not allocate GPU memory at all: code working inside a
+// pre-sized memory pool, allocator-less embedded hosts, or a time step of a
+// larger solver that has fixed its memory budget up front.  rz_eikonal_noalloc() serves them: it computes one shot's
 // traveltime field with the same kernels and reference-exact arithmetic as
 // rz_eikonal(), but never calls cudaMalloc, cudaFree or any allocating
 // routine.  Its working space (traveltimes in a pitched layout, the pass
 // snapshot, two skewed copies of the slowness, two source indices) lives in
 // one file-scope __device__ array of kNoAllocFloats floats (32 MiB), which
-// every GPU that loads the library holds until the process exits.
+// every GPU that loads the library holds until the process exits.  The
+// slowness is checked on the device (first invalid cell in the array); an
+// invalid model sets status bit ERR_BAD_MODEL and no solve runs.
 //
 // Rules for callers:
 //   * the first call on a device looks up the array's device address
@@ -59,17 +60,26 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t
                                   const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-bool encode_field_map(CUtensorMap *m, float *base, int nx, int ny, int nxp, int box_cols, int box_rows) {
+// the driver's tensor-map encoder, looked up once for all host threads
+EncodeTiledFn encoder() {
+    static std::once_flag once;
     static EncodeTiledFn fn = nullptr;
-    if (!fn) {
+    std::call_once(once, [] {
         void *p = nullptr;
         cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) !=
-                cudaSuccess ||
-            q != cudaDriverEntryPointSuccess)
-            return false;
-        fn = reinterpret_cast<EncodeTiledFn>(p);
-    }
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<EncodeTiledFn>(p);
+        else
+            (void)cudaGetLastError();
+    });
+    return fn;
+}
+
+bool encode_field_map(CUtensorMap *m, float *base, int nx, int ny, int nxp, int box_cols, int box_rows) {
+    const EncodeTiledFn fn = encoder();
+    if (!fn) return false;
     cuuint64_t dims[3] = {(cuuint64_t)nx, (cuuint64_t)ny, 1};
     cuuint64_t strides[2] = {(cuuint64_t)nxp * 4, (cuuint64_t)nxp * ny * 4};
     cuuint32_t box[3] = {(cuuint32_t)box_cols, (cuuint32_t)box_rows, 1};
@@ -109,7 +119,7 @@ extern "C" int rz_eikonal_noalloc(const rz_grid *grid, const float *S, float src
     float *base = nullptr;
     if (int r = scratch_address(&base)) return r;
     float *T = base, *Told = base + field, *Sp = base + 2 * field, *SA = base + 3 * field, *SB = SA + skew;
-    int *src = reinterpret_cast<int *>(SB + skew);
+    int *src = reinterpret_cast<int *>(SB + skew);  // [0..1] source index, [2] first invalid slowness cell
 
     ShotMaps M;
     if (!encode_field_map(&M.tld, T, g.nx, g.ny, nxp, kBlk, kBoxRows) ||
@@ -146,12 +156,15 @@ extern "C" int rz_eikonal_noalloc(const rz_grid *grid, const float *S, float src
     P.src_k = src + 1;
     P.passes_fwd = info;
     P.status = info + 1;
+    P.model_bad = src + 2;
 
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    if (launch_skew_field(S, g.nx, g.ny, g.nx, nstrips, nxb, SA, SB, st) != cudaSuccess) return RZ_ECUDA;
-    if (cudaMemcpy2DAsync(Sp, (size_t)nxp * 4, S, (size_t)g.nx * 4, (size_t)g.nx * 4, g.ny, cudaMemcpyDeviceToDevice,
-                          st) != cudaSuccess)
+    // the row-pitched copy of S and its first invalid cell (as rz_set_slowness
+    // checks it); with S given as both source and destination nothing is
+    // written to the caller's array
+    if (launch_prep_model(S, false, const_cast<float *>(S), Sp, g.nx, g.ny, nxp, src + 2, st) != cudaSuccess)
         return RZ_ECUDA;
+    if (launch_skew_field(S, g.nx, g.ny, g.nx, nstrips, nxb, SA, SB, st) != cudaSuccess) return RZ_ECUDA;
     noalloc_prologue<<<1, 1, 0, st>>>(src, hs, ks, info);
     if (cudaGetLastError() != cudaSuccess) return RZ_ECUDA;
     if (launch_shot_kernel(P, kModeReference, M, st) != cudaSuccess) return RZ_ECUDA;

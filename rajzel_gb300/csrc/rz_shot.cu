@@ -24,6 +24,7 @@
 // 32 values one wavefront step needs are one 128-byte line: fully coalesced
 // and prefetched eight steps ahead into registers.
 #include <algorithm>
+#include <mutex>
 
 #include "rz_device.cuh"
 #include "rz_internal.h"
@@ -153,7 +154,7 @@ RZ_DEV void stamp(const ShotParams &P, int z, int slot) {
 
 RZ_DEV void ring_wait(Warp &w, int slot) {
     uint32_t par = (w.phase >> slot) & 1u;
-    if (!mbar_wait(&w.mbar[slot], par, w.abort_word)) w.err |= ERR_TMA_TIMEOUT;
+    if (!mbar_wait_copy(smem_u32(&w.mbar[slot]), par)) w.err |= ERR_TMA_TIMEOUT;
     w.phase ^= 1u << slot;
 }
 
@@ -184,6 +185,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const int l = w.l, g = w.g;
     if (g >= W) return;  // warps beyond this grid's W only join the CTA's barriers
     const bool pipe = seq.pipelined != 0;
+    const uint32_t spin = P.spin ? P.spin : kSpinLimit;  // polls before a wait for another warp gives up
     // strips are swept in bands of W (one strip per warp); sig is the strip's
     // position in sweep order, s its index from the top of the grid
     const int sig = pipe ? (DY > 0 ? g : P.nstrips - 1 - g) : band * W + g;
@@ -213,7 +215,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     if (pipe && is_producer_warp) {
         // the halo row belongs to the next strip in sweep order: it must hold
         // that strip's values after the previous sweep
-        if (l == 0 && !wait_flag_ge(w.done + (DY > 0 ? g + 1 : g - 1), seq.n, w.abort_word)) w.err |= ERR_FLAG_TIMEOUT;
+        if (l == 0 && !wait_flag_ge(w.done + (DY > 0 ? g + 1 : g - 1), seq.n, w.abort_word, spin))
+            w.err |= ERR_FLAG_TIMEOUT;
         __syncwarp();
         fence_proxy_async_global();
     }
@@ -226,6 +229,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
         prev_row = (ADJ ? P.L : P.T) + (size_t)z * P.fstride + (size_t)rup * P.nxp;
     }
     const bool producer = (l == 31) && is_producer_warp;
+    // test hook: warp 0 withholds the signal of hand-off group 2 of its first sweep
+    const bool withhold = P.withhold && g == 0 && seq.n == 0;
     const int ngrp = ncol >> 3;  // hand-off groups per sweep
     float *ring = &w.ws->ring[0][0];
     const uint32_t ring_s = smem_u32(ring);
@@ -258,7 +263,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     float acc_l = 0.f;  // fast-mode sum of |change| (the caller's acc lives in local memory)
     float mag_l = 0.f;  // exact adjoint: sum of |mu|
     auto ring_wait_l = [&](int slot) {
-        if (!mbar_wait_a(mbar_s + 8u * slot, (phase >> slot) & 1u, abort_s)) err |= ERR_TMA_TIMEOUT;
+        if (!mbar_wait_copy(mbar_s + 8u * slot, (phase >> slot) & 1u)) err |= ERR_TMA_TIMEOUT;
         phase ^= 1u << slot;
     };
 
@@ -419,7 +424,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 const int G = t0 >> 3;
                 if (G < ngrp) {
                     const int Gg = G + cons_base;  // group number in this ring's lifetime
-                    if (!mbar_wait_a(full_in + 8u * (Gg & (kGroups - 1)), (Gg >> kGroupsLog2) & 1, abort_s)) err |= ERR_FLAG_TIMEOUT;
+                    if (!mbar_wait_a(full_in + 8u * (Gg & (kGroups - 1)), (Gg >> kGroupsLog2) & 1, abort_s, spin))
+                        err |= ERR_FLAG_TIMEOUT;
                     const uint32_t hb_g = hb_in + 4u * (uint32_t)((t0 + cb8) & (kHandoff - 1));  // 32-byte aligned
                     const float4 h0 = lds4(hb_g), h1 = lds4(hb_g + 16u);
                     hbq[0] = h0.x, hbq[1] = h0.y, hbq[2] = h0.z, hbq[3] = h0.w;
@@ -446,7 +452,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 // lane 31 writes hand-off group Gp (columns t0-32 .. t0-25) in this group
                 const int Gp = (t0 - 32) >> 3, Gpg = Gp + prod_base;
                 if (t0 >= 32 && Gpg >= kGroups && Gp < ngrp &&
-                    !mbar_wait_a(empty_out + 8u * (Gpg & (kGroups - 1)), ((Gpg >> kGroupsLog2) - 1) & 1, abort_s))
+                    !mbar_wait_a(empty_out + 8u * (Gpg & (kGroups - 1)), ((Gpg >> kGroupsLog2) - 1) & 1, abort_s,
+                                 spin))
                     err |= ERR_FLAG_TIMEOUT;
             }
             {
@@ -584,7 +591,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 if (ii == 5) h5 = r;
                 if (ii == 6) {
                     sts4_if(hq + 16u, h3, h4, h5, r, hand);
-                    mbar_arrive_if(full_out + 8u * (uint32_t)(((upp0 + pb8) >> 3) & (kGroups - 1)), hand);
+                    mbar_arrive_if(full_out + 8u * (uint32_t)(((upp0 + pb8) >> 3) & (kGroups - 1)),
+                                   hand && !(withhold && upp0 == 16));
                 }
                 if (ii == 7) hand_carry = r;
                 if (REC) changed |= valid && r != own;
@@ -789,7 +797,7 @@ struct CheckRing {
     int err;
     RZ_DEV void wait(int b) {
         const int s = b % kCheckSlots;
-        if (!mbar_wait_a(bars + 8u * s, (phase >> s) & 1u, abort_s)) err |= ERR_TMA_TIMEOUT;
+        if (!mbar_wait_copy(bars + 8u * s, (phase >> s) & 1u)) err |= ERR_TMA_TIMEOUT;
         phase ^= 1u << s;
     }
 };
@@ -1190,6 +1198,13 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
     w.abort_word = &sh.ctl[1];
 
     stamp(P, z, 0);
+    if (P.model_bad && *(volatile const int *)P.model_bad != kModelOk) {
+        if (tid == 0) {
+            P.passes_fwd[z] = 0;
+            atomicOr(&P.status[z], ERR_BAD_MODEL);
+        }
+        return;
+    }
     float *T = P.T + (size_t)z * P.fstride;
     float *Told = P.Told + (size_t)z * P.fstride;
     float *L = P.L + (size_t)z * P.fstride;
@@ -1485,15 +1500,24 @@ static cudaError_t block_warps(K kern, int W, int *Wb_out) {
 }
 
 // block_warps, remembered per kernel and W
+// The answer depends on the device (its shared-memory limit): the cache is
+// kept per device and shared by host threads under a lock.
+constexpr int kMaxCachedDevices = 64;
+static std::mutex g_block_warps_mutex;
 template <class K>
 static cudaError_t block_warps_cached(K kern, int slot, int W, int *Wb) {
-    static int cache[4][kMaxWarps + 1];
-    if (cache[slot][W] > 0) {
-        *Wb = cache[slot][W];
+    static int cache[kMaxCachedDevices][4][kMaxWarps + 1];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e) return e;
+    if (dev < 0 || dev >= kMaxCachedDevices) return block_warps(kern, W, Wb);
+    std::lock_guard<std::mutex> lock(g_block_warps_mutex);
+    if (cache[dev][slot][W] > 0) {
+        *Wb = cache[dev][slot][W];
         return cudaSuccess;
     }
-    cudaError_t e = block_warps(kern, W, Wb);
-    if (!e) cache[slot][W] = *Wb;
+    e = block_warps(kern, W, Wb);
+    if (!e) cache[dev][slot][W] = *Wb;
     return e;
 }
 

@@ -12,6 +12,10 @@
 
 #include "rajzel_compat.h"
 
+#ifdef RZ_COMPAT_MPI
+#include <mpi.h>
+#endif
+
 float DH, TIME, TTNORM, EPS_ADJ;
 int NX, NY, SNAP = 0, SEISMO = 0, NSHOT1 = 1, NSHOT2 = 1;
 char SNAP_FILE[74], DATA_DIR[74];
@@ -23,7 +27,49 @@ void err(char err_text[]) {
     exit(3);
 }
 void writemod(char modfile[74], float **array, int format) { (void)modfile, (void)array, (void)format; }
-void write_picks(float *Tmod, int ntr, int ishot) { (void)Tmod, (void)ntr, (void)ishot; }
+
+/* picks written through write_picks(), kept per shot for the tests */
+#define H_MAX_SHOTS 32
+#define H_MAX_TR 4096
+static float g_picks[H_MAX_SHOTS + 1][H_MAX_TR];
+static int g_picks_calls = 0;
+void write_picks(float *Tmod, int ntr, int ishot) {
+    g_picks_calls++;
+    if (ishot < 0 || ishot > H_MAX_SHOTS || ntr > H_MAX_TR) return;
+    for (int i = 0; i < ntr; i++) g_picks[ishot][i] = Tmod[i + 1];
+}
+int h_picks(int ishot, int ntr, float *out) {
+    for (int i = 0; i < ntr; i++) out[i] = g_picks[ishot][i];
+    return g_picks_calls;
+}
+
+#ifdef RZ_COMPAT_MPI
+/* the reference's sum_grad_MPI on one rank (sum_grad_MPI.c:19-47): the
+   reduction covers NX*NY floats from index 0 of a vector filled from index
+   1, so the corner grad[NY][NX] receives an element nobody wrote -- made a
+   NaN here so that a shim which does not repeat the frame copy fails */
+void sum_grad_MPI(float **grad) {
+    float *v = (float *)malloc(((size_t)NX + 1) * (NY + 1) * sizeof(float));
+    float *r = (float *)malloc(((size_t)NX + 1) * (NY + 1) * sizeof(float));
+    int h = 1;
+    for (int i = 1; i <= NX; i++)
+        for (int j = 1; j <= NY; j++) v[h++] = grad[j][i];
+    for (size_t k = 0; k < ((size_t)NX + 1) * (NY + 1); k++) r[k] = NAN;
+    MPI_Allreduce(v, r, NX * NY, MPI_FLOAT, MPI_SUM, MPI_COMM_WORLD);
+    h = 1;
+    for (int i = 1; i <= NX; i++)
+        for (int j = 1; j <= NY; j++) grad[j][i] = r[h++];
+    free(v), free(r);
+}
+/* cp_grad_frame.c:18-49: rows 2 -> 1 -> 0 at the top, NY-2 -> NY-1 -> NY at
+   the bottom, then the same for the columns */
+void cp_grad_frame(float **A) {
+    for (int i = 1; i <= NX; i++) A[2][i] = A[3][i], A[1][i] = A[2][i];
+    for (int i = 1; i <= NX; i++) A[NY - 1][i] = A[NY - 2][i], A[NY][i] = A[NY - 1][i];
+    for (int j = 1; j <= NY; j++) A[j][2] = A[j][3], A[j][1] = A[j][2];
+    for (int j = 1; j <= NY; j++) A[j][NX - 1] = A[j][NX - 2], A[j][NX] = A[j][NX - 1];
+}
+#endif
 void precond(float **grad, int nsrc, float **srcpos, int **recpos, int ntr, int iter) {
     (void)grad, (void)nsrc, (void)srcpos, (void)recpos, (void)ntr, (void)iter;
 }
@@ -100,4 +146,23 @@ double h_grad_obj(const char *datadir, const float *S, int ns, const float *sx, 
     memcpy(grad, &g[1][1], sizeof(float) * NX * NY);
     ffree(s), ffree(tt), ffree(l), ffree(g), ffree(src), ifree(r), free(tm), free(to), free(tr);
     return L2;
+}
+
+/* forward() over shots 1..ns with SEISMO = 1: TT / Tmod receive what the
+   reference leaves there (the last shot's), the picks go to write_picks() */
+void h_forward(const float *S, int ns, const float *sx, const float *sz, int ntr, const int *rx, const int *rz,
+               float *TT, float *Tmod) {
+    float **s = fmat(NY, NX), **tt = fmat(NY, NX), **src = fmat(8, ns);
+    float *tm = (float *)calloc(ntr + 2, sizeof(float));
+    int **r = recs(ntr, rx, rz);
+    memcpy(&s[1][1], S, sizeof(float) * NX * NY);
+    for (int i = 0; i < ns; i++) src[1][i + 1] = sx[i], src[2][i + 1] = sz[i];
+    NSHOT1 = 1, NSHOT2 = ns + 1;
+    SEISMO = 1;
+    g_picks_calls = 0;
+    forward(s, tt, tm, src, ns, r, ntr);
+    SEISMO = 0;
+    memcpy(TT, &tt[1][1], sizeof(float) * NX * NY);
+    for (int i = 0; i < ntr; i++) Tmod[i] = tm[i + 1];
+    ffree(s), ffree(tt), ffree(src), ifree(r), free(tm);
 }

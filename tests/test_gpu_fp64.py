@@ -1,0 +1,185 @@
+"""GPU tests of the FP64 oracle (rz_forward_f64, rz_grad_obj_f64, RZ_MODE_FP64)
+and of the error reports it attaches to float results (rz_set_error_check).
+
+The GPU FP64 oracle is pinned to the CPU FP64 restatement (oracle/rz_oracle.c
+*_f64, the reference's algorithm in double): traveltimes bit for bit, gradients
+within 1e-12 (only the order of the misfit and stack sums differs), the exact
+adjoint within 1e-10 (the CPU visits cells in arrival order, the GPU sweeps).
+
+At the benchmark size (1700 x 350, paths of up to ~1800 cells) float32
+traveltimes carry the rounding of every update along the path: the
+reference's own float arithmetic sits 1.3-2.0e-5 (max-norm) and up to ~1.1e-5
+(relative L2) from FP64 there.  Fast mode is gated at "no further from FP64
+than the reference's own float arithmetic"; small grids meet 1e-5.
+"""
+import numpy as np
+import pytest
+
+import oracle as O
+from rajzel_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+TT_TOL = 1e-5
+GRAD_TOL = 1e-4
+
+
+@pytest.fixture(scope="module")
+def R(gpu_lib):
+    O.build(ref=False)
+    return gpu_lib
+
+
+def ctx_for(R, w, mode, vp=None, ttnorm=None, kind="reference"):
+    ctx = R.Context(0, mode)
+    ctx.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm if ttnorm is None else ttnorm, w.eps_adj)
+    ctx.set_velocity(w.vp_true if vp is None else vp)
+    ctx.set_receivers(w.recx, w.recz)
+    ctx.set_gradient(kind)
+    return ctx
+
+
+def picks(R, w, scale=0.97):
+    """Observed picks from a perturbed model (float reference mode)."""
+    ctx = ctx_for(R, w, "reference", vp=(w.vp_true * np.float32(scale)).astype(np.float32))
+    _, Tobs, _ = ctx.forward(w.srcx, w.srcz, want_tt=False)
+    return Tobs
+
+
+def rel_l2(a, b):
+    b = np.asarray(b, np.float64)
+    return float(np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b))
+
+
+def tt_rel(a, b):
+    return float(np.abs(np.asarray(a, np.float64) - b).max() / np.abs(b).max())
+
+
+@pytest.mark.parametrize("nx,ny", [(3, 3), (60, 45), (97, 70), (33, 130)])
+def test_fp64_forward_equals_cpu_fp64_oracle(R, nx, ny):
+    w = synth.small_case(nx * 7 + ny, nx, ny, nshots=3)
+    p = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    ctx = ctx_for(R, w, "reference")
+    S = synth.slowness(w.vp_true).astype(np.float64)
+    TT, Tmod = ctx.forward_f64(w.srcx, w.srcz)
+    for i in range(w.nshots):
+        t64, _ = O.eikonal_f64(p, S, w.srcx[i], w.srcz[i])
+        assert np.array_equal(TT[i], t64)
+        assert np.array_equal(Tmod[i], t64[w.recz - 1, w.recx - 1])
+
+
+def test_fp64_leung_qian_gradient_equals_cpu_fp64_oracle(R):
+    w = synth.small_case(77, 120, 80, nshots=4)
+    p = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    Tobs = picks(R, w)
+    ctx = ctx_for(R, w, "reference")
+    g, L2 = ctx.grad_obj_f64(w.srcx, w.srcz, Tobs)
+    S = synth.slowness(w.vp_true).astype(np.float64)
+    g64, L64 = O.grad_obj_f64(p, S, w.srcx.astype(np.float64), w.srcz.astype(np.float64), w.recx, w.recz,
+                              Tobs.astype(np.float64))
+    assert rel_l2(g, g64) <= 1e-12
+    assert abs(L2 - L64) <= 1e-12 * abs(L64)
+
+
+@pytest.mark.parametrize("muted", [False, True])
+def test_fp64_exact_gradient_equals_cpu_exact_oracle(R, muted):
+    w = synth.small_case(78, 90, 64, nshots=3)
+    p64 = O.Params(w.nx, w.ny, w.dh, w.time, 1e-14, w.eps_adj)
+    Tobs = picks(R, w)
+    if muted:
+        Tobs[:, ::5] = -1.0
+    ctx = ctx_for(R, w, "reference", ttnorm=1e-14, kind="exact")
+    g, L2 = ctx.grad_obj_f64(w.srcx, w.srcz, Tobs)
+    S = synth.slowness(w.vp_true).astype(np.float64)
+    g64, L64 = O.grad_exact_f64(p64, S, w.srcx, w.srcz, w.recx, w.recz, Tobs)
+    assert rel_l2(g, g64) <= 1e-10
+    assert abs(L2 - L64) <= 1e-12 * abs(L64)
+
+
+def test_fp64_mode_runs_the_float_api_in_double(R):
+    """RZ_MODE_FP64 behind rz_forward / rz_grad_obj / rz_misfit: the double
+    results rounded to float."""
+    w = synth.small_case(79, 70, 50, nshots=2)
+    Tobs = picks(R, w)
+    ctx = ctx_for(R, w, "fp64")
+    TT, Tmod, passes = ctx.forward(w.srcx, w.srcz)
+    TT64, Tmod64 = ctx.forward_f64(w.srcx, w.srcz)
+    assert np.array_equal(TT, TT64.astype(np.float32)) and np.array_equal(Tmod, Tmod64.astype(np.float32))
+    g, L2 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    g64, L64 = ctx.grad_obj_f64(w.srcx, w.srcz, Tobs)
+    assert np.array_equal(g, g64.astype(np.float32)) and L2 == L64
+    assert ctx.misfit(w.srcx, w.srcz, Tobs) == L64
+
+
+@pytest.mark.parametrize("mode", ["reference", "fast"])
+def test_error_report_matches_numpy(R, mode):
+    """rz_error_report of a checked gradient call equals the same figures
+    computed here from the returned fields and the FP64 oracle."""
+    w = synth.small_case(80, 110, 75, nshots=3)
+    Tobs = picks(R, w)
+    ctx = ctx_for(R, w, mode)
+    ctx.set_error_check(True)
+    g, L2 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    rep = ctx.error_report()
+    ref = ctx_for(R, w, "reference")
+    g64, L64 = ref.grad_obj_f64(w.srcx, w.srcz, Tobs)
+    TT64, Tmod64 = ref.forward_f64(w.srcx, w.srcz)
+    assert rep["shots"] == w.nshots
+    tt = max(tt_rel(ctx.shot_fields(i)[0], TT64[i]) for i in range(w.nshots))
+    _, Tmod, _ = ctx.forward(w.srcx, w.srcz, want_tt=False)
+    assert rep["tt_rel"] == pytest.approx(tt, rel=1e-9, abs=1e-300)
+    assert rep["tmod_rel"] == pytest.approx(tt_rel(Tmod, Tmod64), rel=1e-9, abs=1e-300)
+    assert rep["grad_rel_l2"] == pytest.approx(rel_l2(g, g64), rel=1e-6)
+    assert rep["grad_rel_max"] == pytest.approx(tt_rel(g, g64), rel=1e-9)
+    assert rep["misfit_rel"] == pytest.approx(abs(L2 - L64) / L64, rel=1e-6, abs=1e-15)
+    if mode == "fast":
+        assert rep["tt_rel"] <= TT_TOL
+
+
+def test_full_size_fast_traveltimes_against_fp64(R):
+    """1700 x 350, 8 of the benchmark's shots: fast-mode traveltimes against
+    the GPU FP64 oracle (itself pinned to the CPU FP64 oracle on one shot) are
+    no further from FP64 than the reference's own float arithmetic
+    (reference mode, bit-exact with the reference) on the same shots."""
+    w = synth.grad_1700x350(nshots=100, ntr=850)
+    idx = np.arange(0, 100, 13)[:8]
+    sx, sz = w.srcx[idx], w.srcz[idx]
+    TT = {m: ctx_for(R, w, m, vp=w.vp_start).forward(sx, sz)[0] for m in ("fast", "reference")}
+    TT64, _ = ctx_for(R, w, "fast", vp=w.vp_start).forward_f64(sx, sz)
+    for i in range(len(idx)):
+        e_fast, e_ref = tt_rel(TT["fast"][i], TT64[i]), tt_rel(TT["reference"][i], TT64[i])
+        assert e_fast <= e_ref * (1 + 1e-3) + 1e-7, (i, e_fast, e_ref)
+        assert e_fast <= 2.5e-5 and rel_l2(TT["fast"][i], TT64[i]) <= 1.5e-5
+    p = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    t64, _ = O.eikonal_f64(p, synth.slowness(w.vp_start).astype(np.float64), sx[0], sz[0])
+    assert np.array_equal(TT64[0], t64)
+
+
+def test_small_grid_fast_traveltimes_within_1e5_of_fp64(R):
+    w = synth.small_case(31, 200, 150, nshots=3)
+    ctx = ctx_for(R, w, "fast")
+    TT, _, _ = ctx.forward(w.srcx, w.srcz)
+    TT64, _ = ctx.forward_f64(w.srcx, w.srcz)
+    assert max(tt_rel(TT[i], TT64[i]) for i in range(3)) <= TT_TOL
+
+
+def test_full_size_error_check_gates(R):
+    """The benchmark workload's 100 shots through rz_set_error_check: fast
+    traveltimes no further from FP64 than the reference's own float
+    arithmetic; Leung-Qian gradient no further than twice the reference's
+    plus 1e-4."""
+    w = synth.grad_1700x350(nshots=100, ntr=850)
+    tobs_ctx = ctx_for(R, w, "fast")
+    _, Tobs, _ = tobs_ctx.forward(w.srcx, w.srcz, want_tt=False)
+    reps = {}
+    for mode, kind in (("reference", "reference"), ("fast", "reference"), ("fast", "exact")):
+        ctx = ctx_for(R, w, mode, vp=w.vp_start, kind=kind)
+        ctx.set_error_check(True)
+        ctx.grad_obj(w.srcx, w.srcz, Tobs)
+        reps[mode, kind] = ctx.error_report()
+    fast, ref, ex = reps["fast", "reference"], reps["reference", "reference"], reps["fast", "exact"]
+    assert fast["shots"] == 100 and ref["shots"] == 100
+    assert fast["tt_rel"] <= ref["tt_rel"] * (1 + 1e-3) + 1e-7 and ex["tt_rel"] == fast["tt_rel"]
+    assert fast["grad_rel_l2"] <= 2 * ref["grad_rel_l2"] + GRAD_TOL
+    # the exact gradient of the float misfit: its residuals carry the float
+    # traveltimes' path error (misfit 5.6e-4 from FP64), ~3e-3 here
+    assert ex["grad_rel_l2"] <= 5e-3

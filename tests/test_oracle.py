@@ -186,3 +186,71 @@ def test_exact_adjoint_oracle_matches_finite_differences(oracle_mod, muted):
         jm = O.misfit_f64(p, S - eps * d, w.srcx, w.srcz, w.recx, w.recz, Tobs)
         fd = (jp - jm) / (2 * eps)
         assert abs(fd - (g_s * d).sum()) <= 1e-6 * abs(fd)
+
+
+# ---------------------------------------------------------------------------
+# FATT and preconditioning: the restatement against the reference's own
+# compiled fatt(), LBFGS.c, wolfels.c, check_descent.c, precond.c,
+# gauss_filt.c and taper_grad.c
+# ---------------------------------------------------------------------------
+def _fatt_case(O, seed, nx, ny, ns, pert):
+    """Picks from the true model; start = the true model with a smooth slow
+    anomaly (the reference's l-BFGS makes progress on these)."""
+    w = synth.small_case(seed, nx, ny, nshots=ns)
+    p = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    S_true = synth.slowness(w.vp_true)
+    Tobs = np.stack([O.calc_fa(p, O.eikonal(p, S_true, w.srcx[i], w.srcz[i])[0], w.recx, w.recz) for i in range(ns)])
+    yy, xx = np.mgrid[0:ny, 0:nx]
+    bump = np.exp(-(((xx - nx / 2) / (nx / 5)) ** 2 + ((yy - ny / 2) / (ny / 5)) ** 2))
+    vp0 = (w.vp_true * (1 - pert * bump)).astype(np.float32)
+    return w, p, Tobs, vp0
+
+
+FATT_OPTS = dict(itermax=6, nlbfgs=3, stepmax=8, eps_scale=0.01, c1=1e-4, c2=0.9, scalefac=2.0, vp_lo=1000.0,
+                 vp_hi=6000.0, pro=0.0, spatfilter=0, filt_size_grad=0, filt_size_grad1=0, taper_hor=0, gradt1=1,
+                 gradt2=1, exp_taper_grad_hor=0.0, recursion=0)
+
+
+@pytest.mark.parametrize("seed,nx,ny,ns,pert,taper", [(56, 60, 40, 4, 0.08, 0), (57, 80, 50, 5, 0.1, 0),
+                                                      (57, 80, 50, 5, 0.1, 1)])
+def test_fatt_restatement_equals_reference_fatt(oracle_mod, seed, nx, ny, ns, pert, taper):
+    """One FATT stage (l-BFGS in slot order, weak-Wolfe line search, model
+    limits, the horizontal taper) by the restatement in the reference's own
+    precision equals the reference's compiled fatt() bit for bit: the misfit
+    of every gradient evaluation in call order and the final model."""
+    O = oracle_mod
+    if not O.ref_available():
+        pytest.skip("reference sources not present on this machine")
+    from oracle import fatt as F
+    w, p, Tobs, vp0 = _fatt_case(O, seed, nx, ny, ns, pert)
+    o = dict(FATT_OPTS, taper_hor=taper, gradt1=3, gradt2=8, exp_taper_grad_hor=0.5)
+    vr, mr, steps, evr = O.Ref(p).fatt(vp0, w.srcx, w.srcz, w.recx, w.recz, Tobs, o)
+    trace = []
+    vq, mq, it, ev = F.fatt(p, vp0, w.srcx, w.srcz, w.recx, w.recz, Tobs, o, precision="reference", trace=trace)
+    assert len(mr) >= 3 and it == len(mr) and ev == len(evr)
+    assert np.array_equal(np.array(trace), evr)  # exact misfits of every evaluation
+    assert np.allclose(mq, mr, rtol=5e-7, atol=0)  # fatt.c's log prints %e (7 digits)
+    assert np.array_equal(vq, vr)
+
+
+@pytest.mark.parametrize("fs,fs1,taper", [(6, 4, 0), (7, 5, 1), (12, 9, 0), (0, 0, 1)])
+def test_precond_restatement_matches_reference(oracle_mod, fs, fs1, taper):
+    """precond() with SPATFILTER 4 (gauss_filt.c, even sizes rounded up) and
+    the horizontal taper (taper_grad.c sws 2): the restatement's Gaussian
+    accumulates in double, the reference's in float (1e-6 relative); the
+    taper alone is bit-exact."""
+    O = oracle_mod
+    if not O.ref_available():
+        pytest.skip("reference sources not present on this machine")
+    from oracle import fatt as F
+    w = synth.small_case(61, 70, 45, nshots=1)
+    p = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    g = np.random.default_rng(fs + fs1).standard_normal((w.ny, w.nx)).astype(np.float32)
+    o = dict(FATT_OPTS, spatfilter=4 if fs else 0, filt_size_grad=fs, filt_size_grad1=fs1, taper_hor=taper, gradt1=3,
+             gradt2=8, exp_taper_grad_hor=1.0)
+    a = O.Ref(p).precond(g, o)
+    b = F.precond(g, o, p.dh)
+    if fs == 0:
+        assert np.array_equal(a, b)
+    else:
+        assert np.abs(a - b).max() <= 1e-6 * np.abs(a).max()

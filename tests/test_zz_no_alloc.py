@@ -1,6 +1,6 @@
 """The allocation-free forward entry point (rz_eikonal_noalloc).
 
-Callers that cannot allocate GPU memory (graph capture, fixed pools, hosts
+Callers that cannot allocate GPU memory (fixed pools or memory budgets, hosts
 without an allocator) get the same traveltimes as rz_eikonal() from a static
 device array.  This file sorts last so that a run stopping at the first
 failure has run every other test first; it also passes alone in a fresh
@@ -60,3 +60,38 @@ def test_noalloc_rejects_oversized_and_bad_input(gpu_lib):
     assert f(C.byref(big), C.c_void_p(16), 100.0, 20.0, C.c_void_p(16), C.c_void_p(16), None) == gpu_lib.RZ_EUNSUPPORTED
     ok = _Grid(100, 50, 10.0, 40.0, 1e-6, 1e-9, 100)
     assert f(C.byref(ok), C.c_void_p(16), -500.0, 20.0, C.c_void_p(16), C.c_void_p(16), None) == gpu_lib.RZ_EINVAL
+
+
+def test_noalloc_reports_invalid_slowness_and_no_convergence(gpu_lib):
+    """An invalid slowness sets status bit 5 (RZ_EINVAL, no solve), a pass
+    limit of 1 the forward no-convergence bit (RZ_ENOCONV); the next call
+    with good input is exact again."""
+    import torch
+    R = gpu_lib
+    lib = R.load_library()
+    f = lib.rz_eikonal_noalloc
+    f.argtypes = [C.POINTER(_Grid), C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
+    f.restype = C.c_int
+    w = synth.small_case(4343, 90, 70, nshots=1)
+    S = synth.slowness(w.vp_true)
+    bad = S.copy()
+    bad[33, 44] = 0.0
+    grid1 = _Grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj, 1)
+    grid = _Grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj, 10000)
+    TT_d = torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda")
+    info_d = torch.zeros(2, dtype=torch.int32, device="cuda")
+    for g, model, want in ((grid1, bad, R.RZ_EINVAL), (grid1, S, R.RZ_ENOCONV)):
+        S_d = torch.from_numpy(model).cuda()
+        assert f(C.byref(g), S_d.data_ptr(), float(w.srcx[0]), float(w.srcz[0]), TT_d.data_ptr(),
+                 info_d.data_ptr(), None) == R.RZ_OK
+        torch.cuda.synchronize()
+        assert lib.rz_status_code(int(info_d.cpu()[1])) == want
+    ctx = R.Context(0, "reference")
+    ctx.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    ctx.set_slowness(S)
+    TT_ref, _, passes = ctx.eikonal(w.srcx[0], w.srcz[0])
+    S_d = torch.from_numpy(S).cuda()
+    assert f(C.byref(grid), S_d.data_ptr(), float(w.srcx[0]), float(w.srcz[0]), TT_d.data_ptr(),
+             info_d.data_ptr(), None) == R.RZ_OK
+    torch.cuda.synchronize()
+    assert np.array_equal(TT_d.cpu().numpy(), TT_ref) and info_d.cpu().tolist() == [passes, 0]
