@@ -110,16 +110,24 @@ int rz_set_velocity(rz_context *ctx, const float *vp, int flags);
 int rz_set_receivers(rz_context *ctx, int ntr, const int *recx, const int *recz);
 
 /* Autotuner (no counterpart in the reference): runs rz_grad_obj on the
-   caller's batch once per candidate band width -- warps per CTA, i.e. strips
-   swept together, the balanced width for the fewest bands of <= 16 strips
-   and for one and two more bands -- times each with CUDA events, and keeps
-   the fastest for later rz_grad_obj calls with the same number of shots,
-   mode and gradient kind.  The width changes no result.  Arguments as
-   rz_grad_obj (grad receives the gradient); best_warps / best_ms (may be
-   NULL) the choice; cand_warps / cand_ms [*ncand] (may be NULL) every
-   candidate, *ncand set to their number. */
+   caller's batch once per candidate launch shape, times each with CUDA
+   events, and keeps the fastest for later rz_grad_obj calls with the same
+   number of shots, mode and gradient kind.  A shape is
+     - the band width: warps that sweep, i.e. strips swept together -- the
+       balanced width for the fewest bands of <= 16 strips and for one and
+       two more bands;
+     - the fixpoint checks' task height: at most 32, 64 or 128 rows of 128
+       columns per warp task;
+     - the CTA width: as many warps as fit at the same occupancy (the spare
+       ones share the cell-parallel phases), or the sweeping warps alone.
+   No shape changes a result.  Arguments as rz_grad_obj (grad receives the
+   gradient); best_warps / best_ms (may be NULL) the chosen band width and
+   its time; cand_warps / cand_ms [*ncand] (may be NULL) every band width
+   with its fastest shape's time, *ncand set to their number.
+   rz_tuned_shape returns the whole chosen shape. */
 int rz_autotune(rz_context *ctx, int nshots, const float *srcx, const float *srcz, const float *Tobs, float *grad,
                 int flags, int *best_warps, double *best_ms, int *cand_warps, double *cand_ms, int *ncand);
+int rz_tuned_shape(rz_context *ctx, int nshots, int *warps, int *cta_warps, int *check_rows);
 
 /* CUDA graphs (default on): rz_grad_obj captures its device sequence
    (per-shot resets, shot-kernel launches, stacks, frame copy, misfit sum)
@@ -268,6 +276,22 @@ int rz_set_error_check(rz_context *ctx, int enable);
 /* The error of the last checked call's results against the FP64 oracle. */
 int rz_error_report(rz_context *ctx, rz_error *err);
 
+/* Traveltime refinement (not in the reference; default off).  Float32
+   traveltimes carry the rounding of every update along their path: on a
+   1700 x 350 grid the reference's own float arithmetic ends up to 2e-5
+   (relative) from the FP64 fixpoint, and residuals of a few hundredths of a
+   second inherit that.  With refinement on, every shot's converged field T
+   is corrected by one linear solve, delta = r + W delta, with r the residual
+   of the discrete equations evaluated in float-float and W the Godunov
+   weights (the sweeps of the exact adjoint, in the forward orders), after
+   which T + delta agrees with the FP64 fixpoint to float precision.  All
+   results use the refined field: traveltimes and picks (rounded to float),
+   residuals and misfit (in double), the Leung-Qian adjoint's inputs, and
+   the exact gradient (weights of the refined field).  Costs one more linear
+   solve per shot; in reference mode the results are then more accurate than
+   the reference's rather than bit-identical to them. */
+int rz_set_refine(rz_context *ctx, int enable);
+
 /* Test hook for the failure path (no counterpart in the reference, which
    aborts through err()/MPI_Abort, util.c:7-17).  Every device wait for
    another warp is bounded: after spin_limit polls (0 = the default budget of
@@ -314,9 +338,10 @@ int rz_shot_fields(rz_context *ctx, int shot, float *TT, float *lam, float *Tres
 int rz_kernel_stats(rz_context *ctx, long long *launches, double *shot_kernel_ms, int *shot_kernel_calls);
 
 /* Diagnostics: device time stamps (ns, %globaltimer) of shot `shot` in the
-   last batch: [0] start, [1] forward converged, [2] residuals done,
-   [3] adjoint prepared, [4] adjoint converged, [5] first forward sweep done,
-   [6] first adjoint sweep done, [7] unused.  stamps has 8 entries. */
+   last batch: [0] start, [1] forward converged (and refined), [2] residuals
+   done, [3] adjoint prepared, [4] adjoint converged, [5] first forward sweep
+   done, [6] first adjoint sweep done, [7] refinement started (0 without
+   refinement).  stamps has 8 entries. */
 int rz_shot_timeline(rz_context *ctx, int shot, unsigned long long *stamps);
 
 /* eikonal(): one source -> TT [ny][nx] and Tmod [ntr] (eikonal.c:10-76). */

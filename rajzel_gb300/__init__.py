@@ -103,6 +103,10 @@ def load_library(path: str = LIB_PATH):
     lib.rz_status_code.restype = C.c_int
     lib.rz_batch_status.argtypes = [vp, vp]
     lib.rz_batch_status.restype = C.c_int
+    lib.rz_tuned_shape.argtypes = [vp, C.c_int, vp, vp, vp]
+    lib.rz_tuned_shape.restype = C.c_int
+    lib.rz_set_refine.argtypes = [vp, C.c_int]
+    lib.rz_set_refine.restype = C.c_int
     lib.rz_set_wait_test.argtypes = [vp, C.c_uint, C.c_int]
     lib.rz_set_wait_test.restype = C.c_int
     lib.rz_forward_f64.argtypes = [vp, C.c_int, vp, vp, vp, vp, C.c_int]
@@ -293,7 +297,10 @@ class Context:
         cw, cm, nc = (C.c_int * 8)(), (C.c_double * 8)(), C.c_int(8)
         self._check(self.lib.rz_autotune(self.h, n, _ptr(srcx), _ptr(srcz), _ptr(Tobs), _ptr(grad), 0, C.byref(best),
                                          C.byref(ms), cw, cm, C.byref(nc)), "rz_autotune")
-        return {"warps": best.value, "ms": ms.value, "candidates": {cw[i]: cm[i] for i in range(min(nc.value, 8))}}
+        w, cta, rows = C.c_int(0), C.c_int(0), C.c_int(0)
+        self._check(self.lib.rz_tuned_shape(self.h, n, C.byref(w), C.byref(cta), C.byref(rows)), "rz_tuned_shape")
+        return {"warps": best.value, "ms": ms.value, "candidates": {cw[i]: cm[i] for i in range(min(nc.value, 8))},
+                "shape": {"sweeping_warps": w.value, "cta_warps": cta.value or "widest", "check_rows": rows.value}}
 
     def set_graphs(self, enable: bool):
         """Capture rz_grad_obj's device sequence as a CUDA graph and replay it (default on)."""
@@ -393,6 +400,10 @@ class Context:
         e = ErrorReport()
         self._check(self.lib.rz_error_report(self.h, C.byref(e)), "rz_error_report")
         return e.as_dict()
+
+    def set_refine(self, enable: bool):
+        """Refine converged traveltimes to the FP64 fixpoint (rz_set_refine)."""
+        self._check(self.lib.rz_set_refine(self.h, int(bool(enable))), "rz_set_refine")
 
     def set_wait_test(self, spin_limit: int = 0, withhold_handoff: bool = False):
         """Test hook of the timeout path (rz_set_wait_test)."""

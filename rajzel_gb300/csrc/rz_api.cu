@@ -99,14 +99,21 @@ struct rz_context {
     // default; rz_autotune records the fastest per (shots, mode, gradient kind)
     int warps = 0;
     bool tuning = false;
-    std::map<std::array<int, 3>, int> tuned;
+    // the launch shape: warps that sweep (warps), CTA width (cta_warps, 0 =
+    // as wide as fits), most rows per fixpoint-check task (check_rows, 0 =
+    // default); rz_autotune records the fastest per (shots, mode, gradient kind)
+    int cta_warps = 0, check_rows = 0;
+    struct Shape {
+        int warps, cta_warps, check_rows;
+    };
+    std::map<std::array<int, 3>, Shape> tuned;
 
     // CUDA graph of the rz_grad_obj sequence, replayed while its key is unchanged
     bool use_graphs = true;
     bool capturing = false;
     struct GraphKey {
         ShotParams P0;  // parameters of the first chunk (pointers, constants)
-        int nshots, chunk, mode, kind, cap_f, flags_dev, warps;
+        int nshots, chunk, mode, kind, cap_f, flags_dev, warps, cta_warps;
         const void *gdst, *grad64, *cube, *S, *L2;
     } gkey;
     cudaGraph_t graph = nullptr;          // kept: its nodes name the exec's event records
@@ -142,6 +149,8 @@ struct rz_context {
     // default) and the withheld hand-off of the timeout test (rz_set_wait_test)
     unsigned spin = 0;
     int withhold = 0;
+    // traveltime refinement to the FP64 fixpoint (rz_set_refine)
+    bool refine = false;
     // errors of float results against the FP64 oracle (rz_set_error_check)
     bool err_check = false;
     bool err_valid = false;
@@ -262,12 +271,12 @@ static void free_batch(rz_context *c) {
 static size_t slot_bytes(const rz_context *c) {
     const size_t fs = (size_t)c->g.ny * c->nxp, ss = (size_t)c->nstrips * c->qn * 32,
                  es = (size_t)c->nstrips * edge_row(c->nxp);
-    const size_t extra = c->grad_kind == RZ_GRADIENT_EXACT ? 4 * ss : 0;
+    const size_t extra = (c->grad_kind == RZ_GRADIENT_EXACT || c->refine) ? 4 * ss : 0;
     return 4 * (3 * fs + 2 * ss + 2 * es + extra) + (size_t)c->nstrips * 4 * (c->nxb + 1);  // + change votes
 }
 
 static int ensure_fields(rz_context *c, int n) {
-    const bool exact = c->grad_kind == RZ_GRADIENT_EXACT;
+    const bool exact = c->grad_kind == RZ_GRADIENT_EXACT || c->refine;  // weight streams
     if (n <= c->cap_f && (!exact || c->fields_exact)) return RZ_OK;
     if (n < c->cap_f) n = c->cap_f;
     free_fields(c);
@@ -456,6 +465,8 @@ static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     P.chg_stride = (size_t)c->nstrips * 4 * (c->nxb + 1);
     P.spin = c->spin;
     P.withhold = c->withhold;
+    P.refine = c->refine ? 1 : 0;
+    P.check_rows = c->check_rows;
 }
 
 static int status_to_code(int bits) {
@@ -517,7 +528,7 @@ static int run_batch(rz_context *c, int first, int n, bool adjoint, bool residua
     CK(cudaEventCreate(&e1));
     const unsigned evf = c->capturing ? cudaEventRecordExternal : cudaEventRecordDefault;
     CK(cudaEventRecordWithFlags(e0, c->st, evf));
-    CK(launch_shot_kernel(P, c->mode, c->maps, c->st, c->warps));
+    CK(launch_shot_kernel(P, c->mode, c->maps, c->st, c->warps, c->cta_warps));
     CK(cudaEventRecordWithFlags(e1, c->st, evf));
     c->shot_events.emplace_back(e0, e1);
     c->launches += 1;
@@ -574,7 +585,7 @@ static int stack_chunk(rz_context *c, int first, int m, float *gdst, bool whole 
     bool fin = false;
     if (c->grad_kind == RZ_GRADIENT_EXACT) {
         CK(launch_stack_exact(c->dT, c->dL, fs, m, c->dSrcH + first, c->dSrcK + first, c->dS, c->g.nx, c->g.ny,
-                              c->nxp, c->g.dh, gdst, c->dGrad64, first > 0, c->st));
+                              c->nxp, c->g.dh, gdst, c->dGrad64, first > 0, c->st, c->refine ? c->dTold : nullptr));
     } else {
         fin = whole && first == 0 && c->g.nx >= 5 && c->g.ny >= 5 && c->dL2;
         CK(launch_stack(c->dL, fs, m, c->dCube, c->dS, c->g.nx, c->g.ny, c->nxp, c->mode, gdst, c->g.nx,
@@ -1152,7 +1163,8 @@ static int grad_obj_impl(rz_context *c, int nshots, const float *srcx, const flo
     if ((r = ensure_div(c))) return r;
     if (!c->tuning) {
         auto it = c->tuned.find({nshots, c->mode, c->grad_kind});
-        c->warps = it != c->tuned.end() ? it->second : 0;
+        const rz_context::Shape sh = it != c->tuned.end() ? it->second : rz_context::Shape{0, 0, 0};
+        c->warps = sh.warps, c->cta_warps = sh.cta_warps, c->check_rows = sh.check_rows;
     }
     // the device sequence: chunks in shot order, each stack continuing the
     // previous chunk's sums (the result does not depend on the chunk size)
@@ -1182,7 +1194,7 @@ static int grad_obj_impl(rz_context *c, int nshots, const float *srcx, const flo
         fill_params(c, key.P0, 0, nshots < chunk ? nshots : chunk);
         key.nshots = nshots, key.chunk = chunk, key.mode = c->mode, key.kind = c->grad_kind, key.cap_f = c->cap_f;
         key.flags_dev = have_dev(flags), key.gdst = gdst, key.grad64 = c->dGrad64, key.cube = c->dCube;
-        key.S = c->dS, key.L2 = c->dL2, key.warps = c->warps;
+        key.S = c->dS, key.L2 = c->dL2, key.warps = c->warps, key.cta_warps = c->cta_warps;
         if (!c->gexec || memcmp(&key, &c->gkey, sizeof key) != 0) {
             drop_graph(c);
             const size_t ev0 = c->shot_events.size();
@@ -1413,6 +1425,12 @@ int rz_set_wait_test(rz_context *c, unsigned spin_limit, int withhold_handoff) {
     return RZ_OK;
 }
 
+int rz_set_refine(rz_context *c, int enable) {
+    if (!c) return RZ_EINVAL;
+    c->refine = enable != 0;
+    return RZ_OK;
+}
+
 int rz_set_error_check(rz_context *c, int enable) {
     if (!c) return RZ_EINVAL;
     c->err_check = enable != 0;
@@ -1556,21 +1574,27 @@ int rz_autotune(rz_context *c, int nshots, const float *srcx, const float *srcz,
     if (c->mode == RZ_MODE_FP64) return fail(c, RZ_EUNSUPPORTED, "the autotuner times the float kernels only");
     if (nshots < 1 || !grad) return fail(c, RZ_EINVAL, "bad arguments");
     cudaSetDevice(c->device);
-    // candidates: the balanced width for the fewest bands and one or two more bands
+    // band widths: the balanced width for the fewest bands and one or two more bands
     const int ns = c->nstrips, nb0 = (ns + kMaxWarps - 1) / kMaxWarps;
-    std::vector<int> cands;
+    std::vector<int> widths;
     for (int nb = nb0; nb <= nb0 + 2 && nb <= ns; ++nb) {
         const int W = (ns + nb - 1) / nb;
-        if (std::find(cands.begin(), cands.end(), W) == cands.end()) cands.push_back(W);
+        if (std::find(widths.begin(), widths.end(), W) == widths.end()) widths.push_back(W);
     }
+    // shapes: band width x fixpoint-check task height x CTA width (as wide as
+    // fits, or the sweeping warps alone)
+    std::vector<rz_context::Shape> shapes;
+    for (int W : widths)
+        for (int rows : {32, 64, 128})
+            for (int cta : {0, W}) shapes.push_back({W, cta, rows});
     const bool graphs = c->use_graphs;
     c->use_graphs = false;
     c->tuning = true;
     double L2 = 0.0;
-    std::vector<double> ms(cands.size(), 0.0);
+    std::vector<double> ms(shapes.size(), 0.0);
     int best = 0;
-    for (size_t i = 0; i < cands.size() && !r; ++i) {
-        c->warps = cands[i];
+    for (size_t i = 0; i < shapes.size() && !r; ++i) {
+        c->warps = shapes[i].warps, c->cta_warps = shapes[i].cta_warps, c->check_rows = shapes[i].check_rows;
         cudaEvent_t e0, e1;
         r = rz_grad_obj(c, nshots, srcx, srcz, Tobs, grad, &L2, flags);  // warm
         if (!r && cudaEventCreate(&e0) == cudaSuccess && cudaEventCreate(&e1) == cudaSuccess) {
@@ -1587,19 +1611,33 @@ int rz_autotune(rz_context *c, int nshots, const float *srcx, const float *srcz,
     }
     c->tuning = false;
     c->use_graphs = graphs;
-    c->warps = 0;
+    c->warps = 0, c->cta_warps = 0, c->check_rows = 0;
     if (r) return r;
-    c->tuned[{nshots, c->mode, c->grad_kind}] = cands[best];
-    if (best_warps) *best_warps = cands[best];
+    c->tuned[{nshots, c->mode, c->grad_kind}] = shapes[best];
+    if (best_warps) *best_warps = shapes[best].warps;
     if (best_ms) *best_ms = ms[best];
     if (ncand) {
+        // per band width, its fastest shape's time
         const int cap = *ncand;
-        for (int i = 0; i < (int)cands.size() && i < cap; ++i) {
-            if (cand_warps) cand_warps[i] = cands[i];
-            if (cand_ms) cand_ms[i] = ms[i];
+        for (int i = 0; i < (int)widths.size() && i < cap; ++i) {
+            double t = 0.0;
+            for (size_t k = 0; k < shapes.size(); ++k)
+                if (shapes[k].warps == widths[i] && (t == 0.0 || ms[k] < t)) t = ms[k];
+            if (cand_warps) cand_warps[i] = widths[i];
+            if (cand_ms) cand_ms[i] = t;
         }
-        *ncand = (int)cands.size();
+        *ncand = (int)widths.size();
     }
+    return RZ_OK;
+}
+
+int rz_tuned_shape(rz_context *c, int nshots, int *warps, int *cta_warps, int *check_rows) {
+    if (!c) return RZ_EINVAL;
+    auto it = c->tuned.find({nshots, c->mode, c->grad_kind});
+    if (it == c->tuned.end()) return fail(c, RZ_ESTATE, "no tuned shape for %d shots in this mode", nshots);
+    if (warps) *warps = it->second.warps;
+    if (cta_warps) *cta_warps = it->second.cta_warps;
+    if (check_rows) *check_rows = it->second.check_rows;
     return RZ_OK;
 }
 

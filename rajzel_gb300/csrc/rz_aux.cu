@@ -138,9 +138,10 @@ cudaError_t launch_stack(const float *L, size_t fstride, int nshots, const doubl
 // Exact-adjoint gradient (not in the reference): dJ/dVp of every cell,
 //   -S^2 * sum over shots of mu * dG/dS,
 // dG/dS from the shot's converged traveltimes (exact_coef), summed in double.
+// With Tlo (refined traveltimes) dG/dS is that of T + Tlo.
 __global__ void stack_exact_kernel(const float *T, const float *L, size_t fstride, int nshots, const int *src_h,
                                    const int *src_k, const float *S, int nx, int ny, int nxp, float dh, float *grad,
-                                   double *grad64, bool accumulate) {
+                                   double *grad64, bool accumulate, const float *Tlo) {
     const long c = (long)blockIdx.x * blockDim.x + threadIdx.x;
     if (c >= (long)nx * ny) return;
     const int k = (int)(c / nx), h = (int)(c - (long)k * nx);
@@ -149,7 +150,7 @@ __global__ void stack_exact_kernel(const float *T, const float *L, size_t fstrid
     double acc = 0.0;
     for (int z = 0; z < nshots; ++z) {
         const ExactCoef cf = exact_coef(T + (size_t)z * fstride, nxp, nx, ny, h, k, s, dh,
-                                        h == src_h[z] && k == src_k[z]);
+                                        h == src_h[z] && k == src_k[z], Tlo ? Tlo + (size_t)z * fstride : nullptr);
         acc += (double)__ldg(L + (size_t)z * fstride + o) * (double)cf.gs;
     }
     acc *= -((double)s * (double)s);
@@ -160,10 +161,10 @@ __global__ void stack_exact_kernel(const float *T, const float *L, size_t fstrid
 
 cudaError_t launch_stack_exact(const float *T, const float *L, size_t fstride, int nshots, const int *src_h,
                                const int *src_k, const float *S, int nx, int ny, int nxp, float dh, float *grad,
-                               double *grad64, bool accumulate, cudaStream_t st) {
+                               double *grad64, bool accumulate, cudaStream_t st, const float *Tlo) {
     const long n = (long)nx * ny;
     stack_exact_kernel<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(T, L, fstride, nshots, src_h, src_k, S, nx, ny,
-                                                                   nxp, dh, grad, grad64, accumulate);
+                                                                   nxp, dh, grad, grad64, accumulate, Tlo);
     return cudaGetLastError();
 }
 

@@ -386,18 +386,44 @@ struct ExactCoef {
     float wx, wz, gs;
 };
 
-RZ_DEV ExactCoef exact_coef(const float *T, int nxp, int nx, int ny, int h, int k, float s, float dh, bool source) {
+// The values one cell's linearisation reads: its traveltime and those of its
+// four neighbours (3e38 for a missing one) and, for refined traveltimes, the
+// neighbours' low parts.  Loading them apart from the arithmetic lets a
+// caller issue the loads of several cells before any of them is used.
+struct CellNb {
+    float tw, te, tn, ts, tc;
+    float lw, le, ln, ls;
+};
+RZ_DEV CellNb load_cell_nb(const float *T, const float *Tlo, int nxp, int nx, int ny, int h, int k) {
+    const float big = 3.0e38f;
+    const size_t o = (size_t)k * nxp + h;
+    const float *p = T + o;
+    CellNb c;
+    c.tw = h > 0 ? __ldcg(p - 1) : big, c.te = h < nx - 1 ? __ldcg(p + 1) : big;
+    c.tn = k > 0 ? __ldcg(p - nxp) : big, c.ts = k < ny - 1 ? __ldcg(p + nxp) : big;
+    c.tc = __ldcg(p);
+    c.lw = c.le = c.ln = c.ls = 0.f;
+    if (Tlo) {
+        const float *q = Tlo + o;
+        c.lw = h > 0 ? __ldcg(q - 1) : 0.f, c.le = h < nx - 1 ? __ldcg(q + 1) : 0.f;
+        c.ln = k > 0 ? __ldcg(q - nxp) : 0.f, c.ls = k < ny - 1 ? __ldcg(q + nxp) : 0.f;
+    }
+    return c;
+}
+
+// With refined traveltimes (T + Tlo, see the traveltime refinement in
+// rz_shot.cu) the neighbours are chosen by their rounded sums and d carries
+// the low parts, so the weights are those of the refined field to float
+// precision; the low parts are 0 otherwise.
+RZ_DEV ExactCoef exact_coef_nb(const CellNb &n, float s, float dh, bool source) {
     ExactCoef c{0.f, 0.f, 0.f};
     if (source) return c;
-    const float big = 3.0e38f;
-    const float *p = T + (size_t)k * nxp + h;
-    const float tw = h > 0 ? __ldcg(p - 1) : big, te = h < nx - 1 ? __ldcg(p + 1) : big;
-    const float tn = k > 0 ? __ldcg(p - nxp) : big, ts = k < ny - 1 ? __ldcg(p + nxp) : big;
-    const bool west = tw <= te, north = tn <= ts;
-    const float a = west ? tw : te, b = north ? tn : ts;
-    const float sh = s * dh, d = a - b;
+    const bool west = n.tw <= n.te, north = n.tn <= n.ts;
+    const float a = west ? n.tw : n.te, b = north ? n.tn : n.ts;
+    const float d = (a - b) + ((west ? n.lw : n.le) - (north ? n.ln : n.ls));
+    const float sh = s * dh;
     if (fabsf(d) >= sh) {
-        if (a <= b) c.wx = west ? -1.f : 1.f;
+        if (d <= 0.f) c.wx = west ? -1.f : 1.f;
         else c.wz = north ? -1.f : 1.f;
         c.gs = dh;
         return c;
@@ -409,6 +435,57 @@ RZ_DEV ExactCoef exact_coef(const float *T, int nxp, int nx, int ny, int h, int 
     c.wz = north ? -wb : wb;
     c.gs = s * dh * dh / r;
     return c;
+}
+
+RZ_DEV ExactCoef exact_coef(const float *T, int nxp, int nx, int ny, int h, int k, float s, float dh, bool source,
+                            const float *Tlo = nullptr) {
+    if (source) return ExactCoef{0.f, 0.f, 0.f};
+    return exact_coef_nb(load_cell_nb(T, Tlo, nxp, nx, ny, h, k), s, dh, false);
+}
+
+// Traveltime refinement (not in the reference).  A converged float field
+// T32 satisfies T32_c = fl(G(a_c, b_c)) at every cell but the source, G the
+// Godunov update and a_c / b_c the smaller x / z neighbour; the FP64 fixpoint
+// T* = T32 + delta solves, to first order, delta_c = r_c + w_a delta_a +
+// w_b delta_b with r_c = G(a_c, b_c) - T32_c and the weights of exact_coef.
+// godunov_residual returns r_c with G evaluated in float-float (error about
+// 2^-42 of the traveltime), a / b the smaller existing neighbours.
+RZ_DEV float godunov_residual(float a, float b, float s, float dh, float t) {
+    const float sh = __fmul_rn(s, dh);
+    const float shl = __fmaf_rn(s, dh, -sh);  // sh + shl = s*dh exactly
+    const float d = __fsub_rn(a, b);
+    if (fabsf(d) >= sh) {
+        // min(a, b) + s*dh - t; min - t is exact (t lies within a factor two of min, or min is 0)
+        return __fadd_rn(__fadd_rn(__fsub_rn(fminf(a, b), t), sh), shl);
+    }
+    // (a + b + sqrt(2 (s dh)^2 - d^2)) / 2 - t in float-float
+    const float sum = __fadd_rn(a, b);
+    const float sbb = __fsub_rn(sum, a);
+    const float se = __fadd_rn(__fsub_rn(a, __fsub_rn(sum, sbb)), __fsub_rn(b, sbb));  // a + b = sum + se
+    const float p2 = __fmul_rn(sh, sh);
+    const float p2l = __fmaf_rn(sh, sh, -p2);
+    const float cross = __fmaf_rn(__fmul_rn(2.0f, sh), shl, p2l);
+    const float d2 = __fmul_rn(d, d);
+    const float d2l = __fmaf_rn(d, d, -d2);
+    const float P = __fmul_rn(2.0f, p2);
+    const float Dh = __fsub_rn(P, d2);
+    const float Dl = __fadd_rn(__fsub_rn(__fsub_rn(P, Dh), d2), __fsub_rn(__fmul_rn(2.0f, cross), d2l));
+    const float rs = rsqrtf(Dh);
+    const float r0 = __fmul_rn(Dh, rs);
+    const float rl = __fmul_rn(__fadd_rn(__fmaf_rn(-r0, r0, Dh), Dl), __fmul_rn(0.5f, rs));
+    const float uh = __fadd_rn(sum, r0);
+    const float ubb = __fsub_rn(uh, sum);
+    const float ue = __fadd_rn(__fsub_rn(sum, __fsub_rn(uh, ubb)), __fsub_rn(r0, ubb));
+    const float ul = __fadd_rn(__fadd_rn(ue, rl), se);
+    // uh - 2t is exact (uh lies within a factor two of 2t)
+    return __fmul_rn(0.5f, __fadd_rn(__fsub_rn(uh, __fmul_rn(2.0f, t)), ul));
+}
+
+// r_c of the traveltime refinement at a cell of the converged field
+// (missing neighbours count as absent, as in exact_coef); 0 at the source
+RZ_DEV float cell_residual_nb(const CellNb &n, float s, float dh, bool source) {
+    if (source) return 0.f;
+    return godunov_residual(fminf(n.tw, n.te), fminf(n.tn, n.ts), s, dh, n.tc);
 }
 
 // Sum of the n floats q[0], q[stride], ..., q[(n-1)*stride] as a double,

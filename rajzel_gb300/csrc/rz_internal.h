@@ -40,9 +40,10 @@ __host__ __device__ inline int skew_lines(int nxb) { return 32 * nxb + 64; }
 constexpr int kEdgePad = 48;
 __host__ __device__ inline int edge_row(int nxp) { return nxp + 2 * kEdgePad; }
 
-// kModeExact names the exact discrete adjoint sweeps (FP32); the forward of
-// such a launch runs in the context's reference or fast arithmetic.
-enum Mode : int { kModeReference = 0, kModeFast = 1, kModeExact = 2 };
+// kModeExact names the exact discrete adjoint sweeps (FP32), kModeTangent the
+// traveltime refinement's linear sweeps (FP32); the forward of such a launch
+// runs in the context's reference or fast arithmetic.
+enum Mode : int { kModeReference = 0, kModeFast = 1, kModeExact = 2, kModeTangent = 3 };
 
 struct ShotParams {
     // grid
@@ -57,6 +58,8 @@ struct ShotParams {
     int do_adjoint;         // 0: forward (+ residuals) only
     int start_adjoint;      // 1: T and Tres are given; skip forward and residuals
     int exact;              // adjoint: 0 Leung-Qian (sweep_adj.c), 1 exact discrete adjoint
+    int refine;             // refine the converged traveltimes to the FP64 fixpoint: T holds the
+                            // refined values rounded to float, Told their low parts
     int cotangent;          // exact: Tobs holds dJ/dTmod itself (vector-Jacobian product)
     // model (shared by all shots)
     const float *S;         // slowness [ny][nx]
@@ -110,6 +113,8 @@ struct ShotParams {
     // signal in its first sweep, so warp 1's bounded wait runs out
     uint32_t spin;
     int withhold;
+    // fixpoint checks: most rows per task (0: kCheckRows), the autotuner's choice
+    int check_rows;
 };
 
 // Tensor maps of a launch.  Field maps cover [shots][ny][nxp] floats with
@@ -147,8 +152,10 @@ int shot_kernel_warps(int nstrips);  // warps per CTA for a grid of nstrips stri
 cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int W, int *nctas, cudaStream_t st);
 // warps: strips swept together per band; 0 = the balanced choice of
 // shot_kernel_warps.  The CTA may hold more warps than that (they share the
-// cell-parallel phases) where this costs no occupancy; no result changes.
-cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const ShotMaps &maps, cudaStream_t st, int warps = 0);
+// cell-parallel phases) where this costs no occupancy: cta_warps caps them
+// (0 = as many as fit).  No result changes.
+cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const ShotMaps &maps, cudaStream_t st, int warps = 0,
+                               int cta_warps = 0);
 
 // launchers (rz_aux.cu)
 cudaError_t launch_skew_field(const float *src, int nx, int ny, int pitch, int nstrips, int nxb, float *dstA,
@@ -168,10 +175,11 @@ cudaError_t launch_stack(const float *L, size_t fstride, int nshots, const doubl
                          cudaStream_t st, bool frame = false, const double *l2 = nullptr, int nl2 = 0,
                          double *l2_out = nullptr);
 // exact-adjoint gradient dJ/dVp = -S^2 sum_s mu_s * dG/dS (G the Godunov
-// update at the converged traveltimes T_s); continues grad64 when accumulate
+// update at the converged traveltimes T_s, or T_s + Tlo_s when refined);
+// continues grad64 when accumulate
 cudaError_t launch_stack_exact(const float *T, const float *L, size_t fstride, int nshots, const int *src_h,
                                const int *src_k, const float *S, int nx, int ny, int nxp, float dh, float *grad,
-                               double *grad64, bool accumulate, cudaStream_t st);
+                               double *grad64, bool accumulate, cudaStream_t st, const float *Tlo = nullptr);
 cudaError_t launch_cp_frame(float *A, double *A64, int nx, int ny, int pitch, int times, cudaStream_t st);
 cudaError_t launch_copy_rows(const float *src, int src_pitch, float *dst, int dst_pitch, int nx, int ny,
                              size_t nbatch, size_t src_bstride, size_t dst_bstride, cudaStream_t st);

@@ -145,9 +145,9 @@ RZ_DEV unsigned long long global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-// per-shot timeline (ns): 0 start, 1 forward done, 2 residuals done,
-// 3 adjoint prep done, 4 adjoint done, 5 first forward sweep done,
-// 6 first adjoint sweep done
+// per-shot timeline (ns): 0 start, 1 forward done (refinement included),
+// 2 residuals done, 3 adjoint prep done, 4 adjoint done, 5 first forward
+// sweep done, 6 first adjoint sweep done, 7 refinement started
 RZ_DEV void stamp(const ShotParams &P, int z, int slot) {
     if (P.timeline && threadIdx.x == 0) P.timeline[(size_t)z * kTimelineSlots + slot] = global_ns();
 }
@@ -180,8 +180,11 @@ constexpr uint32_t kRingBytes = kRing * kSlotBytes;           // 12672
 template <int DX, int DY, bool ADJ, int MODE, int DIV = 1>
 __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mld, const CUtensorMap *mst,
                                    float &acc, float &mag, int band, int W, const SweepSeq &seq) {
-    // exact discrete adjoint: mu = R + sum of the weights neighbours put on this cell
-    constexpr bool EX = ADJ && (MODE == kModeExact);
+    // linear sweeps over weight streams: the exact discrete adjoint, mu = R +
+    // the weights neighbours put on this cell; the traveltime refinement (TAN),
+    // delta = r + this cell's weights on its upwind neighbours
+    constexpr bool TAN = ADJ && (MODE == kModeTangent);
+    constexpr bool EX = ADJ && (MODE == kModeExact || MODE == kModeTangent);
     const int l = w.l, g = w.g;
     if (g >= W) return;  // warps beyond this grid's W only join the CTA's barriers
     const bool pipe = seq.pipelined != 0;
@@ -547,10 +550,16 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     const float lE = DX > 0 ? ev : res_prev, lW = DX > 0 ? res_prev : ev;
                     const float lS = DY > 0 ? sv : nv, lN = DY > 0 ? nv : sv;
                     float m = rcell;
-                    m = wxW > 0.f ? fmaf(wxW, lW, m) : m;
-                    m = wxE < 0.f ? fmaf(-wxE, lE, m) : m;
-                    m = wzN > 0.f ? fmaf(wzN, lN, m) : m;
-                    m = wzS < 0.f ? fmaf(-wzS, lS, m) : m;
+                    if (TAN) {
+                        // own weights: < 0 on the west / north neighbour, > 0 on the east / south one
+                        m = c_tt < 0.f ? fmaf(-c_tt, lW, m) : (c_tt > 0.f ? fmaf(c_tt, lE, m) : m);
+                        m = c_wz < 0.f ? fmaf(-c_wz, lN, m) : (c_wz > 0.f ? fmaf(c_wz, lS, m) : m);
+                    } else {
+                        m = wxW > 0.f ? fmaf(wxW, lW, m) : m;
+                        m = wxE < 0.f ? fmaf(-wxE, lE, m) : m;
+                        m = wzN > 0.f ? fmaf(wzN, lN, m) : m;
+                        m = wzS < 0.f ? fmaf(-wzS, lS, m) : m;
+                    }
                     r = valid ? m : own;
                     mag_l += valid ? fabsf(r) : 0.0f;
                     w_tt = c_tt;
@@ -717,8 +726,9 @@ RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold,
 // is, hence so does the second, and so on through all four sweeps.  Such a
 // pass has zero change, so the stopping rule ends the loop after it; the
 // caller counts it without sweeping it, and every result stays the same.
-// The checks split the grid into tasks of 128 columns x at most kCheckRows
-// rows (check_task_rows balances the tasks over the warps).  A
+// The checks split the grid into tasks of 128 columns x at most P.check_rows
+// rows (kCheckRows by default; check_task_rows balances the tasks over the
+// warps; the autotuner picks the cap).  A
 // warp walks a task top to bottom, four cells per lane.  Lane 0 loads the
 // task's rows in boxes of kCheckBox rows by tensor-map copies into a ring of
 // three slots (one mbarrier each) in the warp's shared memory.  A box of a
@@ -732,10 +742,10 @@ constexpr int kCheckRows = 64, kCheckBox = kCheckBoxRows, kCheckHaloCols = kChec
 
 // Rows per task for `rows` rows in nch column chunks and W warps: the fewest
 // rounds of W tasks times (rows per task + one box of start-up), at most
-// kCheckRows rows per task.
-RZ_DEV int check_task_rows(int rows, int nch, int W) {
-    const int n0 = (rows + kCheckRows - 1) / kCheckRows;
-    int best_r = kCheckRows, best = 0x7fffffff;
+// cap rows per task.
+RZ_DEV int check_task_rows(int rows, int nch, int W, int cap) {
+    const int n0 = (rows + cap - 1) / cap;
+    int best_r = cap, best = 0x7fffffff;
     for (int nrb = n0; nrb <= 4 * n0 + 4; ++nrb) {
         const int r = (rows + nrb - 1) / nrb;
         const int cost = ((nch * nrb + W - 1) / W) * (r + kCheckBox);
@@ -810,7 +820,8 @@ __device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUten
                                                 int z, WarpShared *ws, int *found, volatile int *abort_word) {
     const int nx = P.nx, ny = P.ny;
     const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
-    const int nch = (nx + 127) >> 7, rt = check_task_rows(ny, nch, W), nrb = (ny + rt - 1) / rt;
+    const int cap = P.check_rows > 0 ? P.check_rows : kCheckRows;
+    const int nch = (nx + 127) >> 7, rt = check_task_rows(ny, nch, W, cap), nrb = (ny + rt - 1) / rt;
     if (threadIdx.x == 0) *found = 0;
     fence_proxy_async_smem();  // the ring's generic accesses precede the copies
     __syncthreads();
@@ -891,7 +902,8 @@ __device__ __noinline__ int adjoint_is_fixpoint(const ShotParams &P, const CUten
                                                 int z, WarpShared *ws, int *found, volatile int *abort_word) {
     const int nx = P.nx, ny = P.ny, nxp = P.nxp;
     const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
-    const int nch = (nx + 127) >> 7, rt = check_task_rows(ny - 2, nch, W), nrb = (ny - 2 + rt - 1) / rt;
+    const int cap = P.check_rows > 0 ? P.check_rows : kCheckRows;
+    const int nch = (nx + 127) >> 7, rt = check_task_rows(ny - 2, nch, W, cap), nrb = (ny - 2 + rt - 1) / rt;
     const DivDH div{P.dh, P.dh_rcp, DIV != 0};
     const float eps_h2 = lq_eps_h2(P.eps_adj, P.dh);  // fast-mode Leung-Qian threshold
     if (threadIdx.x == 0) *found = 0;
@@ -1069,7 +1081,10 @@ __device__ __noinline__ void relayout_items(const ShotParams &P, Warp &w, const 
 // the sweeps (x weights in TA/TB, z weights in WZA/WZB, those of the rows
 // bordering each strip in EU/ED), dJ/dT at the receiver cells (RA/RB, the
 // residuals of each cell's receivers summed in receiver order), mu = 0.
-__device__ __noinline__ void exact_prepare(const ShotParams &P, int z, const float *T, float *L) {
+// With refined traveltimes (P.refine) the weights are those of T + Told.
+// tangent: the traveltime refinement's system instead -- the weights of the
+// unrefined field and the residual r of every cell (cell_residual) in RA/RB.
+__device__ __noinline__ void exact_prepare(const ShotParams &P, int z, const float *T, float *L, bool tangent) {
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int l = tid & 31, g = tid >> 5, W = nthr >> 5;
     const int hs = P.src_h[z], ks = P.src_k[z];
@@ -1078,22 +1093,55 @@ __device__ __noinline__ void exact_prepare(const ShotParams &P, int z, const flo
     float *wxa = P.TA + (size_t)z * P.sstride, *wxb = P.TB + (size_t)z * P.sstride;
     float *wza = P.WZA + (size_t)z * P.sstride, *wzb = P.WZB + (size_t)z * P.sstride;
     float *ra = P.RA + (size_t)z * P.sstride, *rb = P.RB + (size_t)z * P.sstride;
-    for (size_t li = g; li < lines; li += W) {
-        const int s = (int)(li / qn), q = (int)(li - (size_t)s * qn) - kSkewFront;
-        const int row = kStrip * s + l;
-        const int ha = q - l, hb = q + l - 31;
-        const size_t o = li * 32 + l;
-        ExactCoef ca{0.f, 0.f, 0.f}, cb{0.f, 0.f, 0.f};
-        if (row < ny) {
-            if (ha >= 0 && ha < nx) ca = exact_coef(T, nxp, nx, ny, ha, row, __ldg(P.SA + o), P.dh, ha == hs && row == ks);
-            if (hb >= 0 && hb < nx) cb = exact_coef(T, nxp, nx, ny, hb, row, __ldg(P.SB + o), P.dh, hb == hs && row == ks);
+    // low parts of refined traveltimes (the adjoint after a refinement)
+    const float *lo = (P.refine && !tangent) ? P.Told + (size_t)z * P.fstride : nullptr;
+    // U lines per warp and round: every load of the round is issued before
+    // any value is used (the prep is bound by memory latency)
+    constexpr int U = 4;
+    for (size_t li0 = g; li0 < lines; li0 += (size_t)U * W) {
+        CellNb na[U], nb[U];
+        float sa[U], sb[U];
+        bool ina[U], inb[U];
+        int ha[U], hb[U], row[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const size_t li = li0 + (size_t)u * W;
+            const int s = (int)(li / qn), q = (int)(li - (size_t)s * qn) - kSkewFront;
+            row[u] = kStrip * s + l;
+            ha[u] = q - l, hb[u] = q + l - 31;
+            const bool live = li < lines && row[u] < ny;
+            ina[u] = live && ha[u] >= 0 && ha[u] < nx;
+            inb[u] = live && hb[u] >= 0 && hb[u] < nx;
+            const size_t o = (li < lines ? li : 0) * 32 + l;
+            sa[u] = ina[u] ? __ldg(P.SA + o) : 0.f;
+            sb[u] = inb[u] ? __ldg(P.SB + o) : 0.f;
+            if (ina[u]) na[u] = load_cell_nb(T, lo, nxp, nx, ny, ha[u], row[u]);
+            if (inb[u]) nb[u] = load_cell_nb(T, lo, nxp, nx, ny, hb[u], row[u]);
         }
-        wxa[o] = ca.wx;
-        wza[o] = ca.wz;
-        ra[o] = 0.f;
-        wxb[o] = cb.wx;
-        wzb[o] = cb.wz;
-        rb[o] = 0.f;
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+            const size_t li = li0 + (size_t)u * W;
+            if (li >= lines) break;
+            const size_t o = li * 32 + l;
+            ExactCoef ca{0.f, 0.f, 0.f}, cb{0.f, 0.f, 0.f};
+            float rva = 0.f, rvb = 0.f;
+            if (ina[u]) {
+                const bool src = ha[u] == hs && row[u] == ks;
+                ca = exact_coef_nb(na[u], sa[u], P.dh, src);
+                if (tangent) rva = cell_residual_nb(na[u], sa[u], P.dh, src);
+            }
+            if (inb[u]) {
+                const bool src = hb[u] == hs && row[u] == ks;
+                cb = exact_coef_nb(nb[u], sb[u], P.dh, src);
+                if (tangent) rvb = cell_residual_nb(nb[u], sb[u], P.dh, src);
+            }
+            wxa[o] = ca.wx;
+            wza[o] = ca.wz;
+            ra[o] = rva;
+            wxb[o] = cb.wx;
+            wzb[o] = cb.wz;
+            rb[o] = rvb;
+        }
     }
     // z weights of the rows above (EU) and below (ED) each strip
     const int er = edge_row(nxp);
@@ -1105,11 +1153,11 @@ __device__ __noinline__ void exact_prepare(const ShotParams &P, int z, const flo
             // slowness of these cells from the skewed copy (family A, q = h + j)
             if (ru >= 0) {
                 const size_t o = ((size_t)(s - 1) * qn + (col + 31) + kSkewFront) * 32 + 31;
-                vu = exact_coef(T, nxp, nx, ny, col, ru, __ldg(P.SA + o), P.dh, col == hs && ru == ks).wz;
+                vu = exact_coef(T, nxp, nx, ny, col, ru, __ldg(P.SA + o), P.dh, col == hs && ru == ks, lo).wz;
             }
             if (rd < ny) {
                 const size_t o = ((size_t)(s + 1) * qn + col + kSkewFront) * 32;
-                vd = exact_coef(T, nxp, nx, ny, col, rd, __ldg(P.SA + o), P.dh, col == hs && rd == ks).wz;
+                vd = exact_coef(T, nxp, nx, ny, col, rd, __ldg(P.SA + o), P.dh, col == hs && rd == ks, lo).wz;
             }
         }
         P.EU[(size_t)z * P.estride + (size_t)s * er + kEdgePad + col] = vu;
@@ -1117,6 +1165,7 @@ __device__ __noinline__ void exact_prepare(const ShotParams &P, int z, const flo
     }
     fill_field(P, L, 0.0f, false);
     __syncthreads();
+    if (tangent) return;
     for (int i = tid; i < P.nxcell; i += nthr) {
         const int h = P.xcell_h[i], k = P.xcell_k[i];
         float sum = 0.f;
@@ -1124,6 +1173,27 @@ __device__ __noinline__ void exact_prepare(const ShotParams &P, int z, const flo
         const int s = k >> 5, j = k & 31;
         ra[((size_t)s * qn + (h + j) + kSkewFront) * 32 + j] = sum;
         rb[((size_t)s * qn + (h - j + 31) + kSkewFront) * 32 + j] = sum;
+    }
+}
+
+// refined traveltimes: T := RN(T + delta), Told := (T - RN(T + delta)) + delta
+// (exact: |delta| <= |T| away from the source, where both are 0)
+RZ_DEV void split_refined(const ShotParams &P, float *T, const float *D, float *Tlo) {
+    const int W = blockDim.x >> 5, g = threadIdx.x >> 5, l = threadIdx.x & 31, nq = P.nxp >> 2;
+    for (int k = g; k < P.ny; k += W) {
+        float4 *t = reinterpret_cast<float4 *>(T + (size_t)k * P.nxp);
+        const float4 *d = reinterpret_cast<const float4 *>(D + (size_t)k * P.nxp);
+        float4 *lo = reinterpret_cast<float4 *>(Tlo + (size_t)k * P.nxp);
+        for (int q = l; q < nq; q += 32) {
+            const float4 a = __ldcg(t + q), b = __ldcg(d + q);
+            float4 hi, rem;
+            hi.x = __fadd_rn(a.x, b.x), rem.x = __fadd_rn(__fsub_rn(a.x, hi.x), b.x);
+            hi.y = __fadd_rn(a.y, b.y), rem.y = __fadd_rn(__fsub_rn(a.y, hi.y), b.y);
+            hi.z = __fadd_rn(a.z, b.z), rem.z = __fadd_rn(__fsub_rn(a.z, hi.z), b.z);
+            hi.w = __fadd_rn(a.w, b.w), rem.w = __fadd_rn(__fsub_rn(a.w, hi.w), b.w);
+            t[q] = hi;
+            lo[q] = rem;
+        }
     }
 }
 
@@ -1273,6 +1343,41 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
         }
         if (tid == 0) P.passes_fwd[z] = pass;
         if (tid == 0 && P.swept) P.swept[2 * z] = swept;
+        if (P.refine && !*w.abort_word) {
+            // Traveltime refinement to the FP64 fixpoint (not in the
+            // reference): delta = r + W delta with r the float-float residual
+            // of every cell and W the weights of the float field, solved by the
+            // linear sweeps in the forward orders until a pass changes delta by
+            // less than 1e-7 of its magnitude; then T := RN(T + delta) and
+            // Told := the remainder, so T + Told is the refined field.
+            __syncthreads();
+            stamp(P, z, 7);
+            exact_prepare(P, z, T, L, true);
+            fence_proxy_async_global();
+            __syncthreads();
+            int tp = 0;
+            for (bool more = true; more;) {
+                if (tp >= P.max_passes) {
+                    cta_err |= ERR_NOCONV_FWD;
+                    break;
+                }
+                float acc = 0.f, mag = 0.f;
+                RZ_SWEEP(+1, +1, true, kModeTangent, &M.lld, &M.lst);
+                RZ_SWEEP(-1, +1, true, kModeTangent, &M.lld, &M.lst);
+                RZ_SWEEP(-1, -1, true, kModeTangent, &M.lld, &M.lst);
+                RZ_SWEEP(+1, -1, true, kModeTangent, &M.lld, &M.lst);
+                if (seq.pipelined) __syncthreads();
+                ++tp;
+                if (*w.abort_word) break;
+                const double tot = block_sum((double)acc, sh);
+                const double m = block_sum((double)mag, sh);
+                more = tot > 1e-7 * m;
+            }
+            __syncthreads();
+            split_refined(P, T, L, Told);
+            fence_proxy_async_global();
+            __syncthreads();
+        }
         stamp(P, z, 1);
 
         // ---------------- receivers: picks, residuals, misfit ----------------
@@ -1287,23 +1392,38 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                 for (int i = tid; i < m; i += blockDim.x) {
                     const int r = base + i;
                     const int h = P.rec_h[r], k = P.rec_k[r];
-                    const float tm = __ldcg(T + (size_t)k * P.nxp + h);
+                    const size_t o = (size_t)k * P.nxp + h;
+                    const float tm = __ldcg(T + o);
+                    // refined traveltimes: T + Told (the low part), residuals in double
+                    const float tl = P.refine ? __ldcg(Told + o) : 0.0f;
                     P.Tmod[(size_t)z * P.ntr + r] = tm;
                     const float tob = P.do_residual ? P.Tobs[(size_t)z * P.ntr + r] : -1.0f;
                     float tr = 0.f, q = 0.f;
                     if (P.cotangent) {
                         tr = tob;  // dJ/dTmod given by the caller
                     } else if (P.exact && tob >= 0.0f) {
-                        tr = __fsub_rn(tm, tob);  // dJ/dTmod of J = 0.5 sum (Tmod - Tobs)^2
-                        q = __fmul_rn(tr, tr);
+                        if (P.refine) {
+                            const double res = ((double)tm - (double)tob) + (double)tl;
+                            tr = __double2float_rn(res);
+                            q = __double2float_rn(res * res);
+                        } else {
+                            tr = __fsub_rn(tm, tob);  // dJ/dTmod of J = 0.5 sum (Tmod - Tobs)^2
+                            q = __fmul_rn(tr, tr);
+                        }
                     } else if (tob >= 0.0f) {
-                        tr = __fsub_rn(tm, tob);
+                        tr = P.refine ? __double2float_rn(((double)tm - (double)tob) + (double)tl) : __fsub_rn(tm, tob);
                         q = __fmul_rn(tr, tr);
                         float gt;
                         bool have = true;
-                        if (k <= P.ny - 2) gt = __fsub_rn(__ldcg(T + (size_t)(k + 1) * P.nxp + h), tm);
-                        else if (k == P.ny - 1) gt = __fsub_rn(tm, __ldcg(T + (size_t)(k - 1) * P.nxp + h));
-                        else have = false;
+                        if (k <= P.ny - 2) {
+                            gt = __fsub_rn(__ldcg(T + o + P.nxp), tm);
+                            if (P.refine) gt = __fadd_rn(gt, __fsub_rn(__ldcg(Told + o + P.nxp), tl));
+                        } else if (k == P.ny - 1) {
+                            gt = __fsub_rn(tm, __ldcg(T + o - P.nxp));
+                            if (P.refine) gt = __fadd_rn(gt, __fsub_rn(tl, __ldcg(Told + o - P.nxp)));
+                        } else {
+                            have = false;
+                        }
                         if (have) {
                             gt = __fdiv_rn(gt, P.dh);
                             tr = (fabsf(gt) > 0.0f) ? __fdiv_rn(tr, gt) : 0.0f;
@@ -1345,7 +1465,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
         return;
     }
     if (P.exact) {
-        exact_prepare(P, z, T, L);
+        exact_prepare(P, z, T, L, false);
     } else {
         {
             const int items = P.nstrips * (P.nxb + 1), Wb = (int)(blockDim.x >> 5);
@@ -1536,18 +1656,17 @@ cudaError_t launch_multi_shot_kernel(const MultiParams &M, int mode, int W, int 
     return cudaGetLastError();
 }
 
-cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const ShotMaps &M, cudaStream_t st, int warps) {
+cudaError_t launch_shot_kernel(const ShotParams &P, int mode, const ShotMaps &M, cudaStream_t st, int warps,
+                               int cta_warps) {
     if (P.nstrips < 1) return cudaErrorInvalidValue;
     const int W = warps > 0 ? std::min(std::min(warps, kMaxWarps), P.nstrips) : shot_kernel_warps(P.nstrips);
     int Wb = W;
     cudaError_t e;
-    if (mode == kModeReference) {
-        if ((e = block_warps_cached(shot_kernel<kModeReference>, 0, W, &Wb))) return e;
-        shot_kernel<kModeReference><<<P.nshots, 32 * Wb, shot_kernel_smem(Wb), st>>>(P, M, W);
-    } else {
-        if ((e = block_warps_cached(shot_kernel<kModeFast>, 1, W, &Wb))) return e;
-        shot_kernel<kModeFast><<<P.nshots, 32 * Wb, shot_kernel_smem(Wb), st>>>(P, M, W);
-    }
+    auto kern = mode == kModeReference ? shot_kernel<kModeReference> : shot_kernel<kModeFast>;
+    if ((e = block_warps_cached(kern, mode == kModeReference ? 0 : 1, W, &Wb))) return e;
+    // a requested CTA width between W and the widest that keeps the occupancy
+    if (cta_warps > 0) Wb = std::max(W, std::min(cta_warps, Wb));
+    kern<<<P.nshots, 32 * Wb, shot_kernel_smem(Wb), st>>>(P, M, W);
     return cudaGetLastError();
 }
 

@@ -29,12 +29,13 @@ def R(gpu_lib):
     return gpu_lib
 
 
-def ctx_for(R, w, mode, vp=None, ttnorm=None, kind="reference"):
+def ctx_for(R, w, mode, vp=None, ttnorm=None, kind="reference", refine=False):
     ctx = R.Context(0, mode)
     ctx.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm if ttnorm is None else ttnorm, w.eps_adj)
     ctx.set_velocity(w.vp_true if vp is None else vp)
     ctx.set_receivers(w.recx, w.recz)
     ctx.set_gradient(kind)
+    ctx.set_refine(refine)
     return ctx
 
 
@@ -183,3 +184,94 @@ def test_full_size_error_check_gates(R):
     # the exact gradient of the float misfit: its residuals carry the float
     # traveltimes' path error (misfit 5.6e-4 from FP64), ~3e-3 here
     assert ex["grad_rel_l2"] <= 5e-3
+
+
+# ---------------------------------------------------------------------------
+# traveltime refinement (rz_set_refine)
+# ---------------------------------------------------------------------------
+@pytest.mark.parametrize("mode", ["fast", "reference"])
+def test_refined_traveltimes_reach_fp64(R, mode):
+    """With refinement the float traveltimes are the FP64 fixpoint rounded to
+    float: within 1e-7 of FP64 at the benchmark size (1700 x 350), where the
+    unrefined float fields sit ~2e-5 away."""
+    w = synth.grad_1700x350(nshots=100, ntr=850)
+    idx = np.arange(0, 100, 13)[:8]
+    sx, sz = w.srcx[idx], w.srcz[idx]
+    ctx = ctx_for(R, w, mode, vp=w.vp_start, refine=True)
+    TT, Tmod, _ = ctx.forward(sx, sz)
+    TT64, Tmod64 = ctx.forward_f64(sx, sz)
+    errs = [tt_rel(TT[i], TT64[i]) for i in range(len(idx))]
+    assert max(errs) <= 1e-7, errs
+    assert tt_rel(Tmod, Tmod64) <= 1e-7
+
+
+def test_refined_exact_gradient_within_1e4_at_full_size(R):
+    """The benchmark's 100 shots: the exact gradient of refined traveltimes is
+    within 1e-4 (relative L2) of the FP64 oracle's exact gradient, and the
+    misfit within 1e-6; the Leung-Qian gradient of refined traveltimes stays
+    no further from FP64 than the unrefined one."""
+    w = synth.grad_1700x350(nshots=100, ntr=850)
+    _, Tobs, _ = ctx_for(R, w, "fast").forward(w.srcx, w.srcz, want_tt=False)
+    reps = {}
+    for kind, refine in (("exact", True), ("reference", True), ("reference", False)):
+        ctx = ctx_for(R, w, "fast", vp=w.vp_start, kind=kind, refine=refine)
+        ctx.set_error_check(True)
+        ctx.grad_obj(w.srcx, w.srcz, Tobs)
+        reps[kind, refine] = ctx.error_report()
+    ex = reps["exact", True]
+    assert ex["shots"] == 100 and ex["tt_rel"] <= 1e-7
+    assert ex["grad_rel_l2"] <= GRAD_TOL and ex["misfit_rel"] <= 1e-5
+    assert reps["reference", True]["grad_rel_l2"] <= reps["reference", False]["grad_rel_l2"]
+
+
+def test_refined_exact_gradient_central_differences_config2(R):
+    """<g, dS> of the refined exact gradient against central differences of
+    the FP64 misfit (GPU FP64 oracle) on 20 random slowness perturbations, 16
+    of the benchmark's shots on 1700 x 350 with 850 receivers, as the relative
+    L2 error of the 20 directional derivatives.  The realised perturbation is
+    the difference of the two float models, so the float rounding of
+    S +- eps dS does not enter."""
+    w = synth.grad_1700x350(nshots=100, ntr=850)
+    idx = np.linspace(0, 99, 16).round().astype(int)
+    sx, sz = w.srcx[idx], w.srcz[idx]
+    _, Tobs, _ = ctx_for(R, w, "fast").forward(sx, sz, want_tt=False)
+    g_vp, _ = ctx_for(R, w, "fast", vp=w.vp_start, kind="exact", refine=True).grad_obj(sx, sz, Tobs)
+    S = synth.slowness(w.vp_start)
+    g_s = -np.asarray(g_vp, np.float64) / (S.astype(np.float64) ** 2)
+    cm = R.Context(0, "fp64")
+    cm.set_grid(w.nx, w.ny, w.dh, w.time, 1e-14, w.eps_adj)
+    cm.set_receivers(w.recx, w.recz)
+    rng = np.random.default_rng(20)
+    fds, projs = [], []
+    for _ in range(20):
+        d = rng.standard_normal(S.shape) * S
+        sp, sm = (S + 1e-6 * d).astype(np.float32), (S - 1e-6 * d).astype(np.float32)
+        step = (sp.astype(np.float64) - sm.astype(np.float64)) / 2
+        cm.set_slowness(sp)
+        jp = cm.misfit(sx, sz, Tobs)
+        cm.set_slowness(sm)
+        jm = cm.misfit(sx, sz, Tobs)
+        fds.append((jp - jm) / 2)
+        projs.append(float((g_s * step).sum()))
+    fds, projs = np.array(fds), np.array(projs)
+    # over the 20 directions (a single random direction can be nearly
+    # orthogonal to the gradient, which inflates its own relative error)
+    assert np.linalg.norm(fds - projs) / np.linalg.norm(fds) <= GRAD_TOL
+
+
+def test_exact_and_reference_gradients_agree_in_direction(R):
+    """The reference's Leung-Qian gradient (ass_grad.c: lambda S^3, the
+    adjoint of the continuous problem with the residuals scaled by dT/dz) and
+    the exact dJ/dVp of the discrete misfit, on the benchmark workload's
+    interior: the measured cosine and scale ratio, kept within bands."""
+    w = synth.grad_1700x350(nshots=100, ntr=850)
+    idx = np.linspace(0, 99, 16).round().astype(int)
+    sx, sz = w.srcx[idx], w.srcz[idx]
+    _, Tobs, _ = ctx_for(R, w, "fast").forward(sx, sz, want_tt=False)
+    ge, _ = ctx_for(R, w, "fast", vp=w.vp_start, kind="exact", refine=True).grad_obj(sx, sz, Tobs)
+    gr, _ = ctx_for(R, w, "reference", vp=w.vp_start).grad_obj(sx, sz, Tobs)
+    a, b = ge[2:-2, 2:-2].astype(np.float64), gr[2:-2, 2:-2].astype(np.float64)
+    cos = float((a * b).sum() / np.linalg.norm(a) / np.linalg.norm(b))
+    scale = float(np.linalg.norm(b) / np.linalg.norm(a))
+    assert 0.6 <= cos <= 0.8, cos
+    assert 0.02 <= scale <= 0.08, scale

@@ -477,8 +477,9 @@ def test_graph_replay_equals_direct_launches(R, mode):
 
 
 def test_autotuner_picks_a_width_that_changes_no_result(R):
-    """rz_autotune times the band-width candidates on the batch itself; the
-    chosen width is used afterwards and every width gives the same result."""
+    """rz_autotune times the launch shapes (band width x CTA width x check
+    task height) on the batch itself; the chosen shape is used afterwards and
+    gives the same result."""
     w = synth.small_case(17, 70, 700, nshots=3)  # 22 strips: 2, 3 or 4 bands
     p = params(w)
     S = synth.slowness(w.vp_true)
@@ -488,6 +489,8 @@ def test_autotuner_picks_a_width_that_changes_no_result(R):
     res = ctx.autotune(w.srcx, w.srcz, Tobs)
     assert set(res["candidates"]) == {11, 8, 6} and res["warps"] in res["candidates"]
     assert all(ms > 0 for ms in res["candidates"].values())
+    shape = res["shape"]  # band width, CTA width and fixpoint-check task height
+    assert shape["sweeping_warps"] == res["warps"] and shape["check_rows"] in (32, 64, 128)
     g1, l1 = ctx.grad_obj(w.srcx, w.srcz, Tobs)
     assert np.array_equal(g0, g1) and l0 == l1
     go, L2o, _, _, _ = O.grad_obj(p, S, w.srcx, w.srcz, w.recx, w.recz, Tobs)
