@@ -28,7 +28,19 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 PORT_SO = os.path.join(HERE, "librz_oracle.so")
 REF_SO = os.path.join(HERE, "_ref", "libref.so")
-REF_SRC = os.environ.get("RAJZEL_REFERENCE_SRC", "/root/reference/src")
+
+
+def _makefile_refsrc() -> str:
+    """The reference source directory the build recipe (oracle/Makefile, REFSRC) names."""
+    with open(os.path.join(HERE, "Makefile")) as f:
+        for line in f:
+            if line.startswith("REFSRC"):
+                return line.split("=", 1)[1].strip()
+    return ""
+
+
+# where the reference's sources are read from: RAJZEL_REFERENCE_SRC, else the recipe's default
+REF_SRC = os.environ.get("RAJZEL_REFERENCE_SRC") or _makefile_refsrc()
 
 RZO_OK, RZO_EINVAL, RZO_ENOCONV = 0, 1, 2
 

@@ -307,6 +307,7 @@ static int ensure_fields(rz_context *c, int n) {
     if ((r = make_map(c, &c->maps.lst, c->dL, n, kBlk, kStrip))) return r;
     if ((r = make_map(c, &c->maps.tchk, c->dT, n, kCheckCols, kCheckBoxRows))) return r;
     if ((r = make_map(c, &c->maps.lchk, c->dL, n, kCheckCols, kCheckBoxRows))) return r;
+    if ((r = make_map(c, &c->maps.tlo, c->dTold, n, kBlk, kBoxRows))) return r;
     return RZ_OK;
 }
 
@@ -426,6 +427,7 @@ static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     P.MB = c->dMB;
     P.T = c->dT;
     P.Told = c->dTold;
+    P.Sp = c->dSp;
     P.L = c->dL;
     P.TA = c->dTA;
     P.TB = c->dTB;

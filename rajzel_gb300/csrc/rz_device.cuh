@@ -428,12 +428,16 @@ RZ_DEV ExactCoef exact_coef_nb(const CellNb &n, float s, float dh, bool source) 
         c.gs = dh;
         return c;
     }
-    const float r = sqrtf(fmaf(2.0f * sh, sh, -d * d));
-    const float half_rcp = 0.5f / r;
+    // r = sqrt(q) and 1/r from one reciprocal square root (a few ulp: the
+    // weights enter a linear solve whose float error is of that order anyway)
+    const float q = fmaf(2.0f * sh, sh, -d * d);
+    const float rr = rsqrtf(q);
+    const float r = q * rr;
+    const float half_rcp = 0.5f * rr;
     const float wa = (r - d) * half_rcp, wb = (r + d) * half_rcp;
     c.wx = west ? -wa : wa;
     c.wz = north ? -wb : wb;
-    c.gs = s * dh * dh / r;
+    c.gs = s * dh * dh * rr;
     return c;
 }
 

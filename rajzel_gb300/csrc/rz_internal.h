@@ -69,6 +69,7 @@ struct ShotParams {
     // per-shot fields; shot z at offset z*fstride (floats)
     float *T;               // traveltime  [nshots][ny][nxp]
     float *Told;            // reference-mode snapshot  [nshots][ny][nxp]
+    const float *Sp;        // slowness in rows of nxp floats [ny][nxp]
     float *L;               // adjoint field lambda [nshots][ny][nxp]
     float *TA, *TB;         // skewed traveltimes [nshots][nstrips][qn][32]
                             // (exact adjoint: signed x weights, see exact_coef)
@@ -126,9 +127,10 @@ struct ShotParams {
 //   tchk traveltime, 136 x 4 box (fixpoint checks)
 //   lchk lambda, 136 x 4 box (adjoint fixpoint check)
 //   schk slowness in rows of nxp floats [1][ny][nxp], 128 x 4 box (forward check)
+//   tlo  low parts of refined traveltimes, 32 x kBoxRows box (exact adjoint preparation)
 constexpr int kCheckCols = 136, kCheckBoxRows = 4;  // box of tchk / lchk
 struct ShotMaps {
-    CUtensorMap tld, tst, lld, lst, tchk, lchk, schk;
+    CUtensorMap tld, tst, lld, lst, tchk, lchk, schk, tlo;
 };
 
 // several grids in one persistent launch

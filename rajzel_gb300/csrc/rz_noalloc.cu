@@ -130,6 +130,7 @@ extern "C" int rz_eikonal_noalloc(const rz_grid *grid, const float *S, float src
     M.lld = M.tld;  // no adjoint here
     M.lst = M.tst;
     M.lchk = M.tchk;
+    M.tlo = M.tld;
 
     ShotParams P;
     memset(&P, 0, sizeof P);

@@ -894,6 +894,96 @@ __device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUten
     return (__syncthreads_or(change) ? 0 : 1) | (R.err << 1);
 }
 
+// Whether a pass of the traveltime refinement's linear sweeps would change a
+// correction delta: for every cell, m = r + (own weights) x (delta of the
+// upwind neighbours), with the weights and the float-float residual r of the
+// float traveltimes as the refinement's preparation computes them, against
+// the cell's delta (relative 1e-6, absolute 1e-9 s).  Returns 1 when no cell
+// would change, plus the error flags shifted left by one.
+// mT / mL: traveltime / delta fields, box kCheckHaloCols x kCheckBox.
+__device__ __noinline__ int tangent_is_converged(const ShotParams &P, const CUtensorMap *mT, const CUtensorMap *mL,
+                                                 int z, WarpShared *ws, int *found, volatile int *abort_word) {
+    const int nx = P.nx, ny = P.ny, nxp = P.nxp;
+    const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
+    const int cap = P.check_rows > 0 ? P.check_rows : kCheckRows;
+    const int nch = (nx + 127) >> 7, rt = check_task_rows(ny, nch, W, cap), nrb = (ny + rt - 1) / rt;
+    const int hs = P.src_h[z], ks = P.src_k[z];
+    const float big = 3.0e38f;
+    if (threadIdx.x == 0) *found = 0;
+    fence_proxy_async_smem();  // the ring's generic accesses precede the copies
+    __syncthreads();
+    CheckRing R{smem_u32(&ws->ring[0][0]), smem_u32(ws->cbar), smem_u32((const void *)abort_word), ws->cphase, 0};
+    bool change = false;
+    for (int task = g; task < nch * nrb && !change; task += W) {
+        if (__shfl_sync(0xffffffffu, *(volatile int *)found, 0)) break;  // warp-uniform
+        const int base = (task % nch) << 7, h0 = base + 4 * l;
+        // rows k0 .. k0+kk-1; window row j is grid row k0-1+j, j = 0 .. kk+1
+        const int k0 = (task / nch) * rt, kk = min(ny - k0, rt);
+        const int nb = ((kk + 1) >> 2) + 1;
+        auto issue = [&](int b) {
+            if (b >= nb || l != 0) return;
+            const uint32_t sl = R.base + (uint32_t)(b % kCheckSlots) * kCheckSlotA;
+            const uint32_t br = R.bars + 8u * (uint32_t)(b % kCheckSlots);
+            mbar_arrive_expect_tx_a(br, kCheckSlotA);
+            tma_load_3d_a(sl, mT, base - 4, k0 - 1 + kCheckBox * b, z, br);
+            tma_load_3d_a(sl + kCheckBox * kRowH, mL, base - 4, k0 - 1 + kCheckBox * b, z, br);
+        };
+        auto trow = [&](int j) {
+            return R.base + (uint32_t)((j >> 2) % kCheckSlots) * kCheckSlotA + (uint32_t)(j & 3) * kRowH;
+        };
+        issue(0), issue(1), issue(2);
+        __syncwarp();
+        R.wait(0);
+        for (int b = 0; b < nb; ++b) {
+#pragma unroll
+            for (int r = 0; r < kCheckBox; ++r) {
+                const int j = kCheckBox * b + r, k = k0 - 1 + j;
+                if (j < 1 || j > kk) continue;  // warp-uniform
+                if (r == kCheckBox - 1) R.wait(b + 1);  // holds row j+1
+                const uint32_t rc = trow(j), ru = trow(j - 1), rd = trow(j + 1);
+                const uint32_t lo = kCheckBox * kRowH;  // delta box follows the T box
+                const Row4 tc = box_row4(rc, l), lc = box_row4(rc + lo, l);
+                const float4 tu = lds4(ru + 16u + 16u * l), td = lds4(rd + 16u + 16u * l);
+                const float4 lu = lds4(ru + lo + 16u + 16u * l), ld = lds4(rd + lo + 16u + 16u * l);
+                const float4 s4 = h0 + 3 < nxp ? __ldg(reinterpret_cast<const float4 *>(P.Sp + (size_t)k * nxp + h0))
+                                               : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float tuv[4] = {tu.x, tu.y, tu.z, tu.w}, tdv[4] = {td.x, td.y, td.z, td.w};
+                const float luv[4] = {lu.x, lu.y, lu.z, lu.w}, ldv[4] = {ld.x, ld.y, ld.z, ld.w};
+                const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int h = h0 + i;
+                    if (h >= nx) continue;
+                    CellNb n;
+                    n.tc = tc.v[i];
+                    n.tw = h > 0 ? (i == 0 ? tc.w : tc.v[i - 1]) : big;
+                    n.te = h < nx - 1 ? (i == 3 ? tc.e : tc.v[i + 1]) : big;
+                    n.tn = k > 0 ? tuv[i] : big;
+                    n.ts = k < ny - 1 ? tdv[i] : big;
+                    n.lw = n.le = n.ln = n.ls = 0.f;
+                    const bool src = h == hs && k == ks;
+                    const ExactCoef c = exact_coef_nb(n, sv[i], P.dh, src);
+                    float m = cell_residual_nb(n, sv[i], P.dh, src);
+                    const float dw = i == 0 ? lc.w : lc.v[i - 1], de = i == 3 ? lc.e : lc.v[i + 1];
+                    m = c.wx < 0.f ? fmaf(-c.wx, dw, m) : (c.wx > 0.f ? fmaf(c.wx, de, m) : m);
+                    m = c.wz < 0.f ? fmaf(-c.wz, luv[i], m) : (c.wz > 0.f ? fmaf(c.wz, ldv[i], m) : m);
+                    const float own = lc.v[i];
+                    change |= !(fabsf(m - own) <= 1e-9f + 1e-6f * fabsf(own));
+                }
+            }
+            // box b-1 is read by no later row: box b+2 takes its slot
+            fence_proxy_async_smem();
+            __syncwarp();
+            if (b >= 1) issue(b + 2);
+        }
+        change = __any_sync(0xffffffffu, change);
+        if (change && l == 0) *(volatile int *)found = 1;
+    }
+    if (l == 0) ws->cphase = R.phase;
+    fence_proxy_async_smem();  // before the next sweep's copies into the ring
+    return (__syncthreads_or(change) ? 0 : 1) | (R.err << 1);
+}
+
 // the Leung-Qian update of interior, non-receiver cells (sweep_adj.c:26-30);
 // skip is the [ny][nxp] byte map of cells the adjoint sweeps leave unchanged.
 // mT / mL: traveltime / lambda fields, box kCheckHaloCols x kCheckBox.
@@ -1020,7 +1110,17 @@ RZ_DEV void fill_field(const ShotParams &P, float *F, float v, bool frame0) {
 // rows bordering each strip (TMA tiles in, coalesced skew lines out).  The
 // work items are (strip s, block G), G = 0..nxb, numbered s*(nxb+1)+G; a warp
 // takes items [i0, i1) in order, so the warps of the CTA share the strips.
-__device__ __noinline__ void relayout_items(const ShotParams &P, Warp &w, const CUtensorMap *mld, int i0, int i1) {
+// The field of shot z under mld goes to the families A / B at dA / dB (the
+// shot's TA / TB by default) and its border rows to dEU / dED (none if null).
+struct SkewDst {
+    float *a, *b, *eu, *ed;
+};
+RZ_DEV SkewDst skew_dst_t(const ShotParams &P, int z) {
+    return {P.TA + (size_t)z * P.sstride, P.TB + (size_t)z * P.sstride, P.EU + (size_t)z * P.estride,
+            P.ED + (size_t)z * P.estride};
+}
+__device__ __noinline__ void relayout_items(const ShotParams &P, Warp &w, const CUtensorMap *mld, int i0, int i1,
+                                            SkewDst dst) {
     const int l = w.l, z = w.z;
     float *ring = &w.ws->ring[0][0];
     const int nxb = P.nxb, per = nxb + 1, er = edge_row(P.nxp);
@@ -1037,10 +1137,10 @@ __device__ __noinline__ void relayout_items(const ShotParams &P, Warp &w, const 
         const int G = it % per;
         if (it / per != s) {  // first item of a strip in this range: tiles G-1 and G
             s = it / per;
-            ta = P.TA + (size_t)z * P.sstride + ((size_t)s * P.qn + kSkewFront) * 32;
-            tb = P.TB + (size_t)z * P.sstride + ((size_t)s * P.qn + kSkewFront) * 32;
-            ed = P.ED + (size_t)z * P.estride + (size_t)s * er + kEdgePad;
-            eu_next = (s + 1 < P.nstrips) ? P.EU + (size_t)z * P.estride + (size_t)(s + 1) * er + kEdgePad : nullptr;
+            ta = dst.a + ((size_t)s * P.qn + kSkewFront) * 32;
+            tb = dst.b + ((size_t)s * P.qn + kSkewFront) * 32;
+            ed = dst.ed ? dst.ed + (size_t)s * er + kEdgePad : nullptr;
+            eu_next = (dst.eu && s + 1 < P.nstrips) ? dst.eu + (size_t)(s + 1) * er + kEdgePad : nullptr;
             fence_proxy_async_smem();  // the slots' earlier generic reads precede the copies
             __syncwarp();
             if (l == 0) {
@@ -1068,7 +1168,7 @@ __device__ __noinline__ void relayout_items(const ShotParams &P, Warp &w, const 
             ta[(size_t)q * 32 + l] = va;
             tb[(size_t)q * 32 + l] = vb;
         }
-        if (G < nxb) {
+        if (G < nxb && ed) {
             ed[kBlk * G + l] = t_cur[32 * kBlk + l];                   // row 32s+32 (zero beyond the grid)
             if (eu_next) eu_next[kBlk * G + l] = t_cur[31 * kBlk + l];  // row 32(s+1)-1
         }
@@ -1081,71 +1181,118 @@ __device__ __noinline__ void relayout_items(const ShotParams &P, Warp &w, const 
 // the sweeps (x weights in TA/TB, z weights in WZA/WZB, those of the rows
 // bordering each strip in EU/ED), dJ/dT at the receiver cells (RA/RB, the
 // residuals of each cell's receivers summed in receiver order), mu = 0.
-// With refined traveltimes (P.refine) the weights are those of T + Told.
-// tangent: the traveltime refinement's system instead -- the weights of the
-// unrefined field and the residual r of every cell (cell_residual) in RA/RB.
-__device__ __noinline__ void exact_prepare(const ShotParams &P, int z, const float *T, float *L, bool tangent) {
+// tangent: the traveltime refinement's system instead -- the residual r of
+// every cell (cell_residual_nb) in RA/RB.
+//
+// The traveltimes are first skewed into TA/TB with their border rows in
+// EU/ED (relayout_items, as for the Leung-Qian adjoint).  A warp then walks
+// the lines of one strip and family in order: every neighbour of the cells
+// of line q lies on line q-1 or q+1 of the same family (the rows above and
+// below the strip in EU/ED), so each line is read once, coalesced, two lines
+// ahead, and the weights replace the traveltimes of line q once lines
+// q-1..q+1 are in registers.
+__device__ __noinline__ void exact_prepare(const ShotParams &P, Warp &w, const CUtensorMap *mld,
+                                           const CUtensorMap *mlo, int z, const float *T, float *L, bool tangent) {
     const int tid = threadIdx.x, nthr = blockDim.x;
     const int l = tid & 31, g = tid >> 5, W = nthr >> 5;
     const int hs = P.src_h[z], ks = P.src_k[z];
     const int nx = P.nx, ny = P.ny, nxp = P.nxp, qn = P.qn;
-    const size_t lines = (size_t)P.nstrips * qn;
-    float *wxa = P.TA + (size_t)z * P.sstride, *wxb = P.TB + (size_t)z * P.sstride;
-    float *wza = P.WZA + (size_t)z * P.sstride, *wzb = P.WZB + (size_t)z * P.sstride;
     float *ra = P.RA + (size_t)z * P.sstride, *rb = P.RB + (size_t)z * P.sstride;
-    // low parts of refined traveltimes (the adjoint after a refinement)
+    // low parts of refined traveltimes (the exact adjoint after a refinement):
+    // skewed into RA/RB, which the walk reads ahead of its writes
     const float *lo = (P.refine && !tangent) ? P.Told + (size_t)z * P.fstride : nullptr;
-    // U lines per warp and round: every load of the round is issued before
-    // any value is used (the prep is bound by memory latency)
-    constexpr int U = 4;
-    for (size_t li0 = g; li0 < lines; li0 += (size_t)U * W) {
-        CellNb na[U], nb[U];
-        float sa[U], sb[U];
-        bool ina[U], inb[U];
-        int ha[U], hb[U], row[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const size_t li = li0 + (size_t)u * W;
-            const int s = (int)(li / qn), q = (int)(li - (size_t)s * qn) - kSkewFront;
-            row[u] = kStrip * s + l;
-            ha[u] = q - l, hb[u] = q + l - 31;
-            const bool live = li < lines && row[u] < ny;
-            ina[u] = live && ha[u] >= 0 && ha[u] < nx;
-            inb[u] = live && hb[u] >= 0 && hb[u] < nx;
-            const size_t o = (li < lines ? li : 0) * 32 + l;
-            sa[u] = ina[u] ? __ldg(P.SA + o) : 0.f;
-            sb[u] = inb[u] ? __ldg(P.SB + o) : 0.f;
-            if (ina[u]) na[u] = load_cell_nb(T, lo, nxp, nx, ny, ha[u], row[u]);
-            if (inb[u]) nb[u] = load_cell_nb(T, lo, nxp, nx, ny, hb[u], row[u]);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-            const size_t li = li0 + (size_t)u * W;
-            if (li >= lines) break;
-            const size_t o = li * 32 + l;
-            ExactCoef ca{0.f, 0.f, 0.f}, cb{0.f, 0.f, 0.f};
-            float rva = 0.f, rvb = 0.f;
-            if (ina[u]) {
-                const bool src = ha[u] == hs && row[u] == ks;
-                ca = exact_coef_nb(na[u], sa[u], P.dh, src);
-                if (tangent) rva = cell_residual_nb(na[u], sa[u], P.dh, src);
+    {
+        const int items = P.nstrips * (P.nxb + 1);
+        const int per_warp = (items + W - 1) / W;
+        const int i0 = min(items, g * per_warp), i1 = min(items, (g + 1) * per_warp);
+        relayout_items(P, w, mld, i0, i1, skew_dst_t(P, z));
+        if (lo) relayout_items(P, w, mlo, i0, i1, SkewDst{ra, rb, nullptr, nullptr});
+    }
+    __syncthreads();
+    const float big = 3.0e38f;
+    const int er = edge_row(nxp);
+    // one warp per strip and family: the lines are rewritten in place in order
+    for (int walk = g; walk < 2 * P.nstrips; walk += W) {
+        const int s = walk >> 1;
+        const bool famA = (walk & 1) == 0;
+        const int row = kStrip * s + l;
+        float *tx = (famA ? P.TA : P.TB) + (size_t)z * P.sstride + (size_t)s * qn * 32 + l;
+        float *wz = (famA ? P.WZA : P.WZB) + (size_t)z * P.sstride + (size_t)s * qn * 32 + l;
+        float *rr = (famA ? ra : rb) + (size_t)s * qn * 32 + l;
+        const float *sl = (famA ? P.SA : P.SB) + (size_t)s * qn * 32 + l;
+        const float *eu = P.EU + (size_t)z * P.estride + (size_t)s * er + kEdgePad;
+        const float *ed = P.ED + (size_t)z * P.estride + (size_t)s * er + kEdgePad;
+        // the values of line qi: its traveltimes, slowness and (lanes 0 / 31)
+        // the traveltime of the row above / below the strip at the cell's column
+        auto col = [&](int qi) { return famA ? qi - kSkewFront - l : qi - kSkewFront + l - 31; };
+        auto load_edge = [&](int qi) -> float {
+            const int h = col(qi);
+            if (qi >= qn || h < 0 || h >= nx || row >= ny) return big;
+            if (l == 0) return row > 0 ? __ldcg(eu + h) : big;
+            if (l == 31) return row < ny - 1 ? __ldcg(ed + h) : big;
+            return big;
+        };
+        auto load_t = [&](int qi) { return qi < qn ? __ldcg(tx + (size_t)qi * 32) : 0.f; };
+        auto load_s = [&](int qi) { return qi < qn ? __ldg(sl + (size_t)qi * 32) : 0.f; };
+        // low parts: the line's from RA/RB, the border rows' from the field
+        auto load_lo = [&](int qi) { return lo && qi < qn ? __ldcg(rr + (size_t)qi * 32) : 0.f; };
+        auto load_lo_edge = [&](int qi) -> float {
+            const int h = col(qi);
+            if (!lo || qi >= qn || h < 0 || h >= nx || row >= ny) return 0.f;
+            if (l == 0) return row > 0 ? __ldcg(lo + (size_t)(row - 1) * nxp + h) : 0.f;
+            if (l == 31) return row < ny - 1 ? __ldcg(lo + (size_t)(row + 1) * nxp + h) : 0.f;
+            return 0.f;
+        };
+        float prev = 0.f, cur = load_t(0), next = load_t(1);
+        float s_cur = load_s(0), s_next = load_s(1);
+        float e_cur = load_edge(0), e_next = load_edge(1);
+        float lprev = 0.f, lcur = load_lo(0), lnext = load_lo(1);
+        float le_cur = load_lo_edge(0), le_next = load_lo_edge(1);
+        for (int qi = 0; qi < qn; ++qi) {
+            const float after = load_t(qi + 2), s_after = load_s(qi + 2), e_after = load_edge(qi + 2);
+            const float lafter = load_lo(qi + 2), le_after = load_lo_edge(qi + 2);
+            const int h = col(qi);
+            const bool valid = row < ny && h >= 0 && h < nx;
+            // north / south neighbours: family A lines q-1 / q+1 at positions
+            // j-1 / j+1, family B lines q+1 / q-1
+            const float up_src = famA ? prev : next, dn_src = famA ? next : prev;
+            float tn = __shfl_up_sync(0xffffffffu, up_src, 1);
+            float ts = __shfl_down_sync(0xffffffffu, dn_src, 1);
+            float ln = __shfl_up_sync(0xffffffffu, famA ? lprev : lnext, 1);
+            float ls = __shfl_down_sync(0xffffffffu, famA ? lnext : lprev, 1);
+            if (l == 0) tn = e_cur, ln = le_cur;
+            if (l == 31) ts = e_cur, ls = le_cur;
+            if (row == ny - 1) ts = big, ls = 0.f;
+            CellNb nbh;
+            nbh.tc = cur;
+            nbh.tw = h > 0 ? prev : big;
+            nbh.te = h < nx - 1 ? next : big;
+            nbh.tn = tn, nbh.ts = ts;
+            nbh.lw = h > 0 ? lprev : 0.f;
+            nbh.le = h < nx - 1 ? lnext : 0.f;
+            nbh.ln = ln, nbh.ls = ls;
+            ExactCoef c{0.f, 0.f, 0.f};
+            float r = 0.f;
+            if (valid) {
+                const bool src = h == hs && row == ks;
+                c = exact_coef_nb(nbh, s_cur, P.dh, src);
+                if (tangent) r = cell_residual_nb(nbh, s_cur, P.dh, src);
             }
-            if (inb[u]) {
-                const bool src = hb[u] == hs && row[u] == ks;
-                cb = exact_coef_nb(nb[u], sb[u], P.dh, src);
-                if (tangent) rvb = cell_residual_nb(nb[u], sb[u], P.dh, src);
-            }
-            wxa[o] = ca.wx;
-            wza[o] = ca.wz;
-            ra[o] = rva;
-            wxb[o] = cb.wx;
-            wzb[o] = cb.wz;
-            rb[o] = rvb;
+            // line qi is not read again: the window of the next lines holds it
+            tx[(size_t)qi * 32] = c.wx;
+            wz[(size_t)qi * 32] = c.wz;
+            rr[(size_t)qi * 32] = r;
+            prev = cur, cur = next, next = after;
+            s_cur = s_next, s_next = s_after;
+            e_cur = e_next, e_next = e_after;
+            lprev = lcur, lcur = lnext, lnext = lafter;
+            le_cur = le_next, le_next = le_after;
         }
     }
-    // z weights of the rows above (EU) and below (ED) each strip
-    const int er = edge_row(nxp);
-    for (int i = tid; i < P.nstrips * nxp; i += nthr) {
+    __syncthreads();
+    // z weights of the rows above (EU) and below (ED) each strip (the exact
+    // adjoint's sweeps read them; the refinement's use only a cell's own weights)
+    for (int i = tid; i < (tangent ? 0 : P.nstrips * nxp); i += nthr) {
         const int s = i / nxp, col = i - s * nxp;
         const int ru = kStrip * s - 1, rd = kStrip * s + kStrip;
         float vu = 0.f, vd = 0.f;
@@ -1352,7 +1499,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             // Told := the remainder, so T + Told is the refined field.
             __syncthreads();
             stamp(P, z, 7);
-            exact_prepare(P, z, T, L, true);
+            exact_prepare(P, w, pTld, &M.tlo, z, T, L, true);
             fence_proxy_async_global();
             __syncthreads();
             int tp = 0;
@@ -1372,6 +1519,12 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                 const double tot = block_sum((double)acc, sh);
                 const double m = block_sum((double)mag, sh);
                 more = tot > 1e-7 * m;
+                if (more && tp < P.max_passes) {
+                    // stop a pass early when the next would change no cell
+                    const int cv = tangent_is_converged(P, &M.tchk, &M.lchk, z, &sh.w[g], &sh.ctl[2], w.abort_word);
+                    w.err |= cv >> 1;
+                    if (cv & 1) more = false;
+                }
             }
             __syncthreads();
             split_refined(P, T, L, Told);
@@ -1465,12 +1618,12 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
         return;
     }
     if (P.exact) {
-        exact_prepare(P, z, T, L, false);
+        exact_prepare(P, w, pTld, &M.tlo, z, T, L, false);
     } else {
         {
             const int items = P.nstrips * (P.nxb + 1), Wb = (int)(blockDim.x >> 5);
             const int per_warp = (items + Wb - 1) / Wb;
-            relayout_items(P, w, pTld, min(items, g * per_warp), min(items, (g + 1) * per_warp));
+            relayout_items(P, w, pTld, min(items, g * per_warp), min(items, (g + 1) * per_warp), skew_dst_t(P, z));
         }
         // lambda: 0 on the frame, 10*TIME inside, residuals at receiver cells
         fill_field(P, L, (float)(10.0 * (double)P.time), true);

@@ -5,9 +5,11 @@ import os
 import numpy as np
 import pytest
 
+import oracle
 import rzio
 
-REF_PAR = "/root/reference/par"
+# the reference tree's example parameter files, beside its sources (absent on the GPU machine)
+REF_PAR = os.path.join(os.path.dirname(oracle.REF_SRC.rstrip("/")), "par")
 
 
 @pytest.fixture(scope="module")
