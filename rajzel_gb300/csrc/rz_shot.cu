@@ -32,6 +32,9 @@
 namespace rz {
 
 constexpr int kCheckSlots = 3;  // box slots in the ring of a fixpoint check
+// exact-adjoint / refinement preparation: lines a warp loads ahead, pieces
+// per walk at most, and units per warp whose boundary lines its ring holds
+constexpr int kWalkDepth = 8, kMaxPieces = 16, kMaxUnitsPerWarp = 24;
 
 // Read-only stream staging.  A sweep step reads per-cell values that no
 // shared-memory ring holds: the skewed slowness or traveltime line, and in
@@ -55,6 +58,7 @@ struct alignas(128) WarpShared {
     uint32_t cphase;                  // fixpoint check: expected parity per slot
 };
 static_assert(sizeof(WarpShared) % 128 == 0, "TMA destinations need 128-byte alignment");
+static_assert(kMaxUnitsPerWarp * 128 <= kRing * kSlotFloats, "the preparation's saved lines fit a warp's ring");
 static_assert(offsetof(WarpShared, hb) == sizeof(float) * kRing * kSlotFloats, "hb follows the ring");
 static_assert(offsetof(WarpShared, stage) == offsetof(WarpShared, hb) + sizeof(float) * kHandoff &&
                   offsetof(WarpShared, stage) % 16 == 0,
@@ -1211,84 +1215,137 @@ __device__ __noinline__ void exact_prepare(const ShotParams &P, Warp &w, const C
     __syncthreads();
     const float big = 3.0e38f;
     const int er = edge_row(nxp);
-    // one warp per strip and family: the lines are rewritten in place in order
-    for (int walk = g; walk < 2 * P.nstrips; walk += W) {
-        const int s = walk >> 1;
-        const bool famA = (walk & 1) == 0;
-        const int row = kStrip * s + l;
-        float *tx = (famA ? P.TA : P.TB) + (size_t)z * P.sstride + (size_t)s * qn * 32 + l;
-        float *wz = (famA ? P.WZA : P.WZB) + (size_t)z * P.sstride + (size_t)s * qn * 32 + l;
-        float *rr = (famA ? ra : rb) + (size_t)s * qn * 32 + l;
-        const float *sl = (famA ? P.SA : P.SB) + (size_t)s * qn * 32 + l;
-        const float *eu = P.EU + (size_t)z * P.estride + (size_t)s * er + kEdgePad;
-        const float *ed = P.ED + (size_t)z * P.estride + (size_t)s * er + kEdgePad;
-        // the values of line qi: its traveltimes, slowness and (lanes 0 / 31)
-        // the traveltime of the row above / below the strip at the cell's column
-        auto col = [&](int qi) { return famA ? qi - kSkewFront - l : qi - kSkewFront + l - 31; };
-        auto load_edge = [&](int qi) -> float {
-            const int h = col(qi);
-            if (qi >= qn || h < 0 || h >= nx || row >= ny) return big;
-            if (l == 0) return row > 0 ? __ldcg(eu + h) : big;
-            if (l == 31) return row < ny - 1 ? __ldcg(ed + h) : big;
-            return big;
-        };
-        auto load_t = [&](int qi) { return qi < qn ? __ldcg(tx + (size_t)qi * 32) : 0.f; };
-        auto load_s = [&](int qi) { return qi < qn ? __ldg(sl + (size_t)qi * 32) : 0.f; };
-        // low parts: the line's from RA/RB, the border rows' from the field
-        auto load_lo = [&](int qi) { return lo && qi < qn ? __ldcg(rr + (size_t)qi * 32) : 0.f; };
-        auto load_lo_edge = [&](int qi) -> float {
-            const int h = col(qi);
-            if (!lo || qi >= qn || h < 0 || h >= nx || row >= ny) return 0.f;
-            if (l == 0) return row > 0 ? __ldcg(lo + (size_t)(row - 1) * nxp + h) : 0.f;
-            if (l == 31) return row < ny - 1 ? __ldcg(lo + (size_t)(row + 1) * nxp + h) : 0.f;
-            return 0.f;
-        };
-        float prev = 0.f, cur = load_t(0), next = load_t(1);
-        float s_cur = load_s(0), s_next = load_s(1);
-        float e_cur = load_edge(0), e_next = load_edge(1);
-        float lprev = 0.f, lcur = load_lo(0), lnext = load_lo(1);
-        float le_cur = load_lo_edge(0), le_next = load_lo_edge(1);
-        for (int qi = 0; qi < qn; ++qi) {
-            const float after = load_t(qi + 2), s_after = load_s(qi + 2), e_after = load_edge(qi + 2);
-            const float lafter = load_lo(qi + 2), le_after = load_lo_edge(qi + 2);
-            const int h = col(qi);
-            const bool valid = row < ny && h >= 0 && h < nx;
-            // north / south neighbours: family A lines q-1 / q+1 at positions
-            // j-1 / j+1, family B lines q+1 / q-1
-            const float up_src = famA ? prev : next, dn_src = famA ? next : prev;
-            float tn = __shfl_up_sync(0xffffffffu, up_src, 1);
-            float ts = __shfl_down_sync(0xffffffffu, dn_src, 1);
-            float ln = __shfl_up_sync(0xffffffffu, famA ? lprev : lnext, 1);
-            float ls = __shfl_down_sync(0xffffffffu, famA ? lnext : lprev, 1);
-            if (l == 0) tn = e_cur, ln = le_cur;
-            if (l == 31) ts = e_cur, ls = le_cur;
-            if (row == ny - 1) ts = big, ls = 0.f;
-            CellNb nbh;
-            nbh.tc = cur;
-            nbh.tw = h > 0 ? prev : big;
-            nbh.te = h < nx - 1 ? next : big;
-            nbh.tn = tn, nbh.ts = ts;
-            nbh.lw = h > 0 ? lprev : 0.f;
-            nbh.le = h < nx - 1 ? lnext : 0.f;
-            nbh.ln = ln, nbh.ls = ls;
-            ExactCoef c{0.f, 0.f, 0.f};
-            float r = 0.f;
-            if (valid) {
-                const bool src = h == hs && row == ks;
-                c = exact_coef_nb(nbh, s_cur, P.dh, src);
-                if (tangent) r = cell_residual_nb(nbh, s_cur, P.dh, src);
-            }
-            // line qi is not read again: the window of the next lines holds it
-            tx[(size_t)qi * 32] = c.wx;
-            wz[(size_t)qi * 32] = c.wz;
-            rr[(size_t)qi * 32] = r;
-            prev = cur, cur = next, next = after;
-            s_cur = s_next, s_next = s_after;
-            e_cur = e_next, e_next = e_after;
-            lprev = lcur, lcur = lnext, lnext = lafter;
-            le_cur = le_next, le_next = le_after;
+    // Work units: piece p of the walk over strip s, family f (lines [q0, q1)),
+    // unit u = (2 s + f) * npc + p; warp g takes units g, g + W, ...  Pieces
+    // rewrite disjoint lines in place, so the two lines just outside each
+    // piece (q0 - 1 and q1: its neighbours' first and last lines) are saved
+    // to the warp's ring first, before any piece writes.  npc is the piece
+    // count per walk that needs the fewest rounds of the slowest warp.
+    const int nwalk = 2 * P.nstrips;
+    int npc = 1;
+    {
+        float best = 3.0e38f;
+        for (int c = 1; c <= kMaxPieces; ++c) {
+            const int per_warp = (nwalk * c + W - 1) / W;
+            const float cost = (float)per_warp / (float)c;  // rounds x lines per piece
+            if (per_warp <= kMaxUnitsPerWarp && cost < best * 0.999f) best = cost, npc = c;
         }
     }
+    const int plen = (qn + npc - 1) / npc, nunit = nwalk * npc;
+    float *sv_ = &w.ws->ring[0][0];  // [unit of this warp][4][32]: T and lo of lines q0-1 and q1
+    auto unit_geom = [&](int u, int &s_, bool &fa, int &q0, int &q1) {
+        const int wk = u / npc, pc = u - wk * npc;
+        s_ = wk >> 1, fa = (wk & 1) == 0;
+        q0 = min(qn, pc * plen), q1 = min(qn, q0 + plen);
+    };
+    auto line_ptr = [&](float *base_A, float *base_B, bool fa, int s_) {
+        return (fa ? base_A : base_B) + (size_t)s_ * qn * 32 + l;
+    };
+    float *const TAz = P.TA + (size_t)z * P.sstride, *const TBz = P.TB + (size_t)z * P.sstride;
+    for (int u = g, ui = 0; npc > 1 && u < nunit; u += W, ++ui) {
+        int s_, q0, q1;
+        bool fa;
+        unit_geom(u, s_, fa, q0, q1);
+        const float *tx = line_ptr(TAz, TBz, fa, s_);
+        const float *rl = line_ptr(ra, rb, fa, s_);
+        float *b = sv_ + ui * 128 + l;
+        b[0] = q0 > 0 ? __ldcg(tx + (size_t)(q0 - 1) * 32) : 0.f;
+        b[32] = (lo && q0 > 0) ? __ldcg(rl + (size_t)(q0 - 1) * 32) : 0.f;
+        b[64] = q1 < qn ? __ldcg(tx + (size_t)q1 * 32) : 0.f;
+        b[96] = (lo && q1 < qn) ? __ldcg(rl + (size_t)q1 * 32) : 0.f;
+    }
+    __syncthreads();
+    for (int u = g, ui = 0; u < nunit; u += W, ++ui) {
+        int s_, q0, q1;
+        bool famA;
+        unit_geom(u, s_, famA, q0, q1);
+        const int row = kStrip * s_ + l;
+        float *tx = line_ptr(TAz, TBz, famA, s_);
+        float *wz = line_ptr(P.WZA + (size_t)z * P.sstride, P.WZB + (size_t)z * P.sstride, famA, s_);
+        float *rr = line_ptr(ra, rb, famA, s_);
+        const float *sl = (famA ? P.SA : P.SB) + (size_t)s_ * qn * 32 + l;
+        const float *eu = P.EU + (size_t)z * P.estride + (size_t)s_ * er + kEdgePad;
+        const float *ed = P.ED + (size_t)z * P.estride + (size_t)s_ * er + kEdgePad;
+        const float *bnd = sv_ + ui * 128 + l;
+        auto col = [&](int qi) { return famA ? qi - kSkewFront - l : qi - kSkewFront + l - 31; };
+        // line qi of the unit's window: its traveltime, slowness, low part and
+        // (lanes 0 / 31) the traveltime and low part of the row above / below
+        // the strip at the cell's column.  Lines of this piece come from
+        // global memory (read before this warp rewrites them), line q1 from
+        // the saved copy, lines past q1 are not needed.
+        struct Line {
+            float t, s, e, lo, le;
+        };
+        auto load_line = [&](int qi) -> Line {
+            Line v{0.f, 0.f, big, 0.f, 0.f};
+            if (qi >= q1 + 1 || qi >= qn) return v;
+            if (qi == q1) {
+                v.t = bnd[64], v.lo = bnd[96];
+            } else {
+                v.t = __ldcg(tx + (size_t)qi * 32);
+                if (lo) v.lo = __ldcg(rr + (size_t)qi * 32);
+            }
+            v.s = __ldg(sl + (size_t)qi * 32);
+            const int h = col(qi);
+            if (h >= 0 && h < nx && row < ny && (l == 0 || l == 31)) {
+                const int rn = l == 0 ? row - 1 : row + 1;
+                if (rn >= 0 && rn < ny) {
+                    v.e = __ldcg((l == 0 ? eu : ed) + h);
+                    if (lo) v.le = __ldcg(lo + (size_t)rn * nxp + h);
+                }
+            }
+            return v;
+        };
+        // a window of D lines in registers: line qi + D replaces line qi once
+        // line qi is done (line qi + 1 is then in the next slot, or in slot 0
+        // when qi ends a round)
+        constexpr int D = kWalkDepth;
+        Line win[D];
+#pragma unroll
+        for (int i = 0; i < D; ++i) win[i] = load_line(q0 + i);
+        float prev = q0 > 0 ? bnd[0] : 0.f, lprev = q0 > 0 ? bnd[32] : 0.f;  // q0 > 0 only with npc > 1
+        for (int qb = q0; qb < q1; qb += D) {
+#pragma unroll
+            for (int i = 0; i < D; ++i) {
+                const int qi = qb + i;
+                if (qi >= q1) break;  // warp-uniform
+                const Line c = win[i];
+                const float next = win[(i + 1) % D].t, lnext = win[(i + 1) % D].lo;
+                const int h = col(qi);
+                const bool valid = row < ny && h >= 0 && h < nx;
+                // north / south neighbours: family A lines q-1 / q+1 at positions
+                // j-1 / j+1, family B lines q+1 / q-1
+                float tn = __shfl_up_sync(0xffffffffu, famA ? prev : next, 1);
+                float ts = __shfl_down_sync(0xffffffffu, famA ? next : prev, 1);
+                float ln = __shfl_up_sync(0xffffffffu, famA ? lprev : lnext, 1);
+                float ls = __shfl_down_sync(0xffffffffu, famA ? lnext : lprev, 1);
+                if (l == 0) tn = c.e, ln = c.le;
+                if (l == 31) ts = c.e, ls = c.le;
+                if (row == ny - 1) ts = big, ls = 0.f;
+                CellNb nbh;
+                nbh.tc = c.t;
+                nbh.tw = h > 0 ? prev : big;
+                nbh.te = h < nx - 1 ? next : big;
+                nbh.tn = tn, nbh.ts = ts;
+                nbh.lw = h > 0 ? lprev : 0.f;
+                nbh.le = h < nx - 1 ? lnext : 0.f;
+                nbh.ln = ln, nbh.ls = ls;
+                ExactCoef cf{0.f, 0.f, 0.f};
+                float r = 0.f;
+                if (valid) {
+                    const bool src = h == hs && row == ks;
+                    cf = exact_coef_nb(nbh, c.s, P.dh, src);
+                    if (tangent) r = cell_residual_nb(nbh, c.s, P.dh, src);
+                }
+                win[i] = load_line(qi + D);  // read before line qi is rewritten (qi + D > qi)
+                tx[(size_t)qi * 32] = cf.wx;
+                wz[(size_t)qi * 32] = cf.wz;
+                rr[(size_t)qi * 32] = r;
+                prev = c.t, lprev = c.lo;
+            }
+        }
+    }
+    fence_proxy_async_smem();  // the saved lines (generic writes) precede later copies into the rings
     __syncthreads();
     // z weights of the rows above (EU) and below (ED) each strip (the exact
     // adjoint's sweeps read them; the refinement's use only a cell's own weights)
@@ -1649,7 +1706,35 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             __syncthreads();
         }
         float acc = 0.f, mag = 0.f;
-        if (P.exact) {
+        bool sweep_stop = false;  // exact adjoint: a sweep of a later pass changed mu by < 1e-7 of |mu|
+        if (P.exact && pass > 0) {
+            // After the first pass, one sweep at a time: a sweep visits every
+            // cell, so a sweep that changes no cell proves the fixpoint (its
+            // updates all saw the final values), and one that changes mu by
+            // less than 1e-7 of its magnitude bounds every cell's residual as
+            // a pass of such sweeps would; the remaining sweeps of the pass
+            // are left out.
+            auto sweep_small = [&]() {
+                if (seq.pipelined) __syncthreads();
+                const double t = block_sum((double)acc, sh), m = block_sum((double)mag, sh);
+                acc = 0.f, mag = 0.f;
+                return !(t > 1e-7 * m);
+            };
+            RZ_SWEEP(+1, +1, true, kModeExact, &M.lld, &M.lst);
+            sweep_stop = sweep_small();
+            if (!sweep_stop) {
+                RZ_SWEEP(+1, -1, true, kModeExact, &M.lld, &M.lst);
+                sweep_stop = sweep_small();
+            }
+            if (!sweep_stop) {
+                RZ_SWEEP(-1, +1, true, kModeExact, &M.lld, &M.lst);
+                sweep_stop = sweep_small();
+            }
+            if (!sweep_stop) {
+                RZ_SWEEP(-1, -1, true, kModeExact, &M.lld, &M.lst);
+                sweep_stop = sweep_small();
+            }
+        } else if (P.exact) {
             // same four orderings as the Leung-Qian sweeps (eikonal_adj.c:43-46)
             RZ_SWEEP(+1, +1, true, kModeExact, &M.lld, &M.lst);
             if (pass == 0) stamp(P, z, 6);
@@ -1673,7 +1758,9 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
         ++pass;
         ++swept;
         if (*w.abort_word) break;
-        if (P.exact) {
+        if (P.exact && pass > 1) {
+            go = !sweep_stop;
+        } else if (P.exact) {
             // the adjoint system is triangular in arrival order: Gauss-Seidel
             // sweeps reach its solution exactly; stop once a pass changes it
             // by less than 1e-7 of its magnitude
