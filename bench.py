@@ -231,12 +231,12 @@ def run_gpu_arm(args, rank, world, local_rank):
     torch.cuda.synchronize()
     # passes and point-updates of one step (identical every step: same inputs)
     passes = np.array([ctx.shot_info(i)[:2] for i in range(w.nshots)])
-    swept = np.array([ctx.shot_work(i) for i in range(w.nshots)])
+    sweeps = np.array([ctx.shot_work(i) for i in range(w.nshots)])
     # point-updates actually performed (a pass proven by the fixpoint check to
     # change nothing is counted by the reference's rule but not swept)
-    pu_fwd = int(swept[:, 0].sum()) * 4 * w.nx * w.ny
-    pu_adj = int(swept[:, 1].sum()) * 4 * (w.nx - 2) * (w.ny - 2)
-    checks = (passes - swept).sum(axis=0)  # successful fixpoint checks (forward, adjoint)
+    pu_fwd = int(sweeps[:, 0].sum()) * w.nx * w.ny
+    pu_adj = int(sweeps[:, 1].sum()) * (w.nx - 2) * (w.ny - 2)
+    checks = (passes - (sweeps + 3) // 4).sum(axis=0)  # successful fixpoint checks (forward, adjoint)
     launches0, _, _ = ctx.kernel_stats()  # also clears the per-launch timing list
 
     clocks = ClockSampler(local_rank)
@@ -345,7 +345,7 @@ def run_gpu_arm(args, rank, world, local_rank):
         "point_updates_per_s": world * (pu_fwd + pu_adj) * args.steps / (ms / 1e3),
         "point_updates_per_step": pu_fwd + pu_adj,
         "passes_fwd_adj": [int(passes[:, 0].sum()), int(passes[:, 1].sum())],
-        "passes_swept_fwd_adj": [int(swept[:, 0].sum()), int(swept[:, 1].sum())],
+        "sweeps_fwd_adj": [int(sweeps[:, 0].sum()), int(sweeps[:, 1].sum())],
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                      "frac": achieved / hbm_peak, "peak_source": peak_src,
                      "traffic": traffic,
@@ -403,19 +403,19 @@ def time_mode(R, w, Tobs, stream, dev, mode, kind, steps, warmup, hbm_peak, peak
     bits = ctx.batch_status()
     if bits:
         raise SystemExit(f"{mode}/{kind}: device status bits 0x{bits:x}")
-    swept = np.array([ctx.shot_work(i) for i in range(w.nshots)])
+    sweeps = np.array([ctx.shot_work(i) for i in range(w.nshots)])
     passes = np.array([ctx.shot_info(i)[:2] for i in range(w.nshots)])
-    checks = (passes - swept).sum(axis=0)
+    checks = (passes - (sweeps + 3) // 4).sum(axis=0)  # passes proven by a fixpoint check, not swept
     adj_bytes = ALG_BYTES_EXACT_ADJ if kind == "exact" else ALG_BYTES_ADJ
-    pu_fwd = int(swept[:, 0].sum()) * 4 * w.nx * w.ny
-    pu_adj = int(swept[:, 1].sum()) * 4 * (w.nx * w.ny if kind == "exact" else (w.nx - 2) * (w.ny - 2))
+    pu_fwd = int(sweeps[:, 0].sum()) * w.nx * w.ny
+    pu_adj = int(sweeps[:, 1].sum()) * (w.nx * w.ny if kind == "exact" else (w.nx - 2) * (w.ny - 2))
     alg = (pu_fwd * ALG_BYTES_FWD + pu_adj * adj_bytes + int(checks[0]) * CHECK_BYTES_FWD * w.nx * w.ny
            + int(checks[1]) * CHECK_BYTES_ADJ * (w.nx - 2) * (w.ny - 2))
     kernel_ms = shot_ms / max(calls, 1)
     achieved = alg / (kernel_ms / 1e3) / 1e9
     return {"mode": mode, "gradient": kind, "refined": refine, "value": w.nshots / (ms / 1e3), "unit": "shots/s",
             "ms_per_step": ms,
-            "steps": steps, "passes_swept_fwd_adj": [int(swept[:, 0].sum()), int(swept[:, 1].sum())],
+            "steps": steps, "sweeps_fwd_adj": [int(sweeps[:, 0].sum()), int(sweeps[:, 1].sum())],
             "point_updates_per_s": (pu_fwd + pu_adj) / (ms / 1e3),
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm_peak, "unit": "GB/s",
                          "frac": achieved / hbm_peak, "peak_source": peak_src, "kernel_ms": kernel_ms,
@@ -578,8 +578,8 @@ def run_workload(args, local_rank):
             ms_i = _events_ms(lambda: launch(i), streams[i], max(1, args.steps // 2))
             sw = np.array([ctxs[i].shot_work(s) for s in range(w.nshots)]).sum(axis=0)
             per_grid.append({"grid": [w.nx, w.ny], "shots": w.nshots, "ms": ms_i,
-                             "passes_swept_fwd_adj": [int(sw[0]), int(sw[1])],
-                             "point_updates": 4 * (int(sw[0]) * w.nx * w.ny + int(sw[1]) * (w.nx - 2) * (w.ny - 2))})
+                             "sweeps_fwd_adj": [int(sw[0]), int(sw[1])],
+                             "point_updates": int(sw[0]) * w.nx * w.ny + int(sw[1]) * (w.nx - 2) * (w.ny - 2)})
         nsh = sum(w.nshots for w in grids)
         pu = sum(g["point_updates"] for g in per_grid)
         cores = os.cpu_count() or 1
@@ -615,7 +615,7 @@ def run_workload(args, local_rank):
         pf = sum(ctx.shot_info(s)[0] for s in range(w.nshots))
         pa = sum(ctx.shot_info(s)[1] for s in range(w.nshots))
         sw = np.array([ctx.shot_work(s) for s in range(w.nshots)]).sum(axis=0)
-        pu = 4 * (int(sw[0]) * w.nx * w.ny + int(sw[1]) * (w.nx - 2) * (w.ny - 2))  # swept passes only
+        pu = int(sw[0]) * w.nx * w.ny + int(sw[1]) * (w.nx - 2) * (w.ny - 2)  # sweeps actually run
         cores = os.cpu_count() or 1
         kind = cpu_kind()
         cpu_s = cpu_run(cores, cores, kind, "stress", w.nshots)
@@ -623,7 +623,7 @@ def run_workload(args, local_rank):
                                "sample": "grad_obj of one shot per core (the first shots of the 1024)"}
         out.update({"metric": "fwd+adjoint shots/s", "value": w.nshots / (ms / 1e3), "unit": "shots/s",
                     "higher_is_better": True, "ms_per_step": ms, "shots": w.nshots,
-                    "forward_only_s": fwd_s, "passes_fwd_adj": [pf, pa], "passes_swept_fwd_adj": [int(sw[0]), int(sw[1])],
+                    "forward_only_s": fwd_s, "passes_fwd_adj": [pf, pa], "sweeps_fwd_adj": [int(sw[0]), int(sw[1])],
                     "point_updates_per_s": pu / (ms / 1e3), "memory_cap_bytes": 120 << 30,
                     "peak_allocated_note": "field slots sized to the cap, chunks of a multiple of the SM count"})
     elif args.workload == "fatt":

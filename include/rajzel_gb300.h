@@ -321,9 +321,12 @@ int rz_status_code(int bits);
    (this call waits for the context stream). */
 int rz_batch_status(rz_context *ctx, int *bits);
 
-/* Passes of shot `shot` in the last batch that were actually swept.  A pass
-   that a parallel fixpoint check proves to change no cell is counted in
-   rz_shot_info's pass counts (the reference runs it) but not swept. */
+/* Directional sweeps of shot `shot` in the last batch that were actually
+   run (forward, adjoint): 4 per swept pass.  A pass that a parallel fixpoint
+   check proves to change no cell is counted in rz_shot_info's pass counts
+   (the reference runs it) but not swept; after its first pass the exact
+   adjoint stops at the first sweep that changes mu by less than 1e-7 of its
+   magnitude, so its count need not be a multiple of 4. */
 int rz_shot_work(rz_context *ctx, int shot, int *fwd_swept, int *adj_swept);
 
 /* Fields of shot `shot` from the last rz_grad_obj: TT, lambda [ny][nx],

@@ -422,7 +422,7 @@ class Context:
         return a.value, b.value, s.value
 
     def shot_work(self, shot):
-        """(forward, adjoint) passes actually swept for one shot of the last batch."""
+        """(forward, adjoint) directional sweeps actually run for one shot of the last batch."""
         a, b = C.c_int(0), C.c_int(0)
         self._check(self.lib.rz_shot_work(self.h, int(shot), C.byref(a), C.byref(b)), "rz_shot_work")
         return a.value, b.value

@@ -1528,7 +1528,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             RZ_SWEEP(+1, -1, false, MODE, pTld, &M.tst);
             if (seq.pipelined) __syncthreads();
             ++pass;
-            ++swept;
+            swept += 4;  // directional sweeps
             if (*w.abort_word) break;
             if (MODE == kModeReference) {
                 go = ref_continue(P, T, Told, sh);
@@ -1707,6 +1707,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
         }
         float acc = 0.f, mag = 0.f;
         bool sweep_stop = false;  // exact adjoint: a sweep of a later pass changed mu by < 1e-7 of |mu|
+        int nsweeps = 4;          // sweeps this pass runs
         if (P.exact && pass > 0) {
             // After the first pass, one sweep at a time: a sweep visits every
             // cell, so a sweep that changes no cell proves the fixpoint (its
@@ -1720,17 +1721,21 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                 acc = 0.f, mag = 0.f;
                 return !(t > 1e-7 * m);
             };
+            nsweeps = 1;
             RZ_SWEEP(+1, +1, true, kModeExact, &M.lld, &M.lst);
             sweep_stop = sweep_small();
             if (!sweep_stop) {
+                ++nsweeps;
                 RZ_SWEEP(+1, -1, true, kModeExact, &M.lld, &M.lst);
                 sweep_stop = sweep_small();
             }
             if (!sweep_stop) {
+                ++nsweeps;
                 RZ_SWEEP(-1, +1, true, kModeExact, &M.lld, &M.lst);
                 sweep_stop = sweep_small();
             }
             if (!sweep_stop) {
+                ++nsweeps;
                 RZ_SWEEP(-1, -1, true, kModeExact, &M.lld, &M.lst);
                 sweep_stop = sweep_small();
             }
@@ -1756,7 +1761,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
         }
         if (seq.pipelined) __syncthreads();
         ++pass;
-        ++swept;
+        swept += nsweeps;
         if (*w.abort_word) break;
         if (P.exact && pass > 1) {
             go = !sweep_stop;
