@@ -495,7 +495,8 @@ def run_workload(args, local_rank):
     """fwd_500x174: one forward solve (latency); uneven: 256 shots over three
     grids, forward + adjoint gradient; stress: 1024 shots on 8192 x 2048
     under a 120 GB cap on the field slots; fatt: 30 l-BFGS iterations, 200
-    shots x 1000 receivers on 2000 x 500."""
+    shots x 1000 receivers on 2000 x 500; phases: per-shot phase times of
+    every gradient path on the benchmark batch."""
     import numpy as np
     import torch
     import rajzel_gb300 as R
@@ -532,6 +533,39 @@ def run_workload(args, local_rank):
                     "passes": passes, "point_updates_per_s": passes * 4 * w.nx * w.ny / (ms / 1e3),
                     "cpu_baseline": {"value": cpu_ms, "unit": "ms", "cores": 1, "kind": "port",
                                      "sample": "the same solve, one core (the reference solves a shot on one rank)"}})
+    elif args.workload == "phases":
+        # where a shot's time goes on each gradient path of the benchmark batch:
+        # medians over the 100 shots of the shot kernel's device clock stamps
+        # (rz_shot_timeline: 0 start, 7 refinement start, 1 forward done,
+        # 2 residuals, 3 adjoint prepared, 4 adjoint done)
+        w = synth.grad_1700x350(nshots=100)
+        ctx = _context(R, w, "fast", stream, w.vp_true)
+        _, Tobs, _ = ctx.forward(w.srcx, w.srcz, want_tt=False)
+        tobs_d = torch.from_numpy(np.ascontiguousarray(Tobs)).cuda()
+        paths = {}
+        for mode, kind, refine in [("fast", "reference", False), ("reference", "reference", False),
+                                   ("fast", "exact", False), ("fast", "reference", True), ("fast", "exact", True)]:
+            c = _context(R, w, mode, stream, w.vp_start)
+            c.set_gradient(kind)
+            c.set_refine(refine)
+            g = torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda")
+            l2 = torch.empty(1, dtype=torch.float64, device="cuda")
+            step = lambda: c.grad_obj_device(w.srcx, w.srcz, tobs_d.data_ptr(), g.data_ptr(), l2.data_ptr())  # noqa
+            for _ in range(max(args.warmup, 3)):
+                step()
+            ms = _events_ms(step, stream, args.steps)
+            if c.batch_status():
+                raise SystemExit(f"{mode}/{kind}: device status bits 0x{c.batch_status():x}")
+            st = np.array([c.shot_timeline(i) for i in range(w.nshots)], dtype=np.float64)
+            med = lambda a, b: float(np.median(st[:, b] - st[:, a]) / 1e3)  # noqa: E731
+            sw = np.array([c.shot_work(i) for i in range(w.nshots)]).mean(axis=0)
+            paths[f"{mode} arithmetic, {'exact' if kind == 'exact' else 'Leung-Qian'} gradient"
+                  + (", refined traveltimes" if refine else "")] = {
+                "ms_per_step": ms, "shots_per_s": w.nshots / (ms / 1e3),
+                "us_per_shot": {"forward": med(0, 7 if refine else 1), "refinement": med(7, 1) if refine else 0.0,
+                                "residuals": med(1, 2), "adjoint_preparation": med(2, 3), "adjoint": med(3, 4)},
+                "sweeps_per_shot_fwd_adj": sw.tolist()}
+        out.update({"metric": "per-shot phase times (median over the batch)", "paths": paths, "shots": w.nshots})
     elif args.workload == "uneven":
         grids = [synth.uneven_grid(i) for i in range(3)]
         ctxs, bufs, streams = [], [], []
@@ -709,7 +743,7 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--mode", choices=["fast", "reference"], default="fast")
     ap.add_argument("--shots", type=int, default=100, help="shots per step (the workload has 100)")
-    ap.add_argument("--workload", choices=["grad_1700x350", "fwd_500x174", "uneven", "stress", "fatt"],
+    ap.add_argument("--workload", choices=["grad_1700x350", "fwd_500x174", "uneven", "stress", "fatt", "phases"],
                     default="grad_1700x350", help="the benchmark workload (default) or another named one")
     ap.add_argument("--no-ref-run", action="store_true", help="fatt: skip the reference-arithmetic comparison run")
     ap.add_argument("--profile-only", action="store_true",
