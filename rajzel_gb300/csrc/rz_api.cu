@@ -77,7 +77,7 @@ struct rz_context {
     float *dT = nullptr, *dTold = nullptr, *dL = nullptr, *dTA = nullptr, *dTB = nullptr, *dEU = nullptr,
           *dED = nullptr;
     uint8_t *dChg = nullptr;  // [slot][nstrips][4*(nxb+1)] change votes of a pass's last sweep
-    float *dWZA = nullptr, *dWZB = nullptr, *dRA = nullptr, *dRB = nullptr;  // exact adjoint only
+    float *dRA = nullptr, *dRB = nullptr;  // exact adjoint and refinement only
     bool fields_exact = false;
     ShotMaps maps{};  // tensor maps of the field buffers and the row-pitched slowness
     int grad_kind = RZ_GRADIENT_REFERENCE;
@@ -239,7 +239,7 @@ static int make_map(rz_context *c, CUtensorMap *m, float *base, int depth, int b
 static void free_fields(rz_context *c) {
     dfree(c->dT), dfree(c->dTold), dfree(c->dL), dfree(c->dTA), dfree(c->dTB), dfree(c->dEU), dfree(c->dED);
     dfree(c->dChg);
-    dfree(c->dWZA), dfree(c->dWZB), dfree(c->dRA), dfree(c->dRB);
+    dfree(c->dRA), dfree(c->dRB);
     c->fields_exact = false;
     c->cap_f = 0;
 }
@@ -267,11 +267,12 @@ static void free_batch(rz_context *c) {
 }
 
 // device bytes of one field slot: T, pass snapshot, lambda, two skewed T copies, border rows,
-// change votes (the exact adjoint adds skewed z weights and receiver terms, two copies each)
+// change votes (the exact adjoint and the refinement add skewed receiver terms or residuals,
+// two copies; their packed weights take the skewed T copies' place)
 static size_t slot_bytes(const rz_context *c) {
     const size_t fs = (size_t)c->g.ny * c->nxp, ss = (size_t)c->nstrips * c->qn * 32,
                  es = (size_t)c->nstrips * edge_row(c->nxp);
-    const size_t extra = (c->grad_kind == RZ_GRADIENT_EXACT || c->refine) ? 4 * ss : 0;
+    const size_t extra = (c->grad_kind == RZ_GRADIENT_EXACT || c->refine) ? 2 * ss : 0;
     return 4 * (3 * fs + 2 * ss + 2 * es + extra) + (size_t)c->nstrips * 4 * (c->nxb + 1);  // + change votes
 }
 
@@ -293,8 +294,6 @@ static int ensure_fields(rz_context *c, int n) {
     CK(cudaMemsetAsync(c->dEU, 0, es * n * 4, c->st));
     CK(cudaMemsetAsync(c->dED, 0, es * n * 4, c->st));
     if (exact) {
-        CK(dalloc(&c->dWZA, ss * n));
-        CK(dalloc(&c->dWZB, ss * n));
         CK(dalloc(&c->dRA, ss * n));
         CK(dalloc(&c->dRB, ss * n));
         c->fields_exact = true;
@@ -450,8 +449,6 @@ static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     P.xcell_k = c->dXcK;
     P.xcell_off = c->dXcOff;
     P.xcell_rec = c->dXcRec;
-    P.WZA = c->dWZA;
-    P.WZB = c->dWZB;
     P.RA = c->dRA;
     P.RB = c->dRB;
     P.Tobs = c->dTobs + (size_t)first * c->ntr;

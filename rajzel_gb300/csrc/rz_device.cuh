@@ -386,6 +386,33 @@ struct ExactCoef {
     float wx, wz, gs;
 };
 
+// A cell's two weights in one float, for the skewed weight streams.  Every
+// cell with an upwind neighbour has |wx| + |wz| = 1 (one-sided: 1 and 0;
+// two-sided: (r-d)/2r and (r+d)/2r), so the smaller magnitude is stored and
+// the larger is 1 minus it: the sign bit is the x direction (set: west),
+// significand bit 0 the z direction (set: south), bit 1 whether the stored
+// magnitude is |wz|; those two bits cost at most 2 ulp of the smaller weight.
+// 2.0 marks a cell with no upwind neighbour (the source, cells outside the
+// grid).
+RZ_DEV float pack_weights(const ExactCoef &c) {
+    if (c.wx == 0.f && c.wz == 0.f) return 2.0f;
+    const float ax = fabsf(c.wx), az = fabsf(c.wz);
+    const bool z_small = az < ax;
+    uint32_t b = __float_as_uint(z_small ? az : ax) & ~3u;
+    b |= (c.wz > 0.f ? 1u : 0u) | (z_small ? 2u : 0u) | (c.wx < 0.f ? 0x80000000u : 0u);
+    return __uint_as_float(b);
+}
+RZ_DEV void unpack_weights(float p, float &wx, float &wz) {
+    const uint32_t b = __float_as_uint(p);
+    const float a = __uint_as_float(b & 0x7ffffffcu);
+    const bool none = a > 1.5f;
+    const float big = 1.0f - a;
+    float ax = (b & 2u) ? big : a, az = (b & 2u) ? a : big;
+    ax = none ? 0.f : ax, az = none ? 0.f : az;
+    wx = (b >> 31) ? -ax : ax;
+    wz = (b & 1u) ? az : -az;
+}
+
 // The values one cell's linearisation reads: its traveltime and those of its
 // four neighbours (3e38 for a missing one) and, for refined traveltimes, the
 // neighbours' low parts.  Loading them apart from the arithmetic lets a

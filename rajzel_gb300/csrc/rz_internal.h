@@ -75,7 +75,6 @@ struct ShotParams {
                             // (exact adjoint: signed x weights, see exact_coef)
     float *EU, *ED;         // rows above / below each strip [nshots][nstrips][edge_row(nxp)]
                             // (exact adjoint: their signed z weights)
-    float *WZA, *WZB;       // exact adjoint: skewed signed z weights, like TA/TB
     float *RA, *RB;         // exact adjoint: skewed dJ/dT at receiver cells, like TA/TB
     size_t fstride;         // ny*nxp
     size_t sstride;         // nstrips*qn*32

@@ -293,7 +293,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     constexpr int QOFF = ADJ ? 1 : 0;    // the adjoint streams the downstream traveltime
     const float *xs;
     const uint32_t *mk = nullptr;
-    const float *zs = nullptr, *rs = nullptr;  // exact adjoint: z weights (one column ahead), own-cell R
+    const float *rs = nullptr;  // linear sweeps: own-cell R (the x stream holds packed weights, one column ahead)
     const float *ewin0 = nullptr, *ewin31 = nullptr;  // adjoint: edge values of group 0 for lanes 0 / 31
     {
         const int q0 = (DX > 0 ? 0 : ncol + 30) + QS * QOFF + kSkewFront;
@@ -301,10 +301,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
             xs = (famA ? P.SA : P.SB) + ((size_t)s * P.qn + q0) * 32 + j;
         } else {
             xs = (famA ? P.TA : P.TB) + (size_t)z * P.sstride + ((size_t)s * P.qn + q0) * 32 + j;
-            if (EX) {
-                zs = (famA ? P.WZA : P.WZB) + (size_t)z * P.sstride + ((size_t)s * P.qn + q0) * 32 + j;
-                rs = (famA ? P.RA : P.RB) + (size_t)z * P.sstride + ((size_t)s * P.qn + (q0 - QS)) * 32 + j;
-            }
+            if (EX) rs = (famA ? P.RA : P.RB) + (size_t)z * P.sstride + ((size_t)s * P.qn + (q0 - QS)) * 32 + j;
             mk = (famA ? P.MA : P.MB) + (size_t)s * P.qn + (q0 - QS * QOFF);
             // lane 0 takes its north neighbour's (dy > 0) traveltime and lambda
             // from the row above the strip, lane 31 its south one's from the row
@@ -344,19 +341,15 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     float xq[8];
     uint32_t mq[8];
     float eq[8];
-    float zq[8], rq[8];
+    float rq[8];
 #pragma unroll
-    for (int i = 0; i < 8; ++i) {
-        if (EX) {
-            zq[i] = __ldca(zs + QS * 32 * i);
-            rq[i] = __ldca(rs + QS * 32 * i);
-        }
-    }
+    for (int i = 0; i < 8; ++i)
+        if (EX) rq[i] = __ldca(rs + QS * 32 * i);
     stage_issue(0);
     float c_tt = 0.f, w_tt = 0.f;  // exact adjoint: x weights of this and the previous column
     float c_wz = 0.f, w_wz = 0.f;  // exact adjoint: z weights of this and the previous column
-    if (ADJ) c_tt = __ldca(xs - QS * 32);
-    if (EX) c_wz = __ldca(zs - QS * 32);
+    if (ADJ && !EX) c_tt = __ldca(xs - QS * 32);
+    if (EX) unpack_weights(__ldca(xs - QS * 32), c_tt, c_wz);
 
     issue(0);
     if (nxb > 1) issue(1);
@@ -480,7 +473,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 if (G + 1 < ngroups) stage_issue(G + 1);
             }
             const int u0 = t0 - l;
-            const float *zr = EX ? zs + QS * 32 * t0 : nullptr;
             const float *rr = EX ? rs + QS * 32 * t0 : nullptr;
             // ---- 8 wavefront steps, straight-line code.  In an interior group
             // (every lane's 8 columns strictly inside the grid, every row of the
@@ -538,12 +530,11 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     r = fminf(own, tt);
                     r = valid ? r : own;
                 } else if (EX) {
-                    const float e_wz = zq[ii];
-                    zq[ii] = __ldca(zr + QS * 32 * (ii + 8));
+                    float e_wx, e_wz;  // weights of the cell one column downstream
+                    unpack_weights(xv, e_wx, e_wz);
                     const float rcell = rq[ii];
                     rq[ii] = __ldca(rr + QS * 32 * (ii + 8));
                     const float edge = eq[ii];
-                    const float e_wx = xv;  // x weight one column downstream
                     float n_wz = __shfl_up_sync(0xffffffffu, w_wz, 1);
                     float s_wz = __shfl_down_sync(0xffffffffu, e_wz, 1);
                     n_wz = (l == 0) ? edge : n_wz;
@@ -556,8 +547,9 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     float m = rcell;
                     if (TAN) {
                         // own weights: < 0 on the west / north neighbour, > 0 on the east / south one
-                        m = c_tt < 0.f ? fmaf(-c_tt, lW, m) : (c_tt > 0.f ? fmaf(c_tt, lE, m) : m);
-                        m = c_wz < 0.f ? fmaf(-c_wz, lN, m) : (c_wz > 0.f ? fmaf(c_wz, lS, m) : m);
+                        // (the other side's term adds an exact zero: no branch on the weights)
+                        m = fmaf(fmaxf(c_tt, 0.f), lE, fmaf(fmaxf(-c_tt, 0.f), lW, m));
+                        m = fmaf(fmaxf(c_wz, 0.f), lS, fmaf(fmaxf(-c_wz, 0.f), lN, m));
                     } else {
                         m = wxW > 0.f ? fmaf(wxW, lW, m) : m;
                         m = wxE < 0.f ? fmaf(-wxE, lE, m) : m;
@@ -966,11 +958,13 @@ __device__ __noinline__ int tangent_is_converged(const ShotParams &P, const CUte
                     n.ts = k < ny - 1 ? tdv[i] : big;
                     n.lw = n.le = n.ln = n.ls = 0.f;
                     const bool src = h == hs && k == ks;
-                    const ExactCoef c = exact_coef_nb(n, sv[i], P.dh, src);
+                    // the weights exactly as the sweeps see them (packed, then unpacked)
+                    float wx, wz;
+                    unpack_weights(pack_weights(exact_coef_nb(n, sv[i], P.dh, src)), wx, wz);
                     float m = cell_residual_nb(n, sv[i], P.dh, src);
                     const float dw = i == 0 ? lc.w : lc.v[i - 1], de = i == 3 ? lc.e : lc.v[i + 1];
-                    m = c.wx < 0.f ? fmaf(-c.wx, dw, m) : (c.wx > 0.f ? fmaf(c.wx, de, m) : m);
-                    m = c.wz < 0.f ? fmaf(-c.wz, luv[i], m) : (c.wz > 0.f ? fmaf(c.wz, ldv[i], m) : m);
+                    m = fmaf(fmaxf(wx, 0.f), de, fmaf(fmaxf(-wx, 0.f), dw, m));
+                    m = fmaf(fmaxf(wz, 0.f), ldv[i], fmaf(fmaxf(-wz, 0.f), luv[i], m));
                     const float own = lc.v[i];
                     change |= !(fabsf(m - own) <= 1e-9f + 1e-6f * fabsf(own));
                 }
@@ -1182,8 +1176,8 @@ __device__ __noinline__ void relayout_items(const ShotParams &P, Warp &w, const 
 
 // Exact discrete adjoint preparation (not in the reference): signed weights
 // of every cell on its upwind neighbours (exact_coef) in the skewed layout of
-// the sweeps (x weights in TA/TB, z weights in WZA/WZB, those of the rows
-// bordering each strip in EU/ED), dJ/dT at the receiver cells (RA/RB, the
+// the sweeps (both weights of a cell packed in one float in TA/TB, the z
+// weights of the rows bordering each strip in EU/ED), dJ/dT at the receiver cells (RA/RB, the
 // residuals of each cell's receivers summed in receiver order), mu = 0.
 // tangent: the traveltime refinement's system instead -- the residual r of
 // every cell (cell_residual_nb) in RA/RB.
@@ -1261,7 +1255,6 @@ __device__ __noinline__ void exact_prepare(const ShotParams &P, Warp &w, const C
         unit_geom(u, s_, famA, q0, q1);
         const int row = kStrip * s_ + l;
         float *tx = line_ptr(TAz, TBz, famA, s_);
-        float *wz = line_ptr(P.WZA + (size_t)z * P.sstride, P.WZB + (size_t)z * P.sstride, famA, s_);
         float *rr = line_ptr(ra, rb, famA, s_);
         const float *sl = (famA ? P.SA : P.SB) + (size_t)s_ * qn * 32 + l;
         const float *eu = P.EU + (size_t)z * P.estride + (size_t)s_ * er + kEdgePad;
@@ -1338,8 +1331,7 @@ __device__ __noinline__ void exact_prepare(const ShotParams &P, Warp &w, const C
                     if (tangent) r = cell_residual_nb(nbh, c.s, P.dh, src);
                 }
                 win[i] = load_line(qi + D);  // read before line qi is rewritten (qi + D > qi)
-                tx[(size_t)qi * 32] = cf.wx;
-                wz[(size_t)qi * 32] = cf.wz;
+                tx[(size_t)qi * 32] = pack_weights(cf);
                 rr[(size_t)qi * 32] = r;
                 prev = c.t, lprev = c.lo;
             }
