@@ -32,9 +32,9 @@
 namespace rz {
 
 constexpr int kCheckSlots = 3;  // box slots in the ring of a fixpoint check
-// exact-adjoint / refinement preparation: lines a warp loads ahead, pieces
-// per walk at most, and units per warp whose boundary lines its ring holds
-constexpr int kWalkDepth = 8, kMaxPieces = 16, kMaxUnitsPerWarp = 24;
+// lines the exact-adjoint preparation reads ahead of the step that uses them
+constexpr int kPrepAhead = 4;
+static_assert(kBlk % kPrepAhead == 0, "whole groups per item");
 
 // Read-only stream staging.  A sweep step reads per-cell values that no
 // shared-memory ring holds: the skewed slowness or traveltime line, and in
@@ -58,7 +58,6 @@ struct alignas(128) WarpShared {
     uint32_t cphase;                  // fixpoint check: expected parity per slot
 };
 static_assert(sizeof(WarpShared) % 128 == 0, "TMA destinations need 128-byte alignment");
-static_assert(kMaxUnitsPerWarp * 128 <= kRing * kSlotFloats, "the preparation's saved lines fit a warp's ring");
 static_assert(offsetof(WarpShared, hb) == sizeof(float) * kRing * kSlotFloats, "hb follows the ring");
 static_assert(offsetof(WarpShared, stage) == offsetof(WarpShared, hb) + sizeof(float) * kHandoff &&
                   offsetof(WarpShared, stage) % 16 == 0,
@@ -1174,21 +1173,161 @@ __device__ __noinline__ void relayout_items(const ShotParams &P, Warp &w, const 
     }
 }
 
+// The weights of the exact adjoint (or the refinement's residuals) of the
+// cells of items [i0, i1) -- (strip s, block G), numbered s*(nxb+1)+G as in
+// relayout_items -- computed from the traveltime tiles in the warp's ring:
+// blocks G-1, G and G+1 of the strip's 33 rows (the next strip's first row
+// included) are in three slots while the item's lines q in [32G, 32G+32) of
+// both skew families are written.  Lane l walks its row: at step qq it takes
+// column 32G+qq-l (family A) or 32G+qq+l-31 (family B), reads the tile one
+// column ahead (anti-diagonal addresses, one bank per lane), gets the rows
+// above and below by shuffles (lane 0's upper row from T, lane 31's lower one
+// from the tile's 33rd row) and writes its cell of line q: the packed weights
+// to TA/TB and (tangent) the residual to RA/RB.  Slowness lines are read
+// a few steps ahead; the low parts of refined traveltimes come from their
+// skewed copy in RA/RB (lo != null), which this pass only reads.
+__device__ __noinline__ void tile_prepare(const ShotParams &P, Warp &w, const CUtensorMap *mld, int z, const float *T,
+                                          const float *lo, bool tangent, int i0, int i1) {
+    const int l = w.l;
+    const uint32_t ring_s = smem_u32(&w.ws->ring[0][0]);
+    const int nxb = P.nxb, per = nxb + 1, nx = P.nx, ny = P.ny, nxp = P.nxp, qn = P.qn;
+    const int hs = P.src_h[z], ks = P.src_k[z];
+    const float big = 3.0e38f;
+    float *const pa = P.TA + (size_t)z * P.sstride, *const pb = P.TB + (size_t)z * P.sstride;
+    float *const ra = P.RA + (size_t)z * P.sstride, *const rb = P.RB + (size_t)z * P.sstride;
+    auto slot_of = [&](int G) { return mod3(G + 1); };
+    int s = -1;
+    auto issue = [&](int G) {  // lane 0
+        const int sl = slot_of(G);
+        mbar_arrive_expect_tx(&w.mbar[sl], kSlotFloats * 4);
+        tma_load_3d(&w.ws->ring[0][0] + sl * kSlotFloats, mld, kBlk * G, kStrip * s, z, &w.mbar[sl]);
+    };
+    // traveltime of tile row r (grid row 32s+r, r = 0..32) at column c, 32G-33 <= c <= 32G+32
+    auto tile = [&](int r, int c) -> float {
+        const int blk = (c + 64) / kBlk - 2;  // floor(c / 32)
+        return lds(ring_s + (uint32_t)slot_of(blk) * kSlotBytes + (uint32_t)(r * kBlk + (c & (kBlk - 1))) * 4u);
+    };
+    for (int it = i0; it < i1; ++it) {
+        const int G = it % per;
+        if (it / per != s) {  // first item of a strip in this range: blocks G-1 and G
+            s = it / per;
+            fence_proxy_async_smem();  // the slots' earlier generic accesses precede the copies
+            __syncwarp();
+            if (l == 0) {
+                issue(G - 1);
+                issue(G);
+            }
+            __syncwarp();
+            ring_wait(w, slot_of(G - 1));
+            ring_wait(w, slot_of(G));
+        }
+        // block G+1 (east neighbours of the item's last column, and the next
+        // item's block) goes where block G-2 was, read by no step of this item
+        const bool nxt = G + 1 <= nxb;
+        fence_proxy_async_smem();
+        __syncwarp();
+        if (l == 0 && nxt) issue(G + 1);
+        __syncwarp();
+        bool waited = !nxt;
+        const int row = kStrip * s + l;
+        const size_t line0 = ((size_t)s * qn + kSkewFront + (size_t)kBlk * G) * 32 + l;  // line q = 32G, lane l
+        auto family = [&](auto fam_tag) {
+            constexpr bool FA = decltype(fam_tag)::value;
+            float *pw = (FA ? pa : pb) + line0;
+            float *pr = (FA ? ra : rb) + line0;
+            const float *sl = (FA ? P.SA : P.SB) + line0;
+            auto col = [&](int qq) { return FA ? kBlk * G + qq - l : kBlk * G + qq + l - (kStrip - 1); };
+            // lanes 0 / 31: the traveltime (lane 0) and low part of the row
+            // above / below the strip at the cell's column (lane 31's
+            // traveltime comes from the tile's 33rd row)
+            auto edge_t = [&](int c) -> float {
+                return (l == 0 && row < ny && row > 0 && c >= 0 && c < nx) ? __ldcg(T + (size_t)(row - 1) * nxp + c)
+                                                                         : big;
+            };
+            auto edge_lo = [&](int c) -> float {
+                if (!lo || row >= ny || c < 0 || c >= nx) return 0.f;
+                if (l == 0) return row > 0 ? __ldcg(lo + (size_t)(row - 1) * nxp + c) : 0.f;
+                if (l == kStrip - 1) return row < ny - 1 ? __ldcg(lo + (size_t)(row + 1) * nxp + c) : 0.f;
+                return 0.f;
+            };
+            float prev = tile(l, col(0) - 1), cur = tile(l, col(0));
+            float lprev = lo ? __ldcg(pr - 32) : 0.f;  // low parts of lines q-1 ..
+            float sv[kPrepAhead], lv[kPrepAhead], et[kPrepAhead], el[kPrepAhead];
+#pragma unroll
+            for (int i = 0; i < kPrepAhead; ++i) {
+                sv[i] = __ldg(sl + 32 * i);
+                lv[i] = lo ? __ldcg(pr + 32 * i) : 0.f;
+                et[i] = edge_t(col(i));
+                el[i] = edge_lo(col(i));
+            }
+            for (int q8 = 0; q8 < kBlk; q8 += kPrepAhead) {
+                // the next group's lines (past the item: its neighbours' lines, inside the stream)
+                float sn[kPrepAhead], ln8[kPrepAhead], etn[kPrepAhead], eln[kPrepAhead];
+#pragma unroll
+                for (int i = 0; i < kPrepAhead; ++i) {
+                    sn[i] = __ldg(sl + 32 * (q8 + kPrepAhead + i));
+                    ln8[i] = lo ? __ldcg(pr + 32 * (q8 + kPrepAhead + i)) : 0.f;
+                    etn[i] = edge_t(col(q8 + kPrepAhead + i));
+                    eln[i] = edge_lo(col(q8 + kPrepAhead + i));
+                }
+#pragma unroll
+                for (int i = 0; i < kPrepAhead; ++i) {
+                    const int qq = q8 + i;
+                    if (qq == kBlk - 1 && !waited) {  // the last step reads column 32G+32
+                        ring_wait(w, slot_of(G + 1));
+                        waited = true;
+                    }
+                    const int c = col(qq);
+                    const float next = tile(l, c + 1);
+                    const float lcur = lv[i], lnext = i < kPrepAhead - 1 ? lv[i + 1] : ln8[0];
+                    const bool valid = row < ny && c >= 0 && c < nx;
+                    // rows above / below: family A lines q-1 / q+1 of lanes l-1 / l+1,
+                    // family B lines q+1 / q-1
+                    float tn = __shfl_up_sync(0xffffffffu, FA ? prev : next, 1);
+                    float ts = __shfl_down_sync(0xffffffffu, FA ? next : prev, 1);
+                    float lnn = __shfl_up_sync(0xffffffffu, FA ? lprev : lnext, 1);
+                    float lss = __shfl_down_sync(0xffffffffu, FA ? lnext : lprev, 1);
+                    const float t32 = tile(kStrip, c);  // row 32s+32 (lane 31's lower row)
+                    if (l == 0) tn = et[i], lnn = el[i];
+                    if (l == kStrip - 1) ts = row < ny - 1 ? t32 : big, lss = el[i];
+                    if (row == ny - 1) ts = big, lss = 0.f;
+                    CellNb nb;
+                    nb.tc = cur;
+                    nb.tw = c > 0 ? prev : big;
+                    nb.te = c < nx - 1 ? next : big;
+                    nb.tn = tn, nb.ts = ts;
+                    nb.lw = c > 0 ? lprev : 0.f;
+                    nb.le = c < nx - 1 ? lnext : 0.f;
+                    nb.ln = lnn, nb.ls = lss;
+                    ExactCoef cf{0.f, 0.f, 0.f};
+                    float r = 0.f;
+                    if (valid) {
+                        const bool src = c == hs && row == ks;
+                        cf = exact_coef_nb(nb, sv[i], P.dh, src);
+                        if (tangent) r = cell_residual_nb(nb, sv[i], P.dh, src);
+                    }
+                    pw[(size_t)qq * 32] = pack_weights(cf);
+                    if (tangent) pr[(size_t)qq * 32] = r;
+                    prev = cur, cur = next, lprev = lcur;
+                }
+#pragma unroll
+                for (int i = 0; i < kPrepAhead; ++i) sv[i] = sn[i], lv[i] = ln8[i], et[i] = etn[i], el[i] = eln[i];
+            }
+        };
+        family(BoolTag<true>{});
+        family(BoolTag<false>{});
+    }
+}
+
 // Exact discrete adjoint preparation (not in the reference): signed weights
 // of every cell on its upwind neighbours (exact_coef) in the skewed layout of
 // the sweeps (both weights of a cell packed in one float in TA/TB, the z
-// weights of the rows bordering each strip in EU/ED), dJ/dT at the receiver cells (RA/RB, the
-// residuals of each cell's receivers summed in receiver order), mu = 0.
-// tangent: the traveltime refinement's system instead -- the residual r of
-// every cell (cell_residual_nb) in RA/RB.
-//
-// The traveltimes are first skewed into TA/TB with their border rows in
-// EU/ED (relayout_items, as for the Leung-Qian adjoint).  A warp then walks
-// the lines of one strip and family in order: every neighbour of the cells
-// of line q lies on line q-1 or q+1 of the same family (the rows above and
-// below the strip in EU/ED), so each line is read once, coalesced, two lines
-// ahead, and the weights replace the traveltimes of line q once lines
-// q-1..q+1 are in registers.
+// weights of the rows bordering each strip in EU/ED), dJ/dT at the receiver
+// cells (RA/RB, the residuals of each cell's receivers summed in receiver
+// order), mu = 0.  tangent: the traveltime refinement's system instead -- the
+// residual r of every cell (cell_residual_nb) in RA/RB.  The cells' weights
+// come from the traveltime tiles (tile_prepare); the border rows' z weights
+// and the receiver terms are gathered from the row-major fields.
 __device__ __noinline__ void exact_prepare(const ShotParams &P, Warp &w, const CUtensorMap *mld,
                                            const CUtensorMap *mlo, int z, const float *T, float *L, bool tangent) {
     const int tid = threadIdx.x, nthr = blockDim.x;
@@ -1197,147 +1336,37 @@ __device__ __noinline__ void exact_prepare(const ShotParams &P, Warp &w, const C
     const int nx = P.nx, ny = P.ny, nxp = P.nxp, qn = P.qn;
     float *ra = P.RA + (size_t)z * P.sstride, *rb = P.RB + (size_t)z * P.sstride;
     // low parts of refined traveltimes (the exact adjoint after a refinement):
-    // skewed into RA/RB, which the walk reads ahead of its writes
+    // skewed into RA/RB for the weights, then overwritten by the receiver terms
     const float *lo = (P.refine && !tangent) ? P.Told + (size_t)z * P.fstride : nullptr;
+    const float big = 3.0e38f;
+    const int er = edge_row(nxp);
     {
         const int items = P.nstrips * (P.nxb + 1);
         const int per_warp = (items + W - 1) / W;
         const int i0 = min(items, g * per_warp), i1 = min(items, (g + 1) * per_warp);
-        relayout_items(P, w, mld, i0, i1, skew_dst_t(P, z));
-        if (lo) relayout_items(P, w, mlo, i0, i1, SkewDst{ra, rb, nullptr, nullptr});
+        if (lo) {
+            relayout_items(P, w, mlo, i0, i1, SkewDst{ra, rb, nullptr, nullptr});
+            __syncthreads();
+        }
+        tile_prepare(P, w, mld, z, T, lo, tangent, i0, i1);
     }
     __syncthreads();
-    const float big = 3.0e38f;
-    const int er = edge_row(nxp);
-    // Work units: piece p of the walk over strip s, family f (lines [q0, q1)),
-    // unit u = (2 s + f) * npc + p; warp g takes units g, g + W, ...  Pieces
-    // rewrite disjoint lines in place, so the two lines just outside each
-    // piece (q0 - 1 and q1: its neighbours' first and last lines) are saved
-    // to the warp's ring first, before any piece writes.  npc is the piece
-    // count per walk that needs the fewest rounds of the slowest warp.
-    const int nwalk = 2 * P.nstrips;
-    int npc = 1;
+    // lines no item covers: no dependence (packed 2.0), no residual; the exact
+    // adjoint's receiver terms start from zero everywhere
     {
-        float best = 3.0e38f;
-        for (int c = 1; c <= kMaxPieces; ++c) {
-            const int per_warp = (nwalk * c + W - 1) / W;
-            const float cost = (float)per_warp / (float)c;  // rounds x lines per piece
-            if (per_warp <= kMaxUnitsPerWarp && cost < best * 0.999f) best = cost, npc = c;
+        const int lead = kSkewFront, tail0 = kSkewFront + kBlk * (P.nxb + 1), nout = lead + (qn - tail0);
+        for (int i = tid; i < 2 * P.nstrips * nout * 32; i += nthr) {
+            const int lane = i & 31, u = i >> 5, fam = u / (P.nstrips * nout), v = u - fam * (P.nstrips * nout);
+            const int st = v / nout, k = v - st * nout, q = k < lead ? k : tail0 + (k - lead);
+            const size_t o = ((size_t)st * qn + q) * 32 + lane;
+            (fam ? P.TB : P.TA)[(size_t)z * P.sstride + o] = 2.0f;
+            if (tangent) (fam ? rb : ra)[o] = 0.f;
+        }
+        if (!tangent) {
+            float4 *a4 = reinterpret_cast<float4 *>(ra), *b4 = reinterpret_cast<float4 *>(rb);
+            for (size_t i = tid; i < P.sstride / 4; i += nthr) a4[i] = b4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
     }
-    const int plen = (qn + npc - 1) / npc, nunit = nwalk * npc;
-    float *sv_ = &w.ws->ring[0][0];  // [unit of this warp][4][32]: T and lo of lines q0-1 and q1
-    auto unit_geom = [&](int u, int &s_, bool &fa, int &q0, int &q1) {
-        const int wk = u / npc, pc = u - wk * npc;
-        s_ = wk >> 1, fa = (wk & 1) == 0;
-        q0 = min(qn, pc * plen), q1 = min(qn, q0 + plen);
-    };
-    auto line_ptr = [&](float *base_A, float *base_B, bool fa, int s_) {
-        return (fa ? base_A : base_B) + (size_t)s_ * qn * 32 + l;
-    };
-    float *const TAz = P.TA + (size_t)z * P.sstride, *const TBz = P.TB + (size_t)z * P.sstride;
-    for (int u = g, ui = 0; npc > 1 && u < nunit; u += W, ++ui) {
-        int s_, q0, q1;
-        bool fa;
-        unit_geom(u, s_, fa, q0, q1);
-        const float *tx = line_ptr(TAz, TBz, fa, s_);
-        const float *rl = line_ptr(ra, rb, fa, s_);
-        float *b = sv_ + ui * 128 + l;
-        b[0] = q0 > 0 ? __ldcg(tx + (size_t)(q0 - 1) * 32) : 0.f;
-        b[32] = (lo && q0 > 0) ? __ldcg(rl + (size_t)(q0 - 1) * 32) : 0.f;
-        b[64] = q1 < qn ? __ldcg(tx + (size_t)q1 * 32) : 0.f;
-        b[96] = (lo && q1 < qn) ? __ldcg(rl + (size_t)q1 * 32) : 0.f;
-    }
-    __syncthreads();
-    for (int u = g, ui = 0; u < nunit; u += W, ++ui) {
-        int s_, q0, q1;
-        bool famA;
-        unit_geom(u, s_, famA, q0, q1);
-        const int row = kStrip * s_ + l;
-        float *tx = line_ptr(TAz, TBz, famA, s_);
-        float *rr = line_ptr(ra, rb, famA, s_);
-        const float *sl = (famA ? P.SA : P.SB) + (size_t)s_ * qn * 32 + l;
-        const float *eu = P.EU + (size_t)z * P.estride + (size_t)s_ * er + kEdgePad;
-        const float *ed = P.ED + (size_t)z * P.estride + (size_t)s_ * er + kEdgePad;
-        const float *bnd = sv_ + ui * 128 + l;
-        auto col = [&](int qi) { return famA ? qi - kSkewFront - l : qi - kSkewFront + l - 31; };
-        // line qi of the unit's window: its traveltime, slowness, low part and
-        // (lanes 0 / 31) the traveltime and low part of the row above / below
-        // the strip at the cell's column.  Lines of this piece come from
-        // global memory (read before this warp rewrites them), line q1 from
-        // the saved copy, lines past q1 are not needed.
-        struct Line {
-            float t, s, e, lo, le;
-        };
-        auto load_line = [&](int qi) -> Line {
-            Line v{0.f, 0.f, big, 0.f, 0.f};
-            if (qi >= q1 + 1 || qi >= qn) return v;
-            if (qi == q1) {
-                v.t = bnd[64], v.lo = bnd[96];
-            } else {
-                v.t = __ldcg(tx + (size_t)qi * 32);
-                if (lo) v.lo = __ldcg(rr + (size_t)qi * 32);
-            }
-            v.s = __ldg(sl + (size_t)qi * 32);
-            const int h = col(qi);
-            if (h >= 0 && h < nx && row < ny && (l == 0 || l == 31)) {
-                const int rn = l == 0 ? row - 1 : row + 1;
-                if (rn >= 0 && rn < ny) {
-                    v.e = __ldcg((l == 0 ? eu : ed) + h);
-                    if (lo) v.le = __ldcg(lo + (size_t)rn * nxp + h);
-                }
-            }
-            return v;
-        };
-        // a window of D lines in registers: line qi + D replaces line qi once
-        // line qi is done (line qi + 1 is then in the next slot, or in slot 0
-        // when qi ends a round)
-        constexpr int D = kWalkDepth;
-        Line win[D];
-#pragma unroll
-        for (int i = 0; i < D; ++i) win[i] = load_line(q0 + i);
-        float prev = q0 > 0 ? bnd[0] : 0.f, lprev = q0 > 0 ? bnd[32] : 0.f;  // q0 > 0 only with npc > 1
-        for (int qb = q0; qb < q1; qb += D) {
-#pragma unroll
-            for (int i = 0; i < D; ++i) {
-                const int qi = qb + i;
-                if (qi >= q1) break;  // warp-uniform
-                const Line c = win[i];
-                const float next = win[(i + 1) % D].t, lnext = win[(i + 1) % D].lo;
-                const int h = col(qi);
-                const bool valid = row < ny && h >= 0 && h < nx;
-                // north / south neighbours: family A lines q-1 / q+1 at positions
-                // j-1 / j+1, family B lines q+1 / q-1
-                float tn = __shfl_up_sync(0xffffffffu, famA ? prev : next, 1);
-                float ts = __shfl_down_sync(0xffffffffu, famA ? next : prev, 1);
-                float ln = __shfl_up_sync(0xffffffffu, famA ? lprev : lnext, 1);
-                float ls = __shfl_down_sync(0xffffffffu, famA ? lnext : lprev, 1);
-                if (l == 0) tn = c.e, ln = c.le;
-                if (l == 31) ts = c.e, ls = c.le;
-                if (row == ny - 1) ts = big, ls = 0.f;
-                CellNb nbh;
-                nbh.tc = c.t;
-                nbh.tw = h > 0 ? prev : big;
-                nbh.te = h < nx - 1 ? next : big;
-                nbh.tn = tn, nbh.ts = ts;
-                nbh.lw = h > 0 ? lprev : 0.f;
-                nbh.le = h < nx - 1 ? lnext : 0.f;
-                nbh.ln = ln, nbh.ls = ls;
-                ExactCoef cf{0.f, 0.f, 0.f};
-                float r = 0.f;
-                if (valid) {
-                    const bool src = h == hs && row == ks;
-                    cf = exact_coef_nb(nbh, c.s, P.dh, src);
-                    if (tangent) r = cell_residual_nb(nbh, c.s, P.dh, src);
-                }
-                win[i] = load_line(qi + D);  // read before line qi is rewritten (qi + D > qi)
-                tx[(size_t)qi * 32] = pack_weights(cf);
-                rr[(size_t)qi * 32] = r;
-                prev = c.t, lprev = c.lo;
-            }
-        }
-    }
-    fence_proxy_async_smem();  // the saved lines (generic writes) precede later copies into the rings
     __syncthreads();
     // z weights of the rows above (EU) and below (ED) each strip (the exact
     // adjoint's sweeps read them; the refinement's use only a cell's own weights)
