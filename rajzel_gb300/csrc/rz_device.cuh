@@ -443,28 +443,27 @@ RZ_DEV CellNb load_cell_nb(const float *T, const float *Tlo, int nxp, int nx, in
 // the low parts, so the weights are those of the refined field to float
 // precision; the low parts are 0 otherwise.
 RZ_DEV ExactCoef exact_coef_nb(const CellNb &n, float s, float dh, bool source) {
-    ExactCoef c{0.f, 0.f, 0.f};
-    if (source) return c;
+    // both cases are evaluated and one is selected: cells of a warp take
+    // either, and a branch would run them one after the other
     const bool west = n.tw <= n.te, north = n.tn <= n.ts;
     const float a = west ? n.tw : n.te, b = north ? n.tn : n.ts;
     const float d = (a - b) + ((west ? n.lw : n.le) - (north ? n.ln : n.ls));
     const float sh = s * dh;
-    if (fabsf(d) >= sh) {
-        if (d <= 0.f) c.wx = west ? -1.f : 1.f;
-        else c.wz = north ? -1.f : 1.f;
-        c.gs = dh;
-        return c;
-    }
-    // r = sqrt(q) and 1/r from one reciprocal square root (a few ulp: the
-    // weights enter a linear solve whose float error is of that order anyway)
+    const bool one = fabsf(d) >= sh;
+    // two-sided: r = sqrt(q) and 1/r from one reciprocal square root (a few
+    // ulp: the weights enter a linear solve whose float error is of that
+    // order anyway); q <= 0 only where the one-sided case is taken
     const float q = fmaf(2.0f * sh, sh, -d * d);
     const float rr = rsqrtf(q);
     const float r = q * rr;
     const float half_rcp = 0.5f * rr;
-    const float wa = (r - d) * half_rcp, wb = (r + d) * half_rcp;
-    c.wx = west ? -wa : wa;
-    c.wz = north ? -wb : wb;
-    c.gs = s * dh * dh * rr;
+    // one-sided: weight 1 on the smaller neighbour (x when d <= 0), dT/dS = DH
+    const float wa = one ? (d <= 0.f ? 1.f : 0.f) : (r - d) * half_rcp;
+    const float wb = one ? (d <= 0.f ? 0.f : 1.f) : (r + d) * half_rcp;
+    ExactCoef c;
+    c.wx = source ? 0.f : (west ? -wa : wa);
+    c.wz = source ? 0.f : (north ? -wb : wb);
+    c.gs = source ? 0.f : (one ? dh : s * dh * dh * rr);
     return c;
 }
 
@@ -485,10 +484,10 @@ RZ_DEV float godunov_residual(float a, float b, float s, float dh, float t) {
     const float sh = __fmul_rn(s, dh);
     const float shl = __fmaf_rn(s, dh, -sh);  // sh + shl = s*dh exactly
     const float d = __fsub_rn(a, b);
-    if (fabsf(d) >= sh) {
-        // min(a, b) + s*dh - t; min - t is exact (t lies within a factor two of min, or min is 0)
-        return __fadd_rn(__fadd_rn(__fsub_rn(fminf(a, b), t), sh), shl);
-    }
+    // one-sided: min(a, b) + s*dh - t; min - t is exact (t lies within a
+    // factor two of min, or min is 0).  Both cases are evaluated and one is
+    // selected (no divergent branch; the two-sided value is NaN where unused).
+    const float one = __fadd_rn(__fadd_rn(__fsub_rn(fminf(a, b), t), sh), shl);
     // (a + b + sqrt(2 (s dh)^2 - d^2)) / 2 - t in float-float
     const float sum = __fadd_rn(a, b);
     const float sbb = __fsub_rn(sum, a);
@@ -509,7 +508,8 @@ RZ_DEV float godunov_residual(float a, float b, float s, float dh, float t) {
     const float ue = __fadd_rn(__fsub_rn(sum, __fsub_rn(uh, ubb)), __fsub_rn(r0, ubb));
     const float ul = __fadd_rn(__fadd_rn(ue, rl), se);
     // uh - 2t is exact (uh lies within a factor two of 2t)
-    return __fmul_rn(0.5f, __fadd_rn(__fsub_rn(uh, __fmul_rn(2.0f, t)), ul));
+    const float two = __fmul_rn(0.5f, __fadd_rn(__fsub_rn(uh, __fmul_rn(2.0f, t)), ul));
+    return fabsf(d) >= sh ? one : two;
 }
 
 // r_c of the traveltime refinement at a cell of the converged field
