@@ -221,6 +221,25 @@ RZ_DEV bool wait_flag_ge(const int *flag, int need, volatile int *abort_word, ui
 RZ_DEV float ldg_nc(const float *p) { return __ldg(p); }
 RZ_DEV uint32_t ldg_nc_u32(const uint32_t *p) { return __ldg(p); }
 
+// (x >= y) ? u : v and (x > y) ? u : v as one predicated select.  The
+// cells of a warp take either side; a branch would run the sides one after
+// the other, which the compiler chooses when a side holds a division or a
+// square root.  Comparisons with NaN are false, as in C.
+RZ_DEV float sel_ge(float x, float y, float u, float v) {
+    float r;
+    asm("{\n\t.reg .pred p;\n\tsetp.ge.f32 p, %1, %2;\n\tselp.f32 %0, %3, %4, p;\n\t}"
+        : "=f"(r)
+        : "f"(x), "f"(y), "f"(u), "f"(v));
+    return r;
+}
+RZ_DEV float sel_gt(float x, float y, float u, float v) {
+    float r;
+    asm("{\n\t.reg .pred p;\n\tsetp.gt.f32 p, %1, %2;\n\tselp.f32 %0, %3, %4, p;\n\t}"
+        : "=f"(r)
+        : "f"(x), "f"(y), "f"(u), "f"(v));
+    return r;
+}
+
 // ---------------------------------------------------------------------------
 // Forward point update (sweep.c:89-97)
 //
@@ -246,7 +265,10 @@ RZ_DEV float godunov_branch2_f64(float sum, float d, float s, float dh) {
 RZ_DEV float godunov_ref(float a, float b, float s, float dh) {
     float d = __fsub_rn(a, b);
     float sh = __fmul_rn(s, dh);
-    if (fabsf(d) >= sh) return __fadd_rn(fminf(a, b), sh);
+    // branch 1 (|d| >= sh); branch 2 is evaluated for every cell and the
+    // branch selected at the end (its float-float value is NaN or meaningless
+    // where branch 1 holds, and is then not used)
+    const float one_sided = __fadd_rn(fminf(a, b), sh);
     float sum = __fadd_rn(a, b);
     // S*h = sh + shl exactly
     float shl = __fmaf_rn(s, dh, -sh);
@@ -279,8 +301,8 @@ RZ_DEV float godunov_ref(float a, float b, float s, float dh) {
     float below = __fsub_rn(z, __int_as_float(__float_as_int(z) - 1));
     float tol = __fmul_rn(z, 0x1p-38f);
     bool safe = (fabsf(zr) < __fsub_rn(__fmul_rn(0.5f, below), tol)) && (Dh > 0x1p-100f) && (z < 0x1p+100f);
-    if (__builtin_expect(safe, 1)) return __fmul_rn(0.5f, z);
-    return godunov_branch2_f64(sum, d, s, dh);
+    if (__builtin_expect(!(fabsf(d) >= sh) && !safe, 0)) return godunov_branch2_f64(sum, d, s, dh);
+    return sel_ge(fabsf(d), sh, one_sided, __fmul_rn(0.5f, z));
 }
 
 // fast mode: FP32 arithmetic throughout (error ~1 ulp per update), written
@@ -366,7 +388,7 @@ RZ_DEV float leung_qian_fast(float tc, float te, float tw, float ts, float tn, f
     const float ap = tc - te, am = tw - tc, bp = tc - ts, bm = tn - tc;
     const float lhs = (fmaxf(ap, 0.0f) - fminf(am, 0.0f)) + (fmaxf(bp, 0.0f) - fminf(bm, 0.0f));
     const float rhs = (fmaxf(am, 0.0f) * lw - fminf(ap, 0.0f) * le) + (fmaxf(bm, 0.0f) * ln - fminf(bp, 0.0f) * ls);
-    const float lt = (lhs > eps_h2) ? __fdividef(rhs, lhs) : 0.0f;
+    const float lt = sel_gt(lhs, eps_h2, __fdividef(rhs, lhs), 0.0f);
     return fminf(own, lt);
 }
 

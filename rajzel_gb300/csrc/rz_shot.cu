@@ -1331,14 +1331,13 @@ __device__ __noinline__ void tile_prepare(const ShotParams &P, Warp &w, const CU
 __device__ __noinline__ void exact_prepare(const ShotParams &P, Warp &w, const CUtensorMap *mld,
                                            const CUtensorMap *mlo, int z, const float *T, float *L, bool tangent) {
     const int tid = threadIdx.x, nthr = blockDim.x;
-    const int l = tid & 31, g = tid >> 5, W = nthr >> 5;
+    const int g = tid >> 5, W = nthr >> 5;
     const int hs = P.src_h[z], ks = P.src_k[z];
     const int nx = P.nx, ny = P.ny, nxp = P.nxp, qn = P.qn;
     float *ra = P.RA + (size_t)z * P.sstride, *rb = P.RB + (size_t)z * P.sstride;
     // low parts of refined traveltimes (the exact adjoint after a refinement):
     // skewed into RA/RB for the weights, then overwritten by the receiver terms
     const float *lo = (P.refine && !tangent) ? P.Told + (size_t)z * P.fstride : nullptr;
-    const float big = 3.0e38f;
     const int er = edge_row(nxp);
     {
         const int items = P.nstrips * (P.nxb + 1);
