@@ -88,18 +88,21 @@ def _cpu_worker(args):
     return time.perf_counter() - t0
 
 
-def cpu_run(nshots_sample, cores, kind, wname="grad_1700x350", nshots_total=100):
+def cpu_run(nshots_sample, cores, kind, wname="grad_1700x350", nshots_total=100, pool=None):
     """Time grad_obj over `nshots_sample` shots split across `cores` processes
-    exactly as init_MPIshot splits shots over ranks; returns wall seconds."""
+    exactly as init_MPIshot splits shots over ranks; returns wall seconds
+    (the slowest rank's grad_obj, as the reference's shot loop ends at its
+    MPI_Allreduce).  A pool of `cores` spawned processes may be passed in
+    and reused across calls."""
     import multiprocessing as mp
     import oracle as O
     O.build(ref=(kind == "reference"))
     spans = [O.shot_partition(nshots_sample, cores, r) for r in range(cores)]
     jobs = [(kind, list(range(a - 1, b - 1)), nshots_total, wname) for a, b in spans]
-    ctx = mp.get_context("spawn")
-    with ctx.Pool(cores) as pool:
-        times = pool.map(_cpu_worker, jobs)
-    return max(times)
+    if pool is not None:
+        return max(pool.map(_cpu_worker, jobs))
+    with mp.get_context("spawn").Pool(cores) as own:
+        return max(own.map(_cpu_worker, jobs))
 
 
 def cpu_kind():
@@ -111,12 +114,16 @@ def run_reference_arm(args, rank):
     """`--impl reference`: the reference algorithm timed on the host cores."""
     if rank != 0:
         return
+    import multiprocessing as mp
+    from rajzel_gb300 import synth
+    w = synth.grad_1700x350(nshots=100)
     cores = os.cpu_count() or 1
     kind = cpu_kind()
-    sample = cores  # one shot per core per step
-    for _ in range(args.warmup):
-        cpu_run(sample, cores, kind)
-    secs = [cpu_run(sample, cores, kind) for _ in range(args.steps)]
+    sample = w.nshots  # the whole 100-shot batch per step, as the GPU arm's step
+    with mp.get_context("spawn").Pool(cores) as pool:
+        for _ in range(args.warmup):
+            cpu_run(sample, cores, kind, pool=pool)
+        secs = [cpu_run(sample, cores, kind, pool=pool) for _ in range(args.steps)]
     total = sum(secs)
     value = sample * args.steps / total
     line = {
@@ -124,9 +131,12 @@ def run_reference_arm(args, rank):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64",
         "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "sample_shots_per_step": sample, "cores": cores},
+        "config": {"workload": WORKLOAD, "mode": "reference algorithm", "shots": sample, "receivers": w.ntr,
+                   "grid": [w.nx, w.ny], "dh": w.dh, "ttnorm": w.ttnorm,
+                   "parallelism": f"{cores} host processes, init_MPIshot split",
+                   "l2": "per-shot working set ~12 MB per process; no flush"},
         "cpu_baseline": {"value": value, "unit": "shots/s", "cores": cores, "kind": kind,
-                         "sample": f"{sample} of the 100 shots per step, one process per core, init_MPIshot split"},
+                         "sample": f"all {sample} shots per step, one process per core, init_MPIshot split"},
         "e2e": {"value": value, "unit": "shots/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -329,7 +339,7 @@ def run_gpu_arm(args, rank, world, local_rank):
     if rank != 0:
         return
     cores = os.cpu_count() or 1
-    sample = 2 * cores
+    sample = w.nshots
     kind = cpu_kind()
     cpu_s = cpu_run(sample, cores, kind)
     clk = clocks.summary(t_wall0, t_wall1)
@@ -352,7 +362,7 @@ def run_gpu_arm(args, rank, world, local_rank):
                      "kernel": "rz::shot_kernel", "kernel_ms": kernel_ms,
                      "algorithmic_bytes_per_launch": alg_bytes},
         "cpu_baseline": {"value": sample / cpu_s, "unit": "shots/s", "cores": cores, "kind": kind,
-                         "sample": f"grad_obj over {sample} of the 100 shots, one process per core"},
+                         "sample": f"grad_obj over all {sample} shots of the step, one process per core"},
         "e2e": {"value": e2e_value, "unit": "shots/s", "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "plain_per_shot_gpu": {"value": plain_value, "unit": "shots/s",
                                "how": f"same kernels, one shot per launch, {nplain} shots, synchronised"},
