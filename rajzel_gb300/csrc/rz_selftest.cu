@@ -94,3 +94,36 @@ extern "C" int rz_selftest_shot_sum(const float *vals, long ncells, int nshots, 
     cudaFree(dout);
     return e == cudaSuccess ? 0 : 3;
 }
+
+namespace {
+
+__global__ void weights_check(const float *wx, const float *wz, long n, float *ox, float *oz, float *packed) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    rz::ExactCoef c{wx[i], wz[i], 0.f};
+    const float p = rz::pack_weights(c);
+    rz::unpack_weights(p, ox[i], oz[i]);
+    packed[i] = p;
+}
+
+}  // namespace
+
+// rz_selftest_weights: the exact adjoint's packed weight stream, round trip.
+// For host arrays wx, wz [n] of one cell's signed weights (|wx| + |wz| = 1,
+// or both 0), returns the unpacked weights ox, oz and the packed floats.
+extern "C" int rz_selftest_weights(const float *wx, const float *wz, long n, float *ox, float *oz, float *packed) {
+    if (n <= 0) return 1;
+    float *d = nullptr;
+    if (cudaMalloc(&d, 5 * (size_t)n * sizeof(float)) != cudaSuccess) return 3;
+    cudaError_t e = cudaMemcpy(d, wx, n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(d + n, wz, n * sizeof(float), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) {
+        weights_check<<<(unsigned)((n + 255) / 256), 256>>>(d, d + n, n, d + 2 * n, d + 3 * n, d + 4 * n);
+        e = cudaDeviceSynchronize();
+    }
+    if (e == cudaSuccess) e = cudaMemcpy(ox, d + 2 * n, n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(oz, d + 3 * n, n * sizeof(float), cudaMemcpyDeviceToHost);
+    if (e == cudaSuccess) e = cudaMemcpy(packed, d + 4 * n, n * sizeof(float), cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    return e == cudaSuccess ? 0 : 3;
+}

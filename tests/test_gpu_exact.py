@@ -109,3 +109,42 @@ def test_reference_gradient_unchanged_by_exact_switch(R):
     p = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
     go, lo, _, _, _ = O.grad_obj(p, S32, w.srcx, w.srcz, w.recx, w.recz, Tobs)
     assert np.array_equal(g1, go) and np.array_equal(g2, go) and l1 == lo == l2
+
+
+def test_packed_weights_round_trip(R):
+    """The linear sweeps read both weights of a cell from one float: the
+    smaller magnitude, the x direction in the sign bit, the z direction and
+    which magnitude is stored in the two lowest significand bits, 2.0 for a
+    cell with no upwind neighbour.  Every case must come back with its
+    directions, the smaller weight within 2 ulp and the larger as 1 minus it."""
+    import ctypes as C
+    import os
+    lib = C.CDLL(os.path.join(os.path.dirname(R.__file__), "librz_selftest.so"))
+    fp = C.POINTER(C.c_float)
+    lib.rz_selftest_weights.argtypes = [fp, fp, C.c_long, fp, fp, fp]
+    rng = np.random.default_rng(11)
+    wa = rng.uniform(0.0, 1.0, 4000).astype(np.float32)
+    wa[:6] = [0.0, 1.0, 0.5, 1e-7, 1 - 1e-7, 0.25]
+    sx = np.where(rng.random(wa.size) < 0.5, -1.0, 1.0).astype(np.float32)
+    sz = np.where(rng.random(wa.size) < 0.5, -1.0, 1.0).astype(np.float32)
+    wx = sx * wa
+    wz = (sz * (np.float32(1.0) - wa)).astype(np.float32)
+    # the source and cells outside the grid: no upwind neighbour
+    wx = np.concatenate([wx, np.zeros(2, np.float32)])
+    wz = np.concatenate([wz, np.zeros(2, np.float32)])
+    n = wx.size
+    ox, oz, pk = (np.empty(n, np.float32) for _ in range(3))
+    ptr = lambda a: a.ctypes.data_as(fp)  # noqa: E731
+    assert lib.rz_selftest_weights(ptr(wx), ptr(wz), n, ptr(ox), ptr(oz), ptr(pk)) == 0
+    assert np.all(pk[-2:] == 2.0) and np.all(ox[-2:] == 0) and np.all(oz[-2:] == 0)
+    ax, az = np.abs(wx[:-2]), np.abs(wz[:-2])
+    # directions (a zero weight may come back as -0 or +0)
+    nzx, nzz = ax > 0, az > 0
+    assert np.all(np.sign(ox[:-2][nzx]) == np.sign(wx[:-2][nzx]))
+    assert np.all(np.sign(oz[:-2][nzz]) == np.sign(wz[:-2][nzz]))
+    # the smaller weight within 2 ulp, the larger within an ulp of 1 minus it
+    small = np.minimum(ax, az)
+    got_small = np.where(ax <= az, np.abs(ox[:-2]), np.abs(oz[:-2]))
+    got_small = np.where(ax == az, np.minimum(np.abs(ox[:-2]), np.abs(oz[:-2])), got_small)
+    assert np.all(np.abs(got_small - small) <= 2 * np.spacing(small) + 1e-45)
+    assert np.all(np.abs(np.abs(ox[:-2]) + np.abs(oz[:-2]) - 1.0) <= 2 ** -23)
