@@ -413,7 +413,7 @@ struct ExactCoef {
 // two-sided: (r-d)/2r and (r+d)/2r), so the smaller magnitude is stored and
 // the larger is 1 minus it: the sign bit is the x direction (set: west),
 // significand bit 0 the z direction (set: south), bit 1 whether the stored
-// magnitude is |wz|; those two bits cost at most 2 ulp of the smaller weight.
+// magnitude is |wz|; those two bits cost at most 3 ulp of the smaller weight.
 // 2.0 marks a cell with no upwind neighbour (the source, cells outside the
 // grid).
 RZ_DEV float pack_weights(const ExactCoef &c) {
