@@ -223,8 +223,9 @@ int rz_fatt(rz_context *ctx, const rz_fatt_opts *opts, int nshots, const float *
    context holds one grid, its model and receivers; shot i of grid g is a job
    of one persistent kernel whose CTAs take jobs largest grid first, so small
    grids fill the SMs while the large ones run.  Per grid the results equal
-   rz_grad_obj on that context.  All contexts must use the same device and
-   mode and the reference gradient; the work runs on ctxs[0]'s stream.
+   rz_grad_obj on that context (gradient kind and refinement included).  All
+   contexts must use the same device and mode (FP64 excepted); the work runs
+   on ctxs[0]'s stream.
      nshots[g], srcx[g], srcz[g], Tobs[g], grad[g]: as rz_grad_obj, per grid
      L2[ngrids]: misfit per grid */
 int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, const float *const *srcx,

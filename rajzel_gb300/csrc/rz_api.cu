@@ -1459,8 +1459,6 @@ int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, co
         if (c->device != c0->device || c->mode != c0->mode)
             return fail(c0, RZ_EINVAL, "grid %d: every context must use the same device and mode", i);
         if (c->mode == RZ_MODE_FP64) return fail(c0, RZ_EUNSUPPORTED, "grid %d: FP64 mode has no multi-grid launch", i);
-        if (c->grad_kind != RZ_GRADIENT_REFERENCE)
-            return fail(c0, RZ_EUNSUPPORTED, "grid %d: the exact gradient is not available in multi-grid launches", i);
         if (nshots[i] < 1 || !Tobs[i] || !grad[i]) return fail(c0, RZ_EINVAL, "grid %d: bad arguments", i);
         for (int k = 0; k < i; ++k)
             if (ctxs[k] == c) return fail(c0, RZ_EINVAL, "context %d appears twice", i);
@@ -1506,6 +1504,7 @@ int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, co
         fill_params(c, G.P, 0, n);
         G.P.do_residual = 1;
         G.P.do_adjoint = 1;
+        G.P.exact = c->grad_kind == RZ_GRADIENT_EXACT ? 1 : 0;
         G.maps = c->maps;
         G.W = shot_kernel_warps(c->nstrips);
         Wb = std::max(Wb, G.W);
@@ -1546,14 +1545,18 @@ int rz_grad_obj_multi(int ngrids, rz_context *const *ctxs, const int *nshots, co
             if (!c->dGrad) CK(dalloc(&c->dGrad, (size_t)c->g.nx * c->g.ny));
             gdst = c->dGrad;
         }
-        if (c->mode == RZ_MODE_FAST && !c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
+        const bool exact = c->grad_kind == RZ_GRADIENT_EXACT;
+        if ((c->mode == RZ_MODE_FAST || exact) && !c->dGrad64) CK(dalloc(&c->dGrad64, (size_t)c->g.nx * c->g.ny));
         if (!c->dL2) CK(dalloc(&c->dL2, 1));
         bool finished = false;
         if ((r = stack_chunk(c, 0, nshots[i], gdst, true, &finished))) return fail(c0, r, "%s", c->err.c_str());
         if (!finished) {
-            CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, st));
+            if (!exact) {  // the exact gradient has no frame copy (dJ/dVp of every cell)
+                CK(launch_cp_frame(gdst, nullptr, c->g.nx, c->g.ny, c->g.nx, 2, st));
+                c->launches += 1;
+            }
             CK(launch_sum_l2(c->dl2, nshots[i], c->dL2, st));
-            c->launches += 2;
+            c->launches += 1;
         }
         CK(cudaMemcpyAsync(L2 + i, c->dL2, sizeof(double),
                            have_dev(flags) ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, st));

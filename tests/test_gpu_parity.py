@@ -495,3 +495,28 @@ def test_autotuner_picks_a_width_that_changes_no_result(R):
     assert np.array_equal(g0, g1) and l0 == l1
     go, L2o, _, _, _ = O.grad_obj(p, S, w.srcx, w.srcz, w.recx, w.recz, Tobs)
     assert np.array_equal(g1, go)
+
+
+@pytest.mark.parametrize("kind,refine", [("exact", True), ("exact", False), ("reference", True)])
+def test_multi_grid_launch_exact_refined_equals_per_grid_calls(R, kind, refine):
+    """The exact gradient and refined traveltimes through one persistent launch
+    over three grids (one banded) equal each grid's own rz_grad_obj, bit for
+    bit: the tile-fed preparation, the packed weight streams and the
+    refinement's linear sweeps do not depend on the launch they run in."""
+    shapes = [(120, 90, 4), (60, 600, 3), (200, 40, 5)]
+    ctxs, ws, tobs, want = [], [], [], []
+    for k, (nx, ny, ns) in enumerate(shapes):
+        w = synth.small_case(500 + k, nx, ny, nshots=ns)
+        p = params(w)
+        S = synth.slowness(w.vp_true)
+        Tobs = _noisy_picks(p, w, S, ns, 60 + k)
+        ctx = make_ctx(R, w, mode="fast")
+        ctx.set_gradient(kind)
+        ctx.set_refine(refine)
+        want.append(ctx.grad_obj(w.srcx, w.srcz, Tobs))
+        ctxs.append(ctx)
+        ws.append(w)
+        tobs.append(Tobs)
+    got = R.grad_obj_multi(ctxs, [w.srcx for w in ws], [w.srcz for w in ws], tobs)
+    for (g, l2), (gw, lw) in zip(got, want):
+        assert np.array_equal(g, gw) and l2 == lw
