@@ -227,6 +227,9 @@ def run_gpu_arm(args, rank, world, local_rank):
     ctx.set_velocity(w.vp_true)
     _, Tobs, _ = ctx.forward(w.srcx, w.srcz, want_tt=False)  # observed picks (not timed)
     ctx.set_velocity(w.vp_start)
+    if args.profile_only:  # a profiler run may time another gradient path
+        ctx.set_gradient(args.gradient)
+        ctx.set_refine(args.refine)
     tobs_d = torch.from_numpy(np.ascontiguousarray(Tobs)).cuda()
     grad_d = torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda")
     l2_d = torch.empty(1, dtype=torch.float64, device="cuda")
@@ -758,6 +761,9 @@ def main():
     ap.add_argument("--no-ref-run", action="store_true", help="fatt: skip the reference-arithmetic comparison run")
     ap.add_argument("--profile-only", action="store_true",
                     help="only the device-timed loop (for profiler runs); no baselines, no JSON contract line")
+    ap.add_argument("--gradient", choices=["reference", "exact"], default="reference",
+                    help="with --profile-only: the gradient kind of the timed loop")
+    ap.add_argument("--refine", action="store_true", help="with --profile-only: refined traveltimes")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
