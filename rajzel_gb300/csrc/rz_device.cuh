@@ -342,9 +342,12 @@ struct DivDH {
         return __fdiv_rn(x, dh);
     }
     // numerators built from lambda, which can be tiny: the exhaustive check
-    // covers normal quotients only, so tiny ones take IEEE division
+    // covers normal quotients only, so tiny nonzero ones take IEEE division.
+    // A zero numerator (lambda is 0 outside the rays' reach, so zeros are
+    // common) gives a zero either way, at most with the other sign, which no
+    // later operation tells apart
     RZ_DEV float checked(float x) const {
-        if (fast && fabsf(x) >= 0x1p-96f) {
+        if (fast && (fabsf(x) >= 0x1p-96f || x == 0.0f)) {
             float q = __fmul_rn(x, rdh);
             float r = __fmaf_rn(-q, dh, x);
             return __fmaf_rn(r, rdh, q);
