@@ -374,7 +374,8 @@ RZ_DEV float leung_qian_ref(float tc, float te, float tw, float ts, float tn, fl
     float lhs = __fadd_rn(div(__fsub_rn(app, amm)), div(__fsub_rn(bpp, bmm)));
     float rhs = __fadd_rn(div.checked(__fsub_rn(__fmul_rn(amp, lw), __fmul_rn(apm, le))),
                           div.checked(__fsub_rn(__fmul_rn(bmp, ln), __fmul_rn(bpm, ls))));
-    float lt = (lhs > eps_adj) ? __fdiv_rn(rhs, lhs) : 0.0f;
+    // rhs / lhs; a zero rhs is its own quotient (lhs > 0), sign included
+    float lt = (lhs > eps_adj) ? (rhs == 0.0f ? rhs : __fdiv_rn(rhs, lhs)) : 0.0f;
     float r = fminf(own, lt);
     const float kInf = 9999999.0f;  // INF of fd.h:30
     if (tc >= kInf || ts >= kInf || tn >= kInf || te >= kInf || tw >= kInf) r = 0.0f;
