@@ -663,6 +663,18 @@ def run_workload(args, local_rank):
         pa = sum(ctx.shot_info(s)[1] for s in range(w.nshots))
         sw = np.array([ctx.shot_work(s) for s in range(w.nshots)]).sum(axis=0)
         pu = int(sw[0]) * w.nx * w.ny + int(sw[1]) * (w.nx - 2) * (w.ny - 2)  # sweeps actually run
+        # the same batch with the exact gradient of refined traveltimes: larger
+        # field slots, so more chunks under the same cap (one warm-up, one step)
+        ctx.set_gradient("exact")
+        ctx.set_refine(True)
+        step()
+        exact_ms = _events_ms(step, stream, 1)
+        if ctx.batch_status():
+            raise SystemExit(f"stress, exact gradient: device status bits 0x{ctx.batch_status():x}")
+        out["exact_gradient_run"] = {"value": w.nshots / (exact_ms / 1e3), "unit": "shots/s", "ms_per_step": exact_ms,
+                                     "refined": True}
+        ctx.set_gradient("reference")
+        ctx.set_refine(False)
         cores = os.cpu_count() or 1
         kind = cpu_kind()
         cpu_s = cpu_run(cores, cores, kind, "stress", w.nshots)
