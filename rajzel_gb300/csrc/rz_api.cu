@@ -426,7 +426,6 @@ static void fill_params(rz_context *c, ShotParams &P, int first, int n) {
     P.MB = c->dMB;
     P.T = c->dT;
     P.Told = c->dTold;
-    P.Sp = c->dSp;
     P.L = c->dL;
     P.TA = c->dTA;
     P.TB = c->dTB;

@@ -69,7 +69,6 @@ struct ShotParams {
     // per-shot fields; shot z at offset z*fstride (floats)
     float *T;               // traveltime  [nshots][ny][nxp]
     float *Told;            // reference-mode snapshot  [nshots][ny][nxp]
-    const float *Sp;        // slowness in rows of nxp floats [ny][nxp]
     float *L;               // adjoint field lambda [nshots][ny][nxp]
     float *TA, *TB;         // skewed traveltimes [nshots][nstrips][qn][32]
                             // (exact adjoint: signed x weights, see exact_coef)

@@ -889,98 +889,6 @@ __device__ __noinline__ int forward_is_fixpoint(const ShotParams &P, const CUten
     return (__syncthreads_or(change) ? 0 : 1) | (R.err << 1);
 }
 
-// Whether a pass of the traveltime refinement's linear sweeps would change a
-// correction delta: for every cell, m = r + (own weights) x (delta of the
-// upwind neighbours), with the weights and the float-float residual r of the
-// float traveltimes as the refinement's preparation computes them, against
-// the cell's delta (relative 1e-6, absolute 1e-9 s).  Returns 1 when no cell
-// would change, plus the error flags shifted left by one.
-// mT / mL: traveltime / delta fields, box kCheckHaloCols x kCheckBox.
-__device__ __noinline__ int tangent_is_converged(const ShotParams &P, const CUtensorMap *mT, const CUtensorMap *mL,
-                                                 int z, WarpShared *ws, int *found, volatile int *abort_word) {
-    const int nx = P.nx, ny = P.ny, nxp = P.nxp;
-    const int l = threadIdx.x & 31, g = threadIdx.x >> 5, W = blockDim.x >> 5;
-    const int cap = P.check_rows > 0 ? P.check_rows : kCheckRows;
-    const int nch = (nx + 127) >> 7, rt = check_task_rows(ny, nch, W, cap), nrb = (ny + rt - 1) / rt;
-    const int hs = P.src_h[z], ks = P.src_k[z];
-    const float big = 3.0e38f;
-    if (threadIdx.x == 0) *found = 0;
-    fence_proxy_async_smem();  // the ring's generic accesses precede the copies
-    __syncthreads();
-    CheckRing R{smem_u32(&ws->ring[0][0]), smem_u32(ws->cbar), smem_u32((const void *)abort_word), ws->cphase, 0};
-    bool change = false;
-    for (int task = g; task < nch * nrb && !change; task += W) {
-        if (__shfl_sync(0xffffffffu, *(volatile int *)found, 0)) break;  // warp-uniform
-        const int base = (task % nch) << 7, h0 = base + 4 * l;
-        // rows k0 .. k0+kk-1; window row j is grid row k0-1+j, j = 0 .. kk+1
-        const int k0 = (task / nch) * rt, kk = min(ny - k0, rt);
-        const int nb = ((kk + 1) >> 2) + 1;
-        auto issue = [&](int b) {
-            if (b >= nb || l != 0) return;
-            const uint32_t sl = R.base + (uint32_t)(b % kCheckSlots) * kCheckSlotA;
-            const uint32_t br = R.bars + 8u * (uint32_t)(b % kCheckSlots);
-            mbar_arrive_expect_tx_a(br, kCheckSlotA);
-            tma_load_3d_a(sl, mT, base - 4, k0 - 1 + kCheckBox * b, z, br);
-            tma_load_3d_a(sl + kCheckBox * kRowH, mL, base - 4, k0 - 1 + kCheckBox * b, z, br);
-        };
-        auto trow = [&](int j) {
-            return R.base + (uint32_t)((j >> 2) % kCheckSlots) * kCheckSlotA + (uint32_t)(j & 3) * kRowH;
-        };
-        issue(0), issue(1), issue(2);
-        __syncwarp();
-        R.wait(0);
-        for (int b = 0; b < nb; ++b) {
-#pragma unroll
-            for (int r = 0; r < kCheckBox; ++r) {
-                const int j = kCheckBox * b + r, k = k0 - 1 + j;
-                if (j < 1 || j > kk) continue;  // warp-uniform
-                if (r == kCheckBox - 1) R.wait(b + 1);  // holds row j+1
-                const uint32_t rc = trow(j), ru = trow(j - 1), rd = trow(j + 1);
-                const uint32_t lo = kCheckBox * kRowH;  // delta box follows the T box
-                const Row4 tc = box_row4(rc, l), lc = box_row4(rc + lo, l);
-                const float4 tu = lds4(ru + 16u + 16u * l), td = lds4(rd + 16u + 16u * l);
-                const float4 lu = lds4(ru + lo + 16u + 16u * l), ld = lds4(rd + lo + 16u + 16u * l);
-                const float4 s4 = h0 + 3 < nxp ? __ldg(reinterpret_cast<const float4 *>(P.Sp + (size_t)k * nxp + h0))
-                                               : make_float4(0.f, 0.f, 0.f, 0.f);
-                const float tuv[4] = {tu.x, tu.y, tu.z, tu.w}, tdv[4] = {td.x, td.y, td.z, td.w};
-                const float luv[4] = {lu.x, lu.y, lu.z, lu.w}, ldv[4] = {ld.x, ld.y, ld.z, ld.w};
-                const float sv[4] = {s4.x, s4.y, s4.z, s4.w};
-#pragma unroll
-                for (int i = 0; i < 4; ++i) {
-                    const int h = h0 + i;
-                    if (h >= nx) continue;
-                    CellNb n;
-                    n.tc = tc.v[i];
-                    n.tw = h > 0 ? (i == 0 ? tc.w : tc.v[i - 1]) : big;
-                    n.te = h < nx - 1 ? (i == 3 ? tc.e : tc.v[i + 1]) : big;
-                    n.tn = k > 0 ? tuv[i] : big;
-                    n.ts = k < ny - 1 ? tdv[i] : big;
-                    n.lw = n.le = n.ln = n.ls = 0.f;
-                    const bool src = h == hs && k == ks;
-                    // the weights exactly as the sweeps see them (packed, then unpacked)
-                    float wx, wz;
-                    unpack_weights(pack_weights(exact_coef_nb(n, sv[i], P.dh, src)), wx, wz);
-                    float m = cell_residual_nb(n, sv[i], P.dh, src);
-                    const float dw = i == 0 ? lc.w : lc.v[i - 1], de = i == 3 ? lc.e : lc.v[i + 1];
-                    m = fmaf(fmaxf(wx, 0.f), de, fmaf(fmaxf(-wx, 0.f), dw, m));
-                    m = fmaf(fmaxf(wz, 0.f), ldv[i], fmaf(fmaxf(-wz, 0.f), luv[i], m));
-                    const float own = lc.v[i];
-                    change |= !(fabsf(m - own) <= 1e-9f + 1e-6f * fabsf(own));
-                }
-            }
-            // box b-1 is read by no later row: box b+2 takes its slot
-            fence_proxy_async_smem();
-            __syncwarp();
-            if (b >= 1) issue(b + 2);
-        }
-        change = __any_sync(0xffffffffu, change);
-        if (change && l == 0) *(volatile int *)found = 1;
-    }
-    if (l == 0) ws->cphase = R.phase;
-    fence_proxy_async_smem();  // before the next sweep's copies into the ring
-    return (__syncthreads_or(change) ? 0 : 1) | (R.err << 1);
-}
-
 // the Leung-Qian update of interior, non-receiver cells (sweep_adj.c:26-30);
 // skip is the [ny][nxp] byte map of cells the adjoint sweeps leave unchanged.
 // mT / mL: traveltime / lambda fields, box kCheckHaloCols x kCheckBox.
@@ -1586,22 +1494,40 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                     break;
                 }
                 float acc = 0.f, mag = 0.f;
-                RZ_SWEEP(+1, +1, true, kModeTangent, &M.lld, &M.lst);
-                RZ_SWEEP(-1, +1, true, kModeTangent, &M.lld, &M.lst);
-                RZ_SWEEP(-1, -1, true, kModeTangent, &M.lld, &M.lst);
-                RZ_SWEEP(+1, -1, true, kModeTangent, &M.lld, &M.lst);
-                if (seq.pipelined) __syncthreads();
+                // a sweep's change against the magnitude of delta (a CTA-wide sum)
+                auto sweep_small = [&]() {
+                    if (seq.pipelined) __syncthreads();
+                    const double t = block_sum((double)acc, sh), m = block_sum((double)mag, sh);
+                    acc = 0.f, mag = 0.f;
+                    return !(t > 1e-7 * m);
+                };
+                if (tp == 0) {
+                    RZ_SWEEP(+1, +1, true, kModeTangent, &M.lld, &M.lst);
+                    RZ_SWEEP(-1, +1, true, kModeTangent, &M.lld, &M.lst);
+                    RZ_SWEEP(-1, -1, true, kModeTangent, &M.lld, &M.lst);
+                    RZ_SWEEP(+1, -1, true, kModeTangent, &M.lld, &M.lst);
+                    more = !sweep_small();
+                } else {
+                    // later passes one sweep at a time, as the exact adjoint's:
+                    // the first sweep that changes delta by less than 1e-7 of
+                    // its magnitude ends the solve
+                    RZ_SWEEP(+1, +1, true, kModeTangent, &M.lld, &M.lst);
+                    more = !sweep_small();
+                    if (more) {
+                        RZ_SWEEP(-1, +1, true, kModeTangent, &M.lld, &M.lst);
+                        more = !sweep_small();
+                    }
+                    if (more) {
+                        RZ_SWEEP(-1, -1, true, kModeTangent, &M.lld, &M.lst);
+                        more = !sweep_small();
+                    }
+                    if (more) {
+                        RZ_SWEEP(+1, -1, true, kModeTangent, &M.lld, &M.lst);
+                        more = !sweep_small();
+                    }
+                }
                 ++tp;
                 if (*w.abort_word) break;
-                const double tot = block_sum((double)acc, sh);
-                const double m = block_sum((double)mag, sh);
-                more = tot > 1e-7 * m;
-                if (more && tp < P.max_passes) {
-                    // stop a pass early when the next would change no cell
-                    const int cv = tangent_is_converged(P, &M.tchk, &M.lchk, z, &sh.w[g], &sh.ctl[2], w.abort_word);
-                    w.err |= cv >> 1;
-                    if (cv & 1) more = false;
-                }
             }
             __syncthreads();
             split_refined(P, T, L, Told);
