@@ -20,9 +20,11 @@
 // through a per-warp ring of three 33x32 shared-memory tiles filled by TMA
 // (cp.async.bulk.tensor) and written back by TMA; the extra row is the next
 // strip's first row (old values).  Read-only per-cell data (slowness,
-// converged traveltimes, adjoint skip bits) are stored pre-skewed so that the
-// 32 values one wavefront step needs are one 128-byte line: fully coalesced
-// and prefetched eight steps ahead into registers.
+// converged traveltimes, adjoint skip bits, the linear sweeps' packed weights
+// and receiver terms) are stored pre-skewed so that the 32 values one
+// wavefront step needs are one 128-byte line: fully coalesced, staged through
+// shared memory a group of eight steps ahead (the linear sweeps' second
+// stream through registers).
 #include <algorithm>
 #include <mutex>
 
