@@ -272,7 +272,11 @@ int rz_forward_f64(rz_context *ctx, int nshots, const float *srcx, const float *
 int rz_grad_obj_f64(rz_context *ctx, int nshots, const float *srcx, const float *srcz, const float *Tobs,
                     double *grad, double *L2, int flags);
 /* 1: later float calls also run the FP64 oracle on their inputs (the call
-   then synchronises and takes the oracle's time too); 0: off (default). */
+   then synchronises and takes the oracle's time too); 0: off (default).  With
+   refinement on (rz_set_refine) the oracle's forward runs to the fixpoint of
+   the discrete equations (until a pass changes no cell) instead of stopping
+   at TTNORM: on rough models the TTNORM-stopped iterate lies up to ~1e-5
+   from that fixpoint, which a refined field reaches. */
 int rz_set_error_check(rz_context *ctx, int enable);
 /* The error of the last checked call's results against the FP64 oracle. */
 int rz_error_report(rz_context *ctx, rz_error *err);
@@ -326,8 +330,8 @@ int rz_batch_status(rz_context *ctx, int *bits);
    run (forward, adjoint): 4 per swept pass.  A pass that a parallel fixpoint
    check proves to change no cell is counted in rz_shot_info's pass counts
    (the reference runs it) but not swept; after its first pass the exact
-   adjoint stops at the first sweep that changes mu by less than 1e-7 of its
-   magnitude, so its count need not be a multiple of 4. */
+   adjoint stops at the first sweep that moves no cell's mu by more than 1e-6
+   of its value, so its count need not be a multiple of 4. */
 int rz_shot_work(rz_context *ctx, int shot, int *fwd_swept, int *adj_swept);
 
 /* Fields of shot `shot` from the last rz_grad_obj: TT, lambda [ny][nx],

@@ -671,9 +671,12 @@ static void fill_fp64(const rz_context *c, F64Params &P, int first, int m) {
 // residual) are already on the device.  After each chunk's launch,
 // on_chunk(first, m) sees the double traveltimes of shots first..first+m-1
 // in the slots.  adjoint: gradient into d64Grad, misfit into d64L2 (also for
-// residual alone).  Returns the status of the shots.
+// residual alone).  fixpoint: the forward runs to the fixpoint of the
+// discrete equations instead of stopping at TTNORM.  Returns the status of
+// the shots.
 template <class F>
-static int run_fp64(rz_context *c, int n, bool adjoint, bool residual, bool exact, bool cotangent, F &&on_chunk) {
+static int run_fp64(rz_context *c, int n, bool adjoint, bool residual, bool exact, bool cotangent, F &&on_chunk,
+                    bool fixpoint = false) {
     int chunk = 0, r;
     if ((r = ensure_fp64(c, n, adjoint && exact, &chunk))) return r;
     if (!c->rec_set && (r = rz_set_receivers(c, 0, nullptr, nullptr))) return r;
@@ -686,6 +689,7 @@ static int run_fp64(rz_context *c, int n, bool adjoint, bool residual, bool exac
         P.do_adjoint = adjoint ? 1 : 0;
         P.exact = exact ? 1 : 0;
         P.cotangent = cotangent ? 1 : 0;
+        P.fixpoint = fixpoint ? 1 : 0;
         CK(launch_fp64_shots(P, c->st));
         c->launches += 1;
         if ((r = on_chunk(first, m))) return r;
@@ -724,7 +728,9 @@ static int ensure_cmp(rz_context *c, int entries) {
 // same inputs.  what: 0 forward (traveltimes, picks), 1 gradient (also the
 // gradient and misfit), 2 misfit (picks and misfit).  Traveltimes are
 // compared for the shots whose float fields are still in the slots (all of
-// them unless the batch ran in chunks).
+// them unless the batch ran in chunks).  A refined call is compared with the
+// FP64 fixpoint of the discrete equations, which its linear solve approximates;
+// an unrefined one with the FP64 run of the same algorithm, TTNORM included.
 static int error_check(rz_context *c, int n, int what) {
     const bool adjoint = what == 1, residual = what != 0;
     const bool exact = adjoint && c->grad_kind == RZ_GRADIENT_EXACT;
@@ -738,7 +744,7 @@ static int error_check(rz_context *c, int n, int what) {
             CK(launch_compare(c->dT + (size_t)(a - t0) * fsf, c->nxp, c->d64T + (size_t)(a - first) * fs64, c->g.nx,
                               c->g.nx, c->g.ny, b - a, fsf, fs64, c->dCmp + 4 * (size_t)(a - t0), c->st));
         return RZ_OK;
-    });
+    }, c->refine);
     if (r) return r;
     if (c->ntr > 0)
         CK(launch_compare(c->dTmod, c->ntr, c->d64Tmod, c->ntr, c->ntr, n, 1, 0, 0, c->dCmp + 4 * (size_t)ntt, c->st));

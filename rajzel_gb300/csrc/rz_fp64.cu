@@ -100,7 +100,10 @@ __device__ __noinline__ void sweep_fwd64(const F64Params &P, double *T) {
     }
 }
 
-// eikonal.c:31-57 in double; returns the passes run (status bits in *err)
+// eikonal.c:31-57 in double; returns the passes run (status bits in *err).
+// With P.fixpoint the loop ends at the first pass that changes no cell (the
+// updates only ever lower a value, so it ends), the fixpoint of the discrete
+// equations that a refined float field approximates.
 RZ_DEV int forward64(const F64Params &P, int z, double *T, double *Told, double *red, int *err) {
     const int hs = P.src_h[z], ks = P.src_k[z];
     for (size_t c = threadIdx.x; c < P.fstride; c += blockDim.x) T[c] = 2.0 * P.time;
@@ -109,7 +112,7 @@ RZ_DEV int forward64(const F64Params &P, int z, double *T, double *Told, double 
     __syncthreads();
     double l1 = 10.0 * P.time;
     int it = 0;
-    while (l1 >= P.ttnorm) {
+    while (P.fixpoint ? l1 > 0.0 : l1 >= P.ttnorm) {
         if (it >= P.max_passes) {
             *err |= ERR_NOCONV_FWD;
             break;

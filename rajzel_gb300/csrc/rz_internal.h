@@ -201,6 +201,7 @@ struct F64Params {
     int nx, ny, nxp;
     double dh, time, ttnorm, eps_adj;  // the float globals, widened
     int max_passes;
+    int fixpoint;                // forward: sweep until a pass changes no cell (TTNORM not used)
     int nshots;
     int do_residual, do_adjoint;
     int exact;                   // adjoint: 0 Leung-Qian, 1 exact discrete adjoint

@@ -184,7 +184,7 @@ constexpr uint32_t kRingBytes = kRing * kSlotBytes;           // 12672
 // division path out of the step code
 template <int DX, int DY, bool ADJ, int MODE, int DIV = 1>
 __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mld, const CUtensorMap *mst,
-                                   float &acc, float &mag, int band, int W, const SweepSeq &seq) {
+                                   float &acc, uint32_t &moved, int band, int W, const SweepSeq &seq) {
     // linear sweeps over weight streams: the exact discrete adjoint, mu = R +
     // the weights neighbours put on this cell; the traveltime refinement (TAN),
     // delta = r + this cell's weights on its upwind neighbours
@@ -269,7 +269,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     uint32_t phase = w.phase;
     int err = 0;
     float acc_l = 0.f;  // fast-mode sum of |change| (the caller's acc lives in local memory)
-    float mag_l = 0.f;  // exact adjoint: sum of |mu|
+    uint32_t moved_l = 0;  // linear sweeps: this lane moved a cell by more than 1e-6 of its value
     auto ring_wait_l = [&](int slot) {
         if (!mbar_wait_copy(mbar_s + 8u * slot, (phase >> slot) & 1u)) err |= ERR_TMA_TIMEOUT;
         phase ^= 1u << slot;
@@ -558,7 +558,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                         m = wzS < 0.f ? fmaf(-wzS, lS, m) : m;
                     }
                     r = valid ? m : own;
-                    mag_l += valid ? fabsf(r) : 0.0f;
                     w_tt = c_tt;
                     c_tt = e_wx;
                     w_wz = c_wz;
@@ -588,7 +587,8 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                 }
                 sts(cur, r);
                 if (MODE == kModeFast) acc_l += valid ? own - r : 0.0f;
-                if (EX) acc_l += valid ? fabsf(own - r) : 0.0f;
+                // linear sweeps: a cell moved by more than 1e-6 of its value
+                if (EX) moved_l |= (uint32_t)(valid && !(fabsf(own - r) <= 1e-6f * fabsf(r)));
                 if (ii == 0) h0 = r;
                 if (ii == 1) h1 = r;
                 if (ii == 2) sts4_if(hq, hand_carry, h0, h1, r, hand);
@@ -631,7 +631,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     w.phase = phase;
     w.err |= err;
     acc += acc_l;
-    mag += mag_l;
+    moved |= moved_l;
 }
 
 // ---------------------------------------------------------------------------
@@ -1421,7 +1421,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
 #define RZ_SWEEP_D(DX_, DY_, ADJ_, MODE_, DIV_, LD_, ST_)                           \
     do {                                                                           \
         for (int b = 0; b < nbands; ++b) {                                         \
-            sweep<DX_, DY_, ADJ_, MODE_, DIV_>(P, w, LD_, ST_, acc, mag, b, W, seq); \
+            sweep<DX_, DY_, ADJ_, MODE_, DIV_>(P, w, LD_, ST_, acc, moved, b, W, seq); \
             if (!seq.pipelined) sweep_barrier(sh);                                 \
         }                                                                          \
         seq.advance(DY_);                                                          \
@@ -1450,7 +1450,8 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                 fence_proxy_async_global();
                 __syncthreads();
             }
-            float acc = 0.f, mag = 0.f;
+            float acc = 0.f;
+            uint32_t moved = 0;
             RZ_SWEEP(+1, +1, false, MODE, pTld, &M.tst);
             if (pass == 0) stamp(P, z, 5);
             RZ_SWEEP(-1, +1, false, MODE, pTld, &M.tst);
@@ -1481,9 +1482,10 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             // Traveltime refinement to the FP64 fixpoint (not in the
             // reference): delta = r + W delta with r the float-float residual
             // of every cell and W the weights of the float field, solved by the
-            // linear sweeps in the forward orders until a pass changes delta by
-            // less than 1e-7 of its magnitude; then T := RN(T + delta) and
-            // Told := the remainder, so T + Told is the refined field.
+            // linear sweeps in the forward orders until a sweep after the first
+            // pass moves no cell's delta by more than 1e-6 of its value; then
+            // T := RN(T + delta) and Told := the remainder, so T + Told is the
+            // refined field.
             __syncthreads();
             stamp(P, z, 7);
             exact_prepare(P, w, pTld, &M.tlo, z, T, L, true);
@@ -1495,13 +1497,14 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                     cta_err |= ERR_NOCONV_FWD;
                     break;
                 }
-                float acc = 0.f, mag = 0.f;
-                // a sweep's change against the magnitude of delta (a CTA-wide sum)
+                float acc = 0.f;
+                uint32_t moved = 0;
+                // whether the sweep (or pass) just run moved no cell by more
+                // than 1e-6 of its value (a CTA-wide vote, with the barrier)
                 auto sweep_small = [&]() {
-                    if (seq.pipelined) __syncthreads();
-                    const double t = block_sum((double)acc, sh), m = block_sum((double)mag, sh);
-                    acc = 0.f, mag = 0.f;
-                    return !(t > 1e-7 * m);
+                    const int any = __syncthreads_or((int)moved);
+                    moved = 0;
+                    return any == 0;
                 };
                 if (tp == 0) {
                     RZ_SWEEP(+1, +1, true, kModeTangent, &M.lld, &M.lst);
@@ -1511,8 +1514,8 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                     more = !sweep_small();
                 } else {
                     // later passes one sweep at a time, as the exact adjoint's:
-                    // the first sweep that changes delta by less than 1e-7 of
-                    // its magnitude ends the solve
+                    // the first sweep that moves no cell by more than 1e-6 of
+                    // its value ends the solve
                     RZ_SWEEP(+1, +1, true, kModeTangent, &M.lld, &M.lst);
                     more = !sweep_small();
                     if (more) {
@@ -1653,21 +1656,22 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             fence_proxy_async_global();
             __syncthreads();
         }
-        float acc = 0.f, mag = 0.f;
-        bool sweep_stop = false;  // exact adjoint: a sweep of a later pass changed mu by < 1e-7 of |mu|
+        float acc = 0.f;
+        uint32_t moved = 0;
+        bool sweep_stop = false;  // exact adjoint: a sweep of a later pass moved no cell by > 1e-6 of its value
         int nsweeps = 4;          // sweeps this pass runs
         if (P.exact && pass > 0) {
             // After the first pass, one sweep at a time: a sweep visits every
             // cell, so a sweep that changes no cell proves the fixpoint (its
-            // updates all saw the final values), and one that changes mu by
-            // less than 1e-7 of its magnitude bounds every cell's residual as
-            // a pass of such sweeps would; the remaining sweeps of the pass
-            // are left out.
+            // updates all saw the final values), and one that moves no cell
+            // by more than 1e-6 of its value bounds every cell's residual as a
+            // pass of such sweeps would; the remaining sweeps of the pass are
+            // left out.  (A grid-wide sum of the changes would not do: a region
+            // the solution has not reached yet moves little in such a sum.)
             auto sweep_small = [&]() {
-                if (seq.pipelined) __syncthreads();
-                const double t = block_sum((double)acc, sh), m = block_sum((double)mag, sh);
-                acc = 0.f, mag = 0.f;
-                return !(t > 1e-7 * m);
+                const int any = __syncthreads_or((int)moved);
+                moved = 0;
+                return any == 0;
             };
             nsweeps = 1;
             RZ_SWEEP(+1, +1, true, kModeExact, &M.lld, &M.lst);
@@ -1715,11 +1719,9 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             go = !sweep_stop;
         } else if (P.exact) {
             // the adjoint system is triangular in arrival order: Gauss-Seidel
-            // sweeps reach its solution exactly; stop once a pass changes it
-            // by less than 1e-7 of its magnitude
-            double tot = block_sum((double)acc, sh);
-            double m = block_sum((double)mag, sh);
-            go = tot > 1e-7 * m;
+            // sweeps reach its solution exactly; stop once a pass moves no
+            // cell by more than 1e-6 of its value
+            go = __syncthreads_or((int)moved) != 0;
         } else if (MODE == kModeReference) {
             go = ref_continue(P, L, Told, sh);
         } else {

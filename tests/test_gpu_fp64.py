@@ -224,6 +224,47 @@ def test_refined_exact_gradient_within_1e4_at_full_size(R):
     assert reps["reference", True]["grad_rel_l2"] <= reps["reference", False]["grad_rel_l2"]
 
 
+@pytest.mark.parametrize("nx,ny", [(5, 4), (33, 31), (70, 600), (257, 40)])
+def test_refined_paths_on_odd_and_banded_shapes(R, nx, ny):
+    """Shapes that are not multiples of the 32-row strip or 32-column block,
+    a 5 x 4 grid, and a 600-row grid swept in bands, on rough random models
+    with interior sources: refined traveltimes are within 3e-7 of the FP64
+    fixpoint, and the exact gradient of refined traveltimes within 1e-4 of
+    the FP64 exact gradient (error report of the same call).  On these models
+    the TTNORM-stopped iterate lies up to 1.7e-5 from the fixpoint (70 x 600),
+    so the one linear solve starts where upwind choices still flip at
+    near-ties; 3e-7 covers what that leaves (2.0e-7 measured)."""
+    w = synth.small_case(700 + nx, nx, ny, nshots=3)
+    Tobs = picks(R, w)
+    ctx = ctx_for(R, w, "fast", kind="exact", refine=True)
+    ctx.set_error_check(True)
+    ctx.grad_obj(w.srcx, w.srcz, Tobs)
+    rep = ctx.error_report()
+    assert rep["shots"] == 3 and rep["tt_rel"] <= 3e-7, rep
+    assert rep["grad_rel_l2"] <= GRAD_TOL, rep
+
+
+def test_refined_error_check_compares_with_the_fixpoint(R):
+    """The error check of a refined call runs the FP64 forward to the fixpoint
+    of the discrete equations, that of an unrefined call stops at TTNORM as the
+    reference does: on a rough 70 x 600 model the refined field is within 3e-7
+    of the first, while the reference's float field (8-9 passes, as the
+    TTNORM-stopped FP64 run; the fixpoint takes 19-22) is within 1.2e-6 of the
+    second and 1.7e-5 from the first (the CPU oracles measure the same)."""
+    w = synth.small_case(770, 70, 600, nshots=3)
+    ctx = ctx_for(R, w, "fast", refine=True)
+    ctx.set_error_check(True)
+    TT1, _, _ = ctx.forward(w.srcx, w.srcz)
+    assert ctx.error_report()["tt_rel"] <= 3e-7
+    ctx0 = ctx_for(R, w, "reference")
+    ctx0.set_error_check(True)
+    TT0, _, _ = ctx0.forward(w.srcx, w.srcz)
+    assert ctx0.error_report()["tt_rel"] <= 2e-6
+    T64, _ = ctx_for(R, w, "fast", ttnorm=1e-30).forward_f64(w.srcx, w.srcz)
+    assert tt_rel(TT1, T64) <= 3e-7
+    assert tt_rel(TT0, T64) >= 1e-5
+
+
 def test_refined_exact_gradient_central_differences_config2(R):
     """<g, dS> of the refined exact gradient against central differences of
     the FP64 misfit (GPU FP64 oracle) on 20 random slowness perturbations, 16
