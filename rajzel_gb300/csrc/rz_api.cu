@@ -367,7 +367,9 @@ static int ensure_div(rz_context *c) {
     CK(cudaMemcpyAsync(&hbad, dbad, sizeof(unsigned int), cudaMemcpyDeviceToHost, c->st));
     CK(cudaStreamSynchronize(c->st));
     cudaFree(dbad);
-    c->div_fast = (hbad == 0);
+    // the check covers x in [1,2); it carries to every exponent the sweeps use
+    // for DH within [2^-20, 2^20] (quotients and remainders stay normal)
+    c->div_fast = (hbad == 0) && c->g.dh >= 0x1p-20f && c->g.dh <= 0x1p20f;
     c->div_dh = c->g.dh;
     return RZ_OK;
 }

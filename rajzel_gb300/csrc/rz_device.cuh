@@ -327,32 +327,59 @@ RZ_DEV float godunov_fast(float a, float b, float s, float dh) {
 // per-DH check the host runs before enabling it (rz_check_div); otherwise
 // IEEE division is used.
 // ---------------------------------------------------------------------------
+// RN(a/b), b > 0, from qs = RN(a*2^64 / b) and its remainder rs = a*2^64 -
+// qs*b (exact: the remainder of a correctly rounded quotient is representable
+// when nothing underflows, true for |a*2^64| >= 2^-85).  qs*2^-64 is exact
+// and equals RN(a/b) while it is normal.  For a subnormal result RN(qs*2^-64)
+// rounds a second time, which can go wrong only where qs*2^-64 lies exactly
+// halfway between two subnormals: every such midpoint is a 24-bit number at
+// that scale, so none lies strictly between a/b and qs*2^-64.  At a midpoint
+// the remainder's sign says on which side a/b lies (none: a tie, to even).
+// Scaling numerators this way keeps tiny ones off IEEE division's slow path.
+RZ_DEV float unscale_quotient(float qs, float rs) {
+    const float q = __fmul_rn(qs, 0x1p-64f);
+    const bool mid = fabsf(__fmaf_rn(q, 0x1p64f, -qs)) == 0x1p-86f;
+    const float qm = __fmul_rn(__fadd_rn(qs, rs > 0.0f ? 0x1p-86f : -0x1p-86f), 0x1p-64f);
+    return (mid && rs != 0.0f) ? qm : q;
+}
+
+// RN(a/b) for b > 0: a tiny numerator (|a| < 2^-96) is divided at 2^64 times
+// its size (b within [2^-60, 2^40] keeps that quotient normal), any other one
+// by IEEE division
+RZ_DEV float div_rn_tiny_scaled(float a, float b) {
+    const bool tiny = fabsf(a) < 0x1p-96f && b >= 0x1p-60f && b <= 0x1p40f;
+    const float as = tiny ? __fmul_rn(a, 0x1p64f) : a;
+    const float q = __fdiv_rn(as, b);
+    return tiny ? unscale_quotient(q, __fmaf_rn(-q, b, as)) : q;
+}
+
 struct DivDH {
     float dh, rdh;
     bool fast;
     // numerators that are never tiny (differences of traveltimes): a zero
     // numerator may come out as +0 instead of -0, which no later operation
     // of the sweep can tell apart (no division by it, no sign test)
-    RZ_DEV float operator()(float x) const {
-        if (fast) {
-            float q = __fmul_rn(x, rdh);
-            float r = __fmaf_rn(-q, dh, x);
-            return __fmaf_rn(r, rdh, q);
-        }
-        return __fdiv_rn(x, dh);
-    }
-    // numerators built from lambda, which can be tiny: the exhaustive check
-    // covers normal quotients only, so tiny nonzero ones take IEEE division.
-    // A zero numerator (lambda is 0 outside the rays' reach, so zeros are
-    // common) gives a zero either way, at most with the other sign, which no
-    // later operation tells apart
+    RZ_DEV float operator()(float x) const { return fast ? markstein(x) : __fdiv_rn(x, dh); }
+    // numerators built from lambda, which can be tiny.  The exhaustive check
+    // tries every significand of x in [1,2); scaling by powers of two carries
+    // it to every x whose quotient and Markstein remainder stay normal, which
+    // holds for |x| >= 2^-96 (DH within [2^-20, 2^20]).  A smaller x (lambda
+    // decays to tiny and subnormal values away from the rays, so such
+    // numerators are common, and IEEE division of them is slow) is divided at
+    // 2^64 times its size and brought back by unscale_quotient.  A zero
+    // numerator gives a zero either way, at most with the other sign, which no
+    // later operation tells apart.
     RZ_DEV float checked(float x) const {
-        if (fast && (fabsf(x) >= 0x1p-96f || x == 0.0f)) {
-            float q = __fmul_rn(x, rdh);
-            float r = __fmaf_rn(-q, dh, x);
-            return __fmaf_rn(r, rdh, q);
-        }
-        return __fdiv_rn(x, dh);
+        if (!fast) return __fdiv_rn(x, dh);
+        const bool tiny = fabsf(x) < 0x1p-96f;
+        const float xs = tiny ? __fmul_rn(x, 0x1p64f) : x;
+        const float qs = markstein(xs);
+        return tiny ? unscale_quotient(qs, __fmaf_rn(-qs, dh, xs)) : qs;
+    }
+    RZ_DEV float markstein(float x) const {
+        float q = __fmul_rn(x, rdh);
+        float r = __fmaf_rn(-q, dh, x);
+        return __fmaf_rn(r, rdh, q);
     }
 };
 
@@ -375,7 +402,7 @@ RZ_DEV float leung_qian_ref(float tc, float te, float tw, float ts, float tn, fl
     float rhs = __fadd_rn(div.checked(__fsub_rn(__fmul_rn(amp, lw), __fmul_rn(apm, le))),
                           div.checked(__fsub_rn(__fmul_rn(bmp, ln), __fmul_rn(bpm, ls))));
     // rhs / lhs; a zero rhs is its own quotient (lhs > 0), sign included
-    float lt = (lhs > eps_adj) ? (rhs == 0.0f ? rhs : __fdiv_rn(rhs, lhs)) : 0.0f;
+    float lt = (lhs > eps_adj) ? (rhs == 0.0f ? rhs : div_rn_tiny_scaled(rhs, lhs)) : 0.0f;
     float r = fminf(own, lt);
     const float kInf = 9999999.0f;  // INF of fd.h:30
     if (tc >= kInf || ts >= kInf || tn >= kInf || te >= kInf || tw >= kInf) r = 0.0f;

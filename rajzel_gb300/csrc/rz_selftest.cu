@@ -7,6 +7,13 @@
 // DH from the workload set) and compares the certified float-float evaluation
 // of the reference's double branch (godunov_ref) with a direct evaluation of
 // that branch in double.  Any mismatch is a defect.
+//
+// rz_selftest_div_tiny compares the divisions of tiny numerators (below
+// 2^-96, down to the smallest subnormal; quotients normal and subnormal) with
+// IEEE division bit for bit: DivDH::checked for a given DH (after the
+// exhaustive check of Markstein's division for that DH that the engine runs
+// before using it) and div_rn_tiny_scaled for divisors spread log-uniformly
+// over [1e-9, 1e3].
 #include <cuda_runtime.h>
 
 #include "rz_device.cuh"
@@ -126,4 +133,59 @@ extern "C" int rz_selftest_weights(const float *wx, const float *wz, long n, flo
     if (e == cudaSuccess) e = cudaMemcpy(packed, d + 4 * n, n * sizeof(float), cudaMemcpyDeviceToHost);
     cudaFree(d);
     return e == cudaSuccess ? 0 : 3;
+}
+
+namespace {
+
+__global__ void div_check_dh(float dh, float rcp, unsigned long long *bad) {
+    const unsigned int m = blockIdx.x * blockDim.x + threadIdx.x;
+    if (m >= (1u << 23)) return;
+    const float x = __uint_as_float(0x3f800000u | m);
+    if (__float_as_uint(rz::DivDH{dh, rcp, true}.markstein(x)) != __float_as_uint(__fdiv_rn(x, dh)))
+        atomicAdd(bad, 1ull);
+}
+
+// a nonzero float below 2^-96: half the draws subnormal bit patterns, half
+// normal ones with exponents -126..-97
+__device__ float tiny_float(uint64_t seed, uint64_t i, int k) {
+    const uint32_t u = mix(seed * 0x9E3779B97F4A7C15ULL + i * 8 + k);
+    const uint32_t sig = (u >> 9) & 0x7fffffu;
+    uint32_t bits;
+    if (u & 1u) bits = sig ? sig : 1u;
+    else bits = ((1u + (mix(u) % 30u)) << 23) | sig;  // biased exponents 1..30
+    return __uint_as_float(bits | ((u & 2u) << 30));
+}
+
+__global__ void div_tiny_check(uint64_t seed, long n, float dh, float rcp, unsigned long long *bad) {
+    const long i = (long)blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const float x = tiny_float(seed, i, 0);
+    const rz::DivDH d{dh, rcp, true};
+    if (__float_as_uint(d.checked(x)) != __float_as_uint(__fdiv_rn(x, dh))) atomicAdd(bad, 1ull);
+    const float a = tiny_float(seed, i, 1);
+    const float b = exp2f(-29.9f + 39.9f * unif(seed, i, 2));  // ~1e-9 .. ~1e3
+    if (__float_as_uint(rz::div_rn_tiny_scaled(a, b)) != __float_as_uint(__fdiv_rn(a, b))) atomicAdd(bad + 1, 1ull);
+}
+
+}  // namespace
+
+// bad_out[0]: DivDH::checked mismatches, [1]: div_rn_tiny_scaled mismatches.
+// Returns 4 when Markstein's division is not exact for this DH (the engine
+// then uses IEEE division; nothing to test).
+extern "C" int rz_selftest_div_tiny(unsigned long long seed, long n, float dh, unsigned long long *bad_out) {
+    unsigned long long *d = nullptr;
+    if (cudaMalloc(&d, 3 * sizeof(unsigned long long)) != cudaSuccess) return 3;
+    cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+    const float rcp = (float)(1.0 / (double)dh);
+    div_check_dh<<<(1u << 23) / 256, 256>>>(dh, rcp, d + 2);
+    div_tiny_check<<<(unsigned)((n + 255) / 256), 256>>>(seed, n, dh, rcp, d);
+    cudaError_t e = cudaDeviceSynchronize();
+    unsigned long long h[3] = {0, 0, 0};
+    cudaMemcpy(h, d, sizeof h, cudaMemcpyDeviceToHost);
+    cudaFree(d);
+    if (e != cudaSuccess) return 3;
+    if (h[2]) return 4;
+    bad_out[0] = h[0];
+    bad_out[1] = h[1];
+    return 0;
 }

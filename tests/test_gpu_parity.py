@@ -153,6 +153,29 @@ def test_eikonal_adj_entry_point(R):
     assert np.array_equal(lam, lo) and passes == po
 
 
+@pytest.mark.parametrize("scale", [1e-29, 1e-36])
+def test_eikonal_adj_tiny_lambda(R, scale):
+    """Residuals scaled by 1e-29 and 1e-36 make the numerators of sweep_adj.c's
+    rhs/DH divisions tiny: below 2^-96, where Markstein's division by DH runs
+    on the numerator scaled by 2^64, and (1e-36) so small that the quotient is
+    subnormal, which takes IEEE division.  Lambda stays bit-exact with the
+    reference algorithm."""
+    w = synth.small_case(99, 80, 70, nshots=1)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    to, _ = O.eikonal(p, S, w.srcx[0], w.srcz[0])
+    Tmod = O.calc_fa(p, to, w.recx, w.recz)
+    Tres, _ = O.calc_res(p, to, Tmod, Tmod * np.float32(1.02), w.recx, w.recz)
+    Tres = (Tres.astype(np.float64) * scale).astype(np.float32)
+    assert np.all(Tres != 0)
+    ctx = make_ctx(R, w)
+    lam, passes = ctx.eikonal_adj(to, Tres)
+    lo, po = O.eikonal_adj(p, to, Tres, w.recx, w.recz)
+    assert np.array_equal(lam, lo) and passes == po
+    nz = np.abs(lo[lo != 0])  # cells with lambda this small give numerators below 2^-96 / subnormal quotients
+    assert np.any(nz < (1e-26 if scale == 1e-29 else 1.1754944e-38))
+
+
 def test_batched_equals_single_shot(R):
     w = synth.small_case(5, 120, 90, nshots=5)
     ctx = make_ctx(R, w)
@@ -250,6 +273,21 @@ def test_certified_godunov_branch_matches_double(R):
     bad = C.c_ulonglong(1)
     assert lib.rz_selftest_godunov(12345, 20_000_000, C.byref(bad)) == 0
     assert bad.value == 0
+
+
+@pytest.mark.parametrize("dh", [10.0, 5.0, 12.5, 20.0, 7.3])
+def test_tiny_numerator_divisions_match_ieee(R, dh):
+    """Divisions of numerators below 2^-96 (normal and subnormal, quotients
+    down to the subnormal range): by DH (Markstein at 2^64 times the size) and
+    by a general positive divisor, bit for bit against IEEE division on 2e7
+    random draws each."""
+    lib = C.CDLL(os.path.join(os.path.dirname(R.__file__), "librz_selftest.so"))
+    lib.rz_selftest_div_tiny.argtypes = [C.c_ulonglong, C.c_long, C.c_float, C.POINTER(C.c_ulonglong)]
+    bad = (C.c_ulonglong * 2)(1, 1)
+    rc = lib.rz_selftest_div_tiny(99, 20_000_000, dh, bad)
+    if rc == 4:
+        pytest.skip(f"Markstein division not exact for DH={dh}; the engine uses IEEE division")
+    assert rc == 0 and (bad[0], bad[1]) == (0, 0)
 
 
 def _shot_sum(R, vals):
