@@ -254,7 +254,10 @@ RZ_DEV float sel_gt(float x, float y, float u, float v) {
 // the same float.  Otherwise the exact double path runs; that happens for
 // roughly one update in ten thousand.
 // ---------------------------------------------------------------------------
-RZ_DEV float godunov_branch2_f64(float sum, float d, float s, float dh) {
+// Out of line: inlined into the sweep step, its double-precision code made a
+// reference-mode forward pass ~13% slower although it runs for one update in
+// ten thousand.
+static __device__ __noinline__ float godunov_branch2_f64(float sum, float d, float s, float dh) {
     double sd = (double)s, hd = (double)dh, dd = (double)d;
     double p = __dmul_rn(__dmul_rn(2.0, __dmul_rn(sd, sd)), __dmul_rn(hd, hd));
     double q = __dsub_rn(p, __dmul_rn(dd, dd));

@@ -685,11 +685,31 @@ RZ_DEV void sweep_barrier(const CtaShared &sh) {
 // is replayed (rare).
 RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold, const CtaShared &sh) {
     const int n = P.nx * P.ny;
+    // the estimate: each warp takes rows, each lane 16-byte pieces of them,
+    // four pieces in flight; padding columns (h >= nx) count zero
+    const int W = blockDim.x >> 5, g = threadIdx.x >> 5, l = threadIdx.x & 31, nq = P.nxp >> 2;
     float part = 0.f;
-    for (int c = threadIdx.x; c < n; c += blockDim.x) {
-        int k = c / P.nx, h = c - k * P.nx;
-        size_t o = (size_t)k * P.nxp + h;
-        part += fabsf(__fsub_rn(__ldcg(F + o), __ldcg(Fold + o)));
+    auto piece = [&](const float4 x, const float4 y, int q) {
+        const int h = 4 * q;
+        const float d0 = h < P.nx ? fabsf(__fsub_rn(x.x, y.x)) : 0.f;
+        const float d1 = h + 1 < P.nx ? fabsf(__fsub_rn(x.y, y.y)) : 0.f;
+        const float d2 = h + 2 < P.nx ? fabsf(__fsub_rn(x.z, y.z)) : 0.f;
+        const float d3 = h + 3 < P.nx ? fabsf(__fsub_rn(x.w, y.w)) : 0.f;
+        part = __fadd_rn(part, __fadd_rn(__fadd_rn(d0, d1), __fadd_rn(d2, d3)));
+    };
+    for (int k = g; k < P.ny; k += W) {
+        const float4 *a = reinterpret_cast<const float4 *>(F + (size_t)k * P.nxp);
+        const float4 *b = reinterpret_cast<const float4 *>(Fold + (size_t)k * P.nxp);
+        int q = l;
+        for (; q + 96 < nq; q += 128) {
+            const float4 x0 = __ldcg(a + q), x1 = __ldcg(a + q + 32), x2 = __ldcg(a + q + 64), x3 = __ldcg(a + q + 96);
+            const float4 y0 = __ldcg(b + q), y1 = __ldcg(b + q + 32), y2 = __ldcg(b + q + 64), y3 = __ldcg(b + q + 96);
+            piece(x0, y0, q);
+            piece(x1, y1, q + 32);
+            piece(x2, y2, q + 64);
+            piece(x3, y3, q + 96);
+        }
+        for (; q < nq; q += 32) piece(__ldcg(a + q), __ldcg(b + q), q);
     }
     double est = block_sum((double)part, sh);
     if (threadIdx.x == 0) {
@@ -697,7 +717,9 @@ RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold,
         if (est == 0.0) {
             decision = 0;
         } else {
-            double per = (double)(n / (int)blockDim.x + 2);
+            // float additions in one thread's part: 4 per piece, (ny/W + 1)
+            // rows of nq/32 + 1 pieces
+            double per = 4.0 * (double)((P.ny / W + 1) * (nq / 32 + 1)) + 2.0;
             double gam = ((double)n + per + 4.0) * 0x1p-24 + 0x1p-20;
             double thr = (double)P.ttnorm * (double)n;
             if (est * (1.0 - gam) > thr * (1.0 + 0x1p-21)) decision = 1;
@@ -993,12 +1015,21 @@ __device__ __noinline__ int adjoint_is_fixpoint(const ShotParams &P, const CUten
 
 // whole padded rows, a warp per row, 16-byte accesses (rows are 128-byte aligned)
 RZ_DEV void copy_field(const ShotParams &P, const float *src, float *dst) {
-    const int W = blockDim.x >> 5, g = threadIdx.x >> 5, l = threadIdx.x & 31, nq = P.nxp >> 2;
-    for (int k = g; k < P.ny; k += W) {
-        const float4 *a = reinterpret_cast<const float4 *>(src + (size_t)k * P.nxp);
-        float4 *b = reinterpret_cast<float4 *>(dst + (size_t)k * P.nxp);
-        for (int q = l; q < nq; q += 32) b[q] = __ldcg(a + q);
+    // the padded rows are one contiguous block of ny*nxp floats (nxp a
+    // multiple of 4); four 16-byte loads in flight per thread
+    const int n4 = P.ny * (P.nxp >> 2), st = blockDim.x;
+    const float4 *a = reinterpret_cast<const float4 *>(src);
+    float4 *b = reinterpret_cast<float4 *>(dst);
+    int i = threadIdx.x;
+    for (; i + 3 * st < n4; i += 4 * st) {
+        const float4 v0 = __ldcg(a + i), v1 = __ldcg(a + i + st), v2 = __ldcg(a + i + 2 * st),
+                     v3 = __ldcg(a + i + 3 * st);
+        __stcg(b + i, v0);
+        __stcg(b + i + st, v1);
+        __stcg(b + i + 2 * st, v2);
+        __stcg(b + i + 3 * st, v3);
     }
+    for (; i < n4; i += st) __stcg(b + i, __ldcg(a + i));
 }
 
 // F := v on every padded row; with frame0 the frame (rows 0 and ny-1,
