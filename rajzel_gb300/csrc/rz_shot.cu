@@ -268,7 +268,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     const uint32_t empty_out = smem_u32(down->empty);
     uint32_t phase = w.phase;
     int err = 0;
-    float acc_l = 0.f;  // fast-mode sum of |change| (the caller's acc lives in local memory)
+    float acc_l = 0.f;  // sum of the changes (the stopping rule; the caller's acc lives in local memory)
     // linear sweeps: sum of |value| over the sweep, returned in mag.  No
     // stopping rule reads it, but with it the compiler schedules the linear
     // step differently and the exact sweeps run faster (GB300, 100-shot
@@ -592,7 +592,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     c_tt = e_tt;
                 }
                 sts(cur, r);
-                if (MODE == kModeFast) acc_l += valid ? own - r : 0.0f;
+                if (MODE == kModeFast || MODE == kModeReference) acc_l += valid ? own - r : 0.0f;
                 // linear sweeps: a cell moved by more than 1e-6 of its value
                 if (EX) moved_l |= (uint32_t)(valid && !(fabsf(own - r) <= 1e-6f * fabsf(r)));
                 if (ii == 0) h0 = r;
@@ -680,47 +680,23 @@ RZ_DEV void sweep_barrier(const CtaShared &sh) {
 
 // Reference stopping rule (norm1.c:20-29, eikonal.c:44): continue while
 // mean|F-Fold| >= TTNORM, the mean being a sequential float sum in x-outer
-// order.  A parallel estimate decides whenever it is certain; within the
-// worst-case rounding window of the sequential sum the exact sequential sum
-// is replayed (rare).
-RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold, const CtaShared &sh) {
+// order.  The estimate is the pass's own change: every update is
+// min(own, new), so a cell's changes over the pass's sweeps add up to
+// Fold - F, and each lane summed its cells' changes (`acc`; `terms`
+// bounds a lane's float additions, the per-sweep totals included).  It decides whenever it is certain;
+// within the worst-case rounding window of the sequential sum and of the
+// estimate the exact sequential sum is replayed from F and Fold (rare).
+RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold, const CtaShared &sh, float acc,
+                         double terms) {
     const int n = P.nx * P.ny;
-    // the estimate: each warp takes rows, each lane 16-byte pieces of them,
-    // four pieces in flight; padding columns (h >= nx) count zero
-    const int W = blockDim.x >> 5, g = threadIdx.x >> 5, l = threadIdx.x & 31, nq = P.nxp >> 2;
-    float part = 0.f;
-    auto piece = [&](const float4 x, const float4 y, int q) {
-        const int h = 4 * q;
-        const float d0 = h < P.nx ? fabsf(__fsub_rn(x.x, y.x)) : 0.f;
-        const float d1 = h + 1 < P.nx ? fabsf(__fsub_rn(x.y, y.y)) : 0.f;
-        const float d2 = h + 2 < P.nx ? fabsf(__fsub_rn(x.z, y.z)) : 0.f;
-        const float d3 = h + 3 < P.nx ? fabsf(__fsub_rn(x.w, y.w)) : 0.f;
-        part = __fadd_rn(part, __fadd_rn(__fadd_rn(d0, d1), __fadd_rn(d2, d3)));
-    };
-    for (int k = g; k < P.ny; k += W) {
-        const float4 *a = reinterpret_cast<const float4 *>(F + (size_t)k * P.nxp);
-        const float4 *b = reinterpret_cast<const float4 *>(Fold + (size_t)k * P.nxp);
-        int q = l;
-        for (; q + 96 < nq; q += 128) {
-            const float4 x0 = __ldcg(a + q), x1 = __ldcg(a + q + 32), x2 = __ldcg(a + q + 64), x3 = __ldcg(a + q + 96);
-            const float4 y0 = __ldcg(b + q), y1 = __ldcg(b + q + 32), y2 = __ldcg(b + q + 64), y3 = __ldcg(b + q + 96);
-            piece(x0, y0, q);
-            piece(x1, y1, q + 32);
-            piece(x2, y2, q + 64);
-            piece(x3, y3, q + 96);
-        }
-        for (; q < nq; q += 32) piece(__ldcg(a + q), __ldcg(b + q), q);
-    }
-    double est = block_sum((double)part, sh);
+    double est = block_sum((double)acc, sh);
     if (threadIdx.x == 0) {
         int decision;  // 1 continue, 0 stop, 2 undecided
         if (est == 0.0) {
             decision = 0;
         } else {
-            // float additions in one thread's part: 4 per piece, (ny/W + 1)
-            // rows of nq/32 + 1 pieces
-            double per = 4.0 * (double)((P.ny / W + 1) * (nq / 32 + 1)) + 2.0;
-            double gam = ((double)n + per + 4.0) * 0x1p-24 + 0x1p-20;
+            // each change rounded once, then added: 2 roundings per term
+            double gam = ((double)n + 2.0 * terms + 4.0) * 0x1p-24 + 0x1p-20;
             double thr = (double)P.ttnorm * (double)n;
             if (est * (1.0 - gam) > thr * (1.0 + 0x1p-21)) decision = 1;
             else if (est * (1.0 + gam) < thr * (1.0 - 0x1p-21)) decision = 0;
@@ -1500,7 +1476,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             swept += 4;  // directional sweeps
             if (*w.abort_word) break;
             if (MODE == kModeReference) {
-                go = ref_continue(P, T, Told, sh);
+                go = ref_continue(P, T, Told, sh, acc, 4.0 * nbands * (P.nx + 1));
             } else {
                 double tot = block_sum((double)acc, sh);
                 go = (tot / (double)n) >= (double)P.ttnorm;
@@ -1761,7 +1737,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             // cell by more than 1e-6 of its value
             go = __syncthreads_or((int)moved) != 0;
         } else if (MODE == kModeReference) {
-            go = ref_continue(P, L, Told, sh);
+            go = ref_continue(P, L, Told, sh, acc, 4.0 * nbands * (P.nx + 1));
         } else {
             double tot = block_sum((double)acc, sh);
             go = (tot / (double)n) >= (double)P.ttnorm;
