@@ -682,12 +682,16 @@ RZ_DEV void sweep_barrier(const CtaShared &sh) {
 // mean|F-Fold| >= TTNORM, the mean being a sequential float sum in x-outer
 // order.  The estimate is the pass's own change: every update is
 // min(own, new), so a cell's changes over the pass's sweeps add up to
-// Fold - F, and each lane summed its cells' changes (`acc`; `terms`
-// bounds a lane's float additions, the per-sweep totals included).  It decides whenever it is certain;
-// within the worst-case rounding window of the sequential sum and of the
-// estimate the exact sequential sum is replayed from F and Fold (rare).
-RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold, const CtaShared &sh, float acc,
-                         double terms) {
+// Fold - F, and each lane summed its cells' changes (`acc`; `terms` bounds a
+// lane's float additions, the per-sweep totals included).  It decides
+// whenever it is certain; within the worst-case rounding window of the
+// sequential sum and of the estimate the exact sequential sum is replayed
+// from F and Fold (rare).  A first pass starts from the initial field, which
+// is not copied: with fold_ok false, rebuild(Fold) writes it (CTA-wide)
+// before a replay.
+template <class Rebuild>
+RZ_DEV bool ref_continue(const ShotParams &P, const float *F, float *Fold, const CtaShared &sh, float acc,
+                         double terms, bool fold_ok, Rebuild &&rebuild) {
     const int n = P.nx * P.ny;
     double est = block_sum((double)acc, sh);
     if (threadIdx.x == 0) {
@@ -702,22 +706,31 @@ RZ_DEV bool ref_continue(const ShotParams &P, const float *F, const float *Fold,
             else if (est * (1.0 + gam) < thr * (1.0 - 0x1p-21)) decision = 0;
             else decision = 2;
         }
-        if (decision == 2) {
-            float sum = 0.f;
-            for (int h = 0; h < P.nx; ++h)
-                for (int k = 0; k < P.ny; ++k) {
-                    size_t o = (size_t)k * P.nxp + h;
-                    float d = fabsf(__fsub_rn(__ldcg(F + o), __ldcg(Fold + o)));
-                    sum = __double2float_rn(__dadd_rn((double)sum, (double)d));
-                }
-            float l1 = __fdiv_rn(sum, __int2float_rn(n));
-            decision = (l1 >= P.ttnorm) ? 1 : 0;
-        }
         sh.ctl[0] = decision;
     }
     __syncthreads();
     int d = sh.ctl[0];
     __syncthreads();
+    if (d == 2) {
+        if (!fold_ok) {
+            rebuild(Fold);
+            __syncthreads();
+        }
+        if (threadIdx.x == 0) {
+            float sum = 0.f;
+            for (int h = 0; h < P.nx; ++h)
+                for (int k = 0; k < P.ny; ++k) {
+                    size_t o = (size_t)k * P.nxp + h;
+                    float dv = fabsf(__fsub_rn(__ldcg(F + o), __ldcg(Fold + o)));
+                    sum = __double2float_rn(__dadd_rn((double)sum, (double)dv));
+                }
+            float l1 = __fdiv_rn(sum, __int2float_rn(n));
+            sh.ctl[0] = (l1 >= P.ttnorm) ? 1 : 0;
+        }
+        __syncthreads();
+        d = sh.ctl[0];
+        __syncthreads();
+    }
     return d != 0;
 }
 
@@ -1006,6 +1019,17 @@ RZ_DEV void copy_field(const ShotParams &P, const float *src, float *dst) {
         __stcg(b + i + 3 * st, v3);
     }
     for (; i < n4; i += st) __stcg(b + i, __ldcg(a + i));
+}
+
+// the adjoint's initial field (init_travel_adj.c:44-57): 0 on the frame,
+// 10*TIME inside, the residuals at receiver cells (the receiver cells are
+// distinct, each with its last receiver)
+RZ_DEV void fill_field(const ShotParams &P, float *F, float v, bool frame0);
+RZ_DEV void fill_adjoint_start(const ShotParams &P, float *L, int z) {
+    fill_field(P, L, (float)(10.0 * (double)P.time), true);
+    __syncthreads();
+    for (int i = threadIdx.x; i < P.nrcell; i += blockDim.x)
+        L[(size_t)P.rcell_k[i] * P.nxp + P.rcell_h[i]] = P.Tres[(size_t)z * P.ntr + P.rcell_rec[i]];
 }
 
 // F := v on every padded row; with frame0 the frame (rows 0 and ny-1,
@@ -1459,7 +1483,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                 cta_err |= ERR_NOCONV_FWD;
                 break;
             }
-            if (MODE == kModeReference) {
+            if (MODE == kModeReference && pass > 0) {  // pass 0 starts from the initial field
                 copy_field(P, T, Told);
                 fence_proxy_async_global();
                 __syncthreads();
@@ -1476,7 +1500,11 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             swept += 4;  // directional sweeps
             if (*w.abort_word) break;
             if (MODE == kModeReference) {
-                go = ref_continue(P, T, Told, sh, acc, 4.0 * nbands * (P.nx + 1));
+                go = ref_continue(P, T, Told, sh, acc, 4.0 * nbands * (P.nx + 1), pass > 1, [&](float *F0) {
+                    fill_field(P, F0, tinit, false);
+                    __syncthreads();
+                    if (tid == 0) F0[(size_t)ks * P.nxp + hs] = 0.0f;
+                });
             } else {
                 double tot = block_sum((double)acc, sh);
                 go = (tot / (double)n) >= (double)P.ttnorm;
@@ -1647,11 +1675,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             const int per_warp = (items + Wb - 1) / Wb;
             relayout_items(P, w, pTld, min(items, g * per_warp), min(items, (g + 1) * per_warp), skew_dst_t(P, z));
         }
-        // lambda: 0 on the frame, 10*TIME inside, residuals at receiver cells
-        fill_field(P, L, (float)(10.0 * (double)P.time), true);
-        __syncthreads();
-        for (int i = tid; i < P.nrcell; i += blockDim.x)
-            L[(size_t)P.rcell_k[i] * P.nxp + P.rcell_h[i]] = P.Tres[(size_t)z * P.ntr + P.rcell_rec[i]];
+        fill_adjoint_start(P, L, z);
     }
     fence_proxy_async_global();
     __syncthreads();
@@ -1665,7 +1689,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             cta_err |= ERR_NOCONV_ADJ;
             break;
         }
-        if (MODE == kModeReference && !P.exact) {
+        if (MODE == kModeReference && !P.exact && pass > 0) {  // pass 0 starts from the initial field
             copy_field(P, L, Told);
             fence_proxy_async_global();
             __syncthreads();
@@ -1737,7 +1761,9 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             // cell by more than 1e-6 of its value
             go = __syncthreads_or((int)moved) != 0;
         } else if (MODE == kModeReference) {
-            go = ref_continue(P, L, Told, sh, acc, 4.0 * nbands * (P.nx + 1));
+            go = ref_continue(P, L, Told, sh, acc, 4.0 * nbands * (P.nx + 1), pass > 1, [&](float *F0) {
+                fill_adjoint_start(P, F0, z);
+            });
         } else {
             double tot = block_sum((double)acc, sh);
             go = (tot / (double)n) >= (double)P.ttnorm;

@@ -176,6 +176,78 @@ def test_eikonal_adj_tiny_lambda(R, scale):
     assert np.any(nz < (1e-26 if scale == 1e-29 else 1.1754944e-38))
 
 
+def _one_pass(p, fn, *args):
+    """The oracle's field after one pass (max_passes 1 ends it with a
+    no-convergence status, which is expected here)."""
+    lib = O._load_port()
+    q = O.Params(p.nx, p.ny, p.dh, p.time, p.ttnorm, p.eps_adj, 1)
+    return fn(lib, q, *args)
+
+
+def _norm1(new, old):
+    """norm1.c's mean change: |new - old| in float, added in x-outer order to
+    a float through double, divided by NX*NY in float."""
+    d = np.abs(new.astype(np.float32) - old.astype(np.float32)).T.ravel()
+    s = np.float32(0.0)
+    for v in d:
+        s = np.float32(np.float64(s) + np.float64(v))
+    return np.float32(s / np.float32(d.size))
+
+
+@pytest.mark.parametrize("phase", ["forward", "adjoint"])
+def test_stopping_rule_at_its_boundary_after_the_first_pass(R, phase):
+    """TTNORM equal to the first pass's mean change, and the next float above:
+    the reference continues at the first and stops at the second.  The GPU's
+    estimate cannot decide there, so it replays the exact sequential sum
+    against the pass's start field, which the first pass does not copy (it is
+    the initial field, rebuilt for the replay).  Fields and pass counts must
+    equal the oracle's at both values."""
+    w = synth.small_case(123, 80, 70, nshots=1)
+    p = params(w)
+    S = synth.slowness(w.vp_true)
+    sx, sz = w.srcx[0], w.srcz[0]
+    to, _ = O.eikonal(p, S, sx, sz)
+    Tmod = O.calc_fa(p, to, w.recx, w.recz)
+    Tres, _ = O.calc_res(p, to, Tmod, Tmod * np.float32(1.02), w.recx, w.recz)
+    if phase == "forward":
+        def fwd1(lib, q):
+            TT = np.empty(p.nx * p.ny, np.float32)
+            it = C.c_int(0)
+            lib.rzo_eikonal(C.byref(q.grid()), O._f32(S).reshape(-1), sx, sz, TT, C.byref(it))
+            return TT.reshape(p.ny, p.nx)
+        start = np.full((p.ny, p.nx), np.float32(2.0 * np.float64(np.float32(w.time))), np.float32)
+        start[int(np.floor(sz / w.dh + 0.5)) - 1, int(np.floor(sx / w.dh + 0.5)) - 1] = 0.0
+        l1 = _norm1(_one_pass(p, fwd1), start)
+    else:
+        def adj1(lib, q):
+            lam = np.empty(p.nx * p.ny, np.float32)
+            it = C.c_int(0)
+            rx, rz = O._i32(w.recx), O._i32(w.recz)
+            lib.rzo_eikonal_adj(C.byref(q.grid()), O._f32(to).reshape(-1), O._f32(Tres), len(rx), rx, rz, lam,
+                                C.byref(it))
+            return lam.reshape(p.ny, p.nx)
+        start = np.zeros((p.ny, p.nx), np.float32)
+        start[1:-1, 1:-1] = np.float32(10.0 * np.float64(np.float32(w.time)))
+        for i in range(len(w.recx)):
+            h, k = int(w.recx[i]) - 1, int(w.recz[i]) - 1
+            if 0 < h < p.nx - 1 and 0 < k < p.ny - 1:
+                start[k, h] = Tres[i]
+        l1 = _norm1(_one_pass(p, adj1), start)
+    passes = []
+    for tn in (l1, np.nextafter(l1, np.float32(np.inf))):
+        q = O.Params(p.nx, p.ny, p.dh, p.time, float(tn), p.eps_adj)
+        ctx = make_ctx(R, w, ttnorm=float(tn))
+        if phase == "forward":
+            got, _, pg = ctx.eikonal(sx, sz)
+            want, pw = O.eikonal(q, S, sx, sz)
+        else:
+            got, pg = ctx.eikonal_adj(to, Tres)
+            want, pw = O.eikonal_adj(q, to, Tres, w.recx, w.recz)
+        assert np.array_equal(got, want) and pg == pw
+        passes.append(pw)
+    assert passes[0] > passes[1] == 1  # the boundary is exactly at l1
+
+
 def test_batched_equals_single_shot(R):
     w = synth.small_case(5, 120, 90, nshots=5)
     ctx = make_ctx(R, w)
