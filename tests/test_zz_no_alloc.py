@@ -95,3 +95,51 @@ def test_noalloc_reports_invalid_slowness_and_no_convergence(gpu_lib):
              info_d.data_ptr(), None) == R.RZ_OK
     torch.cuda.synchronize()
     assert np.array_equal(TT_d.cpu().numpy(), TT_ref) and info_d.cpu().tolist() == [passes, 0]
+
+
+def test_noalloc_calls_capture_into_cuda_graphs(gpu_lib):
+    """After one warm call, two calls (two sources) are captured into two CUDA
+    graphs on a side stream; replays in either order give rz_eikonal's
+    traveltimes and pass counts bit for bit (the graphs share the static
+    array and replay one after the other on one stream)."""
+    import torch
+    R = gpu_lib
+    lib = R.load_library()
+    f = lib.rz_eikonal_noalloc
+    f.argtypes = [C.POINTER(_Grid), C.c_void_p, C.c_float, C.c_float, C.c_void_p, C.c_void_p, C.c_void_p]
+    f.restype = C.c_int
+
+    w = synth.small_case(4343, 200, 100, nshots=2)
+    S = synth.slowness(w.vp_true)
+    ctx = R.Context(0, "reference")
+    ctx.set_grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    ctx.set_slowness(S)
+    grid = _Grid(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj, 10000)
+    S_d = torch.from_numpy(S).cuda()
+    TT = [torch.empty((w.ny, w.nx), dtype=torch.float32, device="cuda") for _ in range(2)]
+    info = [torch.zeros(2, dtype=torch.int32, device="cuda") for _ in range(2)]
+    torch.cuda.synchronize()
+    assert f(C.byref(grid), S_d.data_ptr(), float(w.srcx[0]), float(w.srcz[0]), TT[0].data_ptr(),
+             info[0].data_ptr(), None) == R.RZ_OK  # warm call: the one-time set-up
+    torch.cuda.synchronize()
+
+    side = torch.cuda.Stream()
+    graphs = [torch.cuda.CUDAGraph() for _ in range(2)]
+    for i in range(2):
+        with torch.cuda.graph(graphs[i], stream=side):
+            st = f(C.byref(grid), S_d.data_ptr(), float(w.srcx[i]), float(w.srcz[i]), TT[i].data_ptr(),
+                   info[i].data_ptr(), C.c_void_p(torch.cuda.current_stream().cuda_stream))
+        assert st == R.RZ_OK
+    want = [ctx.eikonal(w.srcx[i], w.srcz[i]) for i in range(2)]
+    for order in ((1, 0), (0, 1)):
+        for i in range(2):
+            TT[i].fill_(-1.0)
+            info[i].fill_(-7)
+        for i in order:
+            graphs[i].replay()
+        torch.cuda.synchronize()
+        for i in range(2):
+            TT_ref, _, passes_ref = want[i]
+            assert np.array_equal(TT[i].cpu().numpy(), TT_ref)
+            got = info[i].cpu().numpy()
+            assert got[0] == passes_ref and got[1] == 0
