@@ -182,7 +182,7 @@ constexpr uint32_t kRingBytes = kRing * kSlotBytes;           // 12672
 // DIV: reference-mode adjoint only, whether the verified Markstein division by
 // DH may be used (P.div_fast); a compile-time choice keeps the unused
 // division path out of the step code
-template <int DX, int DY, bool ADJ, int MODE, int DIV = 1>
+template <int DX, int DY, bool ADJ, int MODE, int DIV = 1, bool RQS = false>
 __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mld, const CUtensorMap *mst,
                                    float &acc, float &mag, uint32_t &moved, int band, int W, const SweepSeq &seq) {
     // linear sweeps over weight streams: the exact discrete adjoint, mu = R +
@@ -330,6 +330,9 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     constexpr bool REC = !EX && (ADJ ? (DX < 0 && DY < 0) : (DX > 0 && DY < 0));
     uint8_t *const chg = (REC && P.chg) ? P.chg + (size_t)z * P.chg_stride + (size_t)s * ngroups : nullptr;
     const float *xline = xs - j;  // the 32-float line of step 0
+    constexpr bool RQ = EX && RQS;  // the second stream staged in a lent slot
+    const uint32_t sq = RQ ? smem_u32(&w.ws_all[W + g / 12].ring[0][0]) + 1024u * (uint32_t)(g % 12) : 0u;
+    const float *rline = RQ ? rs - j : nullptr;
     auto stage_issue = [&](int G) {
         const uint32_t dst = sg;
 #pragma unroll
@@ -341,6 +344,13 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
         if (ADJ && l >= 2 && l < 5)
             cp_async16(dst + kStageEdge + 16u * (uint32_t)l, ewin31 + (DX > 0 ? 8 * G : -8 * G) + 4 * (l - 2));
         if (ADJ && !EX && l < 8) cp_async4(dst + kStageMask + 4u * (uint32_t)l, mk + QS * (8 * G + l));
+        if (RQ) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int c = l + 32 * h, line = c >> 3, piece = c & 7;
+                cp_async16(sq + 16u * (uint32_t)c, rline + QS * 32 * (8 * G + line) + 4 * piece);
+            }
+        }
         cp_async_commit();
     };
 
@@ -350,7 +360,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     float rq[8];
 #pragma unroll
     for (int i = 0; i < 8; ++i)
-        if (EX) rq[i] = __ldca(rs + QS * 32 * i);
+        if (EX && !RQ) rq[i] = __ldca(rs + QS * 32 * i);
     stage_issue(0);
     float c_tt = 0.f, w_tt = 0.f;  // exact adjoint: x weights of this and the previous column
     float c_wz = 0.f, w_wz = 0.f;  // exact adjoint: z weights of this and the previous column
@@ -474,6 +484,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                         eq[ii] = lds(sg + kStageEdge + 4u * (uint32_t)ei);
                     }
                     if (ADJ && !EX) mq[ii] = lds_u32(sg + kStageMask + 4u * (uint32_t)ii);
+                    if (RQ) rq[ii] = lds(sq + 128u * (uint32_t)ii + 4u * (uint32_t)j);
                 }
                 __syncwarp();  // every lane has read the slot: refill it
                 if (G + 1 < ngroups) stage_issue(G + 1);
@@ -539,7 +550,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                     float e_wx, e_wz;  // weights of the cell one column downstream
                     unpack_weights(xv, e_wx, e_wz);
                     const float rcell = rq[ii];
-                    rq[ii] = __ldca(rr + QS * 32 * (ii + 8));
+                    if (!RQ) rq[ii] = __ldca(rr + QS * 32 * (ii + 8));
                     const float edge = eq[ii];
                     float n_wz = __shfl_up_sync(0xffffffffu, w_wz, 1);
                     float s_wz = __shfl_down_sync(0xffffffffu, e_wz, 1);
@@ -632,6 +643,7 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     }
     tma_store_wait_all<0>();
     fence_proxy_async_global();
+    if (RQ) fence_proxy_async_smem();  // the lent slot's copies precede later tensor copies into that ring
     __syncwarp();
     if (pipe && l == 0) st_release_smem(w.done + g, seq.n + 1);
     w.phase = phase;
@@ -1413,6 +1425,21 @@ RZ_DEV void init_cta(const CtaShared &sh, int Wb, bool reinit) {
     __syncthreads();
 }
 
+// the linear sweeps stage their second stream when the CTA has enough warps
+// that do not sweep (each lends 12 slots of its ring)
+template <int DX, int DY, bool ADJ, int MODE, int DIV>
+__device__ __forceinline__ void sweep_dispatch(const ShotParams &P, Warp &w, const CUtensorMap *mld,
+                                               const CUtensorMap *mst, float &acc, float &mag, uint32_t &moved,
+                                               int band, int W, const SweepSeq &seq) {
+    if constexpr (ADJ && (MODE == kModeExact || MODE == kModeTangent)) {
+        if (((int)(blockDim.x >> 5) - W) * 12 >= W) {
+            sweep<DX, DY, ADJ, MODE, DIV, true>(P, w, mld, mst, acc, mag, moved, band, W, seq);
+            return;
+        }
+    }
+    sweep<DX, DY, ADJ, MODE, DIV, false>(P, w, mld, mst, acc, mag, moved, band, W, seq);
+}
+
 // One shot (forward, residuals, adjoint) by a CTA whose warps 0..Wg-1 take
 // the strips (further warps of the CTA only join its barriers and the
 // cell-parallel loops).
@@ -1459,7 +1486,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
 #define RZ_SWEEP_D(DX_, DY_, ADJ_, MODE_, DIV_, LD_, ST_)                           \
     do {                                                                           \
         for (int b = 0; b < nbands; ++b) {                                         \
-            sweep<DX_, DY_, ADJ_, MODE_, DIV_>(P, w, LD_, ST_, acc, mag, moved, b, W, seq); \
+            sweep_dispatch<DX_, DY_, ADJ_, MODE_, DIV_>(P, w, LD_, ST_, acc, mag, moved, b, W, seq); \
             if (!seq.pipelined) sweep_barrier(sh);                                 \
         }                                                                          \
         seq.advance(DY_);                                                          \
