@@ -61,6 +61,7 @@ struct alignas(128) WarpShared {
 };
 static_assert(sizeof(WarpShared) % 128 == 0, "TMA destinations need 128-byte alignment");
 static_assert(offsetof(WarpShared, hb) == sizeof(float) * kRing * kSlotFloats, "hb follows the ring");
+static_assert(12 * 1024 <= sizeof(float) * kRing * kSlotFloats, "a ring lends 12 one-KB stage slots");
 static_assert(offsetof(WarpShared, stage) == offsetof(WarpShared, hb) + sizeof(float) * kHandoff &&
                   offsetof(WarpShared, stage) % 16 == 0,
               "the stage slot follows hb, 16-byte aligned");
@@ -330,7 +331,14 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     constexpr bool REC = !EX && (ADJ ? (DX < 0 && DY < 0) : (DX > 0 && DY < 0));
     uint8_t *const chg = (REC && P.chg) ? P.chg + (size_t)z * P.chg_stride + (size_t)s * ngroups : nullptr;
     const float *xline = xs - j;  // the 32-float line of step 0
-    constexpr bool RQ = EX && RQS;  // the second stream staged in a lent slot
+    // RQS (linear sweeps): the second stream (receiver terms or residuals) is
+    // staged like the first, group by group, in a 1 KB slot that a warp which
+    // does not sweep lends from its ring (warp W + g/12, slot g%12; its
+    // barriers are not touched, and no phase that uses that ring overlaps the
+    // sweeps).  Without RQS the stream is read through registers 8 steps
+    // ahead, which leaves the loads' latency exposed (the exact adjoint's
+    // sweeps run 25% longer).  sweep_dispatch chooses.
+    constexpr bool RQ = EX && RQS;
     const uint32_t sq = RQ ? smem_u32(&w.ws_all[W + g / 12].ring[0][0]) + 1024u * (uint32_t)(g % 12) : 0u;
     const float *rline = RQ ? rs - j : nullptr;
     auto stage_issue = [&](int G) {
@@ -1425,8 +1433,10 @@ RZ_DEV void init_cta(const CtaShared &sh, int Wb, bool reinit) {
     __syncthreads();
 }
 
-// the linear sweeps stage their second stream when the CTA has enough warps
-// that do not sweep (each lends 12 slots of its ring)
+// The linear sweeps stage their second stream (RQS) when the CTA has enough
+// warps that do not sweep (each lends 12 one-KB slots of its 12.4 KB ring);
+// each choice is its own instantiation, so neither carries the other's
+// registers.
 template <int DX, int DY, bool ADJ, int MODE, int DIV>
 __device__ __forceinline__ void sweep_dispatch(const ShotParams &P, Warp &w, const CUtensorMap *mld,
                                                const CUtensorMap *mst, float &acc, float &mag, uint32_t &moved,
