@@ -185,7 +185,7 @@ constexpr uint32_t kRingBytes = kRing * kSlotBytes;           // 12672
 // division path out of the step code
 template <int DX, int DY, bool ADJ, int MODE, int DIV = 1, bool RQS = false>
 __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorMap *mld, const CUtensorMap *mst,
-                                   float &acc, float &mag, uint32_t &moved, int band, int W, const SweepSeq &seq) {
+                                   float &acc, uint32_t &moved, int band, int W, const SweepSeq &seq) {
     // linear sweeps over weight streams: the exact discrete adjoint, mu = R +
     // the weights neighbours put on this cell; the traveltime refinement (TAN),
     // delta = r + this cell's weights on its upwind neighbours
@@ -270,11 +270,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     uint32_t phase = w.phase;
     int err = 0;
     float acc_l = 0.f;  // sum of the changes (the stopping rule; the caller's acc lives in local memory)
-    // linear sweeps: sum of |value| over the sweep, returned in mag.  No
-    // stopping rule reads it, but with it the compiler schedules the linear
-    // step differently and the exact sweeps run faster (GB300, 100-shot
-    // 1700 x 350 exact-gradient step: 5.53 ms with it, 6.02 ms without)
-    float mag_l = 0.f;
     uint32_t moved_l = 0;  // linear sweeps: this lane moved a cell by more than 1e-6 of its value
     auto ring_wait_l = [&](int slot) {
         if (!mbar_wait_copy(mbar_s + 8u * slot, (phase >> slot) & 1u)) err |= ERR_TMA_TIMEOUT;
@@ -582,7 +577,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                         m = wzS < 0.f ? fmaf(-wzS, lS, m) : m;
                     }
                     r = valid ? m : own;
-                    mag_l += valid ? fabsf(r) : 0.0f;
                     w_tt = c_tt;
                     c_tt = e_wx;
                     w_wz = c_wz;
@@ -657,7 +651,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
     w.phase = phase;
     w.err |= err;
     acc += acc_l;
-    mag += mag_l;
     moved |= moved_l;
 }
 
@@ -1439,15 +1432,15 @@ RZ_DEV void init_cta(const CtaShared &sh, int Wb, bool reinit) {
 // registers.
 template <int DX, int DY, bool ADJ, int MODE, int DIV>
 __device__ __forceinline__ void sweep_dispatch(const ShotParams &P, Warp &w, const CUtensorMap *mld,
-                                               const CUtensorMap *mst, float &acc, float &mag, uint32_t &moved,
-                                               int band, int W, const SweepSeq &seq) {
+                                               const CUtensorMap *mst, float &acc, uint32_t &moved, int band, int W,
+                                               const SweepSeq &seq) {
     if constexpr (ADJ && (MODE == kModeExact || MODE == kModeTangent)) {
         if (((int)(blockDim.x >> 5) - W) * 12 >= W) {
-            sweep<DX, DY, ADJ, MODE, DIV, true>(P, w, mld, mst, acc, mag, moved, band, W, seq);
+            sweep<DX, DY, ADJ, MODE, DIV, true>(P, w, mld, mst, acc, moved, band, W, seq);
             return;
         }
     }
-    sweep<DX, DY, ADJ, MODE, DIV, false>(P, w, mld, mst, acc, mag, moved, band, W, seq);
+    sweep<DX, DY, ADJ, MODE, DIV, false>(P, w, mld, mst, acc, moved, band, W, seq);
 }
 
 // One shot (forward, residuals, adjoint) by a CTA whose warps 0..Wg-1 take
@@ -1496,7 +1489,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
 #define RZ_SWEEP_D(DX_, DY_, ADJ_, MODE_, DIV_, LD_, ST_)                           \
     do {                                                                           \
         for (int b = 0; b < nbands; ++b) {                                         \
-            sweep_dispatch<DX_, DY_, ADJ_, MODE_, DIV_>(P, w, LD_, ST_, acc, mag, moved, b, W, seq); \
+            sweep_dispatch<DX_, DY_, ADJ_, MODE_, DIV_>(P, w, LD_, ST_, acc, moved, b, W, seq); \
             if (!seq.pipelined) sweep_barrier(sh);                                 \
         }                                                                          \
         seq.advance(DY_);                                                          \
@@ -1525,7 +1518,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                 fence_proxy_async_global();
                 __syncthreads();
             }
-            float acc = 0.f, mag = 0.f;
+            float acc = 0.f;
             uint32_t moved = 0;
             RZ_SWEEP(+1, +1, false, MODE, pTld, &M.tst);
             if (pass == 0) stamp(P, z, 5);
@@ -1576,7 +1569,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
                     cta_err |= ERR_NOCONV_FWD;
                     break;
                 }
-                float acc = 0.f, mag = 0.f;
+                float acc = 0.f;
                 uint32_t moved = 0;
                 // whether the sweep (or pass) just run moved no cell by more
                 // than 1e-6 of its value (a CTA-wide vote, with the barrier)
@@ -1731,7 +1724,7 @@ __device__ __forceinline__ void run_shot(const ShotParams &P, const ShotMaps &M,
             fence_proxy_async_global();
             __syncthreads();
         }
-        float acc = 0.f, mag = 0.f;
+        float acc = 0.f;
         uint32_t moved = 0;
         bool sweep_stop = false;  // exact adjoint: a sweep of a later pass moved no cell by > 1e-6 of its value
         int nsweeps = 4;          // sweeps this pass runs
