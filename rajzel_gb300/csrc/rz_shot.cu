@@ -517,7 +517,6 @@ __device__ __noinline__ void sweep(const ShotParams &P, Warp &w, const CUtensorM
                                       (m == kRing - 1 ? kRingBytes : 0u);
 #pragma unroll
             for (int ii = 0; ii < 8; ++ii) {
-                const int t = t0 + ii;
                 const int up = u0 + ii;
                 const float own = own_next;
                 const float ev = ev_next;
