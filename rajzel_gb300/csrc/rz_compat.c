@@ -21,6 +21,9 @@
 #endif
 
 #define RZ_STRING_SIZE 74 /* STRING_SIZE of fd.h:25 */
+/* a snapshot name: SNAP_FILE, "_shot_", the shot number and ".tt" (the
+   reference formats it into STRING_SIZE bytes, which a long SNAP_FILE overruns) */
+#define RZ_SNAP_NAME (RZ_STRING_SIZE + 24)
 
 /* the reference's globals (globvar.h) and helpers (util.c, writemod.c, write_picks.c) */
 extern float DH, TIME, TTNORM, EPS_ADJ;
@@ -116,7 +119,7 @@ void eikonal(float **S, float **TT, float *Tmod, float **srcpos, int ishot, int 
     int st = rz_eikonal(g_ctx, srcpos[1][ishot], srcpos[2][ishot], &TT[1][1], ntr > 0 ? &Tmod[1] : NULL, NULL, 0);
     if (st) fail("rz_eikonal", st);
     if (SNAP == 1) {
-        char filename[RZ_STRING_SIZE];
+        char filename[RZ_SNAP_NAME];
         snprintf(filename, sizeof filename, "%s_shot_%d.tt", SNAP_FILE, ishot);
         writemod(filename, TT, 3);
     }
@@ -162,7 +165,7 @@ void forward(float **S, float **TT, float *Tmod, float **srcpos, int nshots, int
             const int ishot = first + s;
             for (int i = 0; i < ntr; i++) Tmod[i + 1] = tm[(size_t)s * ntr + i];
             if (SNAP == 1) {
-                char filename[RZ_STRING_SIZE];
+                char filename[RZ_SNAP_NAME];
                 memcpy(&TT[1][1], tt + (size_t)s * cells, sizeof(float) * cells);
                 snprintf(filename, sizeof filename, "%s_shot_%d.tt", SNAP_FILE, ishot);
                 writemod(filename, TT, 3);
