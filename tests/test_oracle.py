@@ -112,6 +112,29 @@ def test_fp64_oracle_close_to_float(oracle_mod):
     assert np.abs(t32 - t64).max() / np.abs(t64).max() < 1e-5
 
 
+def test_ttnorm_iterate_and_fixpoint_differ_on_rough_models(oracle_mod):
+    """The FP64 oracle stopped by TTNORM (a mean change of 1e-6 s per pass) is
+    not the fixpoint of the discrete equations on a rough random model with
+    interior sources: on 70 x 600 it stops after 8-9 passes, 1.7e-5 (relative,
+    max norm) from the fixpoint that 19-22 passes reach, because single cells
+    still moving by ~1e-6 s vanish in the grid mean.  Refined traveltimes
+    approximate the fixpoint, so their error check runs the FP64 forward to
+    it."""
+    O = oracle_mod
+    w = synth.small_case(770, 70, 600, nshots=3)
+    S = synth.slowness(w.vp_true).astype(np.float64)
+    stop = O.Params(w.nx, w.ny, w.dh, w.time, w.ttnorm, w.eps_adj)
+    fix = O.Params(w.nx, w.ny, w.dh, w.time, 1e-30, w.eps_adj)
+    diffs, passes = [], []
+    for i in range(3):
+        ta, pa = O.eikonal_f64(stop, S, w.srcx[i], w.srcz[i])
+        tb, pb = O.eikonal_f64(fix, S, w.srcx[i], w.srcz[i])
+        diffs.append(np.abs(ta - tb).max() / np.abs(tb).max())
+        passes.append((pa, pb))
+    assert max(diffs) > 1e-5 and min(diffs) > 1e-6
+    assert all(pb > 2 * pa for pa, pb in passes)
+
+
 def test_pow_cube_pin(oracle_mod):
     """ass_grad.c:23 uses libm pow(S,3.0); it is faithful but not always the
     correctly rounded cube, which is why the reference-mode GPU stack takes
